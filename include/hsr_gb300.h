@@ -1,0 +1,211 @@
+/*
+ * hsr_gb300.h — C ABI of the GB300 radar path-tracing backend.
+ *
+ * This library replaces libhussar's two ray-tracing backends:
+ *   - cpu::Backend (Embree), libhussar/include/hussar/arch/cpu.h:17-63, src/arch/cpu.cpp:32-87
+ *   - gpu::Backend (OptiX),  libhussar/include/hussar/arch/gpu.h:17-47, src/arch/gpu.cpp:482-532
+ * together with the integrator they run, PathTracer::sample
+ * (libhussar/include/hussar/integrators/path.h:235-451), and the frame splat it feeds
+ * (libradar/include/radar/radar.h:564-626).
+ *
+ * Everything is plain C: POD structs, pointers and sizes. No exceptions cross this
+ * boundary; every call returns an hsr_status and hsr_last_error() gives the message
+ * of the last failure on the calling thread. The reference reports the same failures
+ * by throwing sutil::Exception (src/arch/gpu/host/sutil/Exception.h:91-191) or by
+ * Log(EError) + exit(-1) (core/logging.h:43-46).
+ *
+ * Device: one NVIDIA GB300 (sm_103a). There is no CPU fallback: without a usable GPU
+ * every entry point that computes returns HSR_ERR_NO_DEVICE.
+ */
+#ifndef HSR_GB300_H
+#define HSR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HSR_ABI_VERSION 1
+
+typedef enum hsr_status {
+    HSR_OK = 0,
+    HSR_ERR_INVALID_ARGUMENT = 1,  /* bad pointer, size or configuration */
+    HSR_ERR_CUDA = 2,              /* a CUDA runtime call failed */
+    HSR_ERR_OUT_OF_MEMORY = 3,     /* device allocation failed */
+    HSR_ERR_INTERRUPTED = 4,       /* the caller's interrupt flag was set */
+    HSR_ERR_DEVICE = 5,            /* a kernel reported an error in its device status word */
+    HSR_ERR_NOT_SUPPORTED = 6,     /* a flag combination this backend does not implement */
+    HSR_ERR_NO_DEVICE = 7          /* no CUDA device is visible */
+} hsr_status;
+
+/* FMCW ramp parameters; field-for-field radar::RFConfig (libradar/include/radar/radar.h:113-136).
+ * Units: Hz, Hz/s, Hz, s, s, s. */
+typedef struct hsr_rf_config {
+    float startFreq;
+    float freqSlope;
+    float adcRate;
+    float idleTime;
+    float rampTime;
+    float antennaDelay;
+} hsr_rf_config;
+
+/* Radar cube shape; radar::FrameConfig (libradar/include/radar/radar.h:141-164).
+ * The cube is stored [chirp][sample][channel] (radar.h:487-494). */
+typedef struct hsr_frame_config {
+    int32_t chirpCount;
+    int32_t samplesPerChirp;
+    int32_t channelCount;
+} hsr_frame_config;
+
+/* A point antenna with the AWR1243 radiation pattern; hussar::NFAntenna
+ * (libhussar/include/hussar/core/emitter.h:159-214). rotation is the 3x3 matrix
+ * m_rotation in row-major order (rotation[3*row + col]); its third column is the
+ * boresight direction. */
+typedef struct hsr_antenna {
+    float position[3];
+    float rotation[9];
+} hsr_antenna;
+
+/* PathTracer's public configuration members (libhussar/include/hussar/integrators/path.h:153-169)
+ * plus Integrator::produceDebugImage (core/integrator.h:58), which in the reference also
+ * turns off the zero-contribution early-out of Integrator::splat (integrator.h:121-124).
+ * Booleans are 0/1. */
+typedef struct hsr_tracer_flags {
+    int32_t onlyIndirect;
+    int32_t maxDepth;
+    int32_t useGeometricalOptics;
+    int32_t poDiffraction;
+    int32_t doGuiding;
+    int32_t clearBeforeIteration;
+    int32_t correctPhase;
+    int32_t filterGuiding;
+    int32_t doFiltering;
+    int32_t filteringSphere;
+    int32_t produceDebugImage;
+    float filteringMin;
+    float filteringMax;
+    float filteringRadius;
+} hsr_tracer_flags;
+
+/* How the path phase and range bin are evaluated.
+ *  HSR_PHASE_REFERENCE_FP32: the reference's own single-precision expression
+ *      2*Pi*(f0 - dt*S/2)*dt (core/integrator.h:107-110) and bin N*frac(dt*S/adcRate)
+ *      (radar.h:232-241). This is the parity mode.
+ *  HSR_PHASE_SPLIT_FP64: the path length is carried in FP64; phase cycles and bin are
+ *      reduced modulo one in FP64, the trig is FP32. */
+typedef enum hsr_phase_mode {
+    HSR_PHASE_REFERENCE_FP32 = 0,
+    HSR_PHASE_SPLIT_FP64 = 1
+} hsr_phase_mode;
+
+/* How each next-event contribution reaches the range bins.
+ *  HSR_SPLAT_DIRICHLET16: radar::Frame::splat<16> (radar.h:564-626): 33 bins of the
+ *      truncated sinc kernel per contribution. This is the parity mode.
+ *  HSR_SPLAT_FINE_SYNTH: contributions go to a fine complex range histogram with
+ *      moment correction; a complex histogram x twiddle GEMM on the tensor cores then
+ *      synthesises the exact (untruncated) spectrum. */
+typedef enum hsr_splat_mode {
+    HSR_SPLAT_DIRICHLET16 = 0,
+    HSR_SPLAT_FINE_SYNTH = 1
+} hsr_splat_mode;
+
+typedef struct hsr_scene hsr_scene;   /* resident triangle mesh + device BVH */
+
+/* Library / device information. */
+int32_t hsr_abi_version(void);
+const char *hsr_last_error(void);
+/* Number of kernel launches this library has issued in the calling process. */
+int64_t hsr_launch_count(void);
+
+/* Fills default PathTracer flags exactly as the reference initialises them
+ * (path.h:153-169: onlyIndirect=1, maxDepth=10, useGeometricalOptics=1,
+ * poDiffraction=0, doGuiding=1, clearBeforeIteration=1, correctPhase=0,
+ * filterGuiding=1, doFiltering=1, filteringSphere=1, filteringMin=600,
+ * filteringMax=900, filteringRadius=160; produceDebugImage=0). */
+void hsr_default_flags(hsr_tracer_flags *flags);
+
+/* Builds a resident scene from a triangle mesh: the device BVH is built once here.
+ * Replaces the Backend constructors Backend(const TriangleMesh&, Integrator&)
+ * (arch/cpu.h:18-20 -> src/arch/cpu.cpp:32-47 rtcCommitScene; arch/gpu.h:18-20 ->
+ * src/arch/gpu.cpp:482-493 buildMeshAccel). vertices: vertex_count x 3 floats
+ * (TriangleMesh::vertexBuffer, core/mesh.h:27); indices: triangle_count x 3 int32
+ * (TriangleMesh::indexBuffer, core/mesh.h:28). The caller's arrays may be freed after
+ * the call returns (the reference copies them too, src/arch/cpu.cpp:36-40). */
+hsr_status hsr_scene_create(const float *vertices, int64_t vertex_count,
+                            const int32_t *indices, int64_t triangle_count,
+                            hsr_scene **out_scene);
+hsr_status hsr_scene_destroy(hsr_scene *scene);
+/* Device bytes held by the scene (vertices, triangles, BVH nodes). */
+hsr_status hsr_scene_footprint(const hsr_scene *scene, int64_t *out_bytes);
+/* BVH statistics for tests: node count, maximum depth, leaf count. */
+hsr_status hsr_scene_bvh_stats(const hsr_scene *scene, int64_t *out_nodes,
+                               int32_t *out_max_depth, int64_t *out_leaves);
+
+/* Closest-hit and occlusion queries over a batch of rays (host arrays), the two RT
+ * callbacks of the reference backends: RT::intersect (src/arch/cpu.cpp:63-87,
+ * src/arch/gpu/device/kernel.cu:45-63,76-98) and RT::visible (cpu.cpp:53-61,
+ * kernel.cu:24-43). Rays start at tnear = 5e-5 (hussar.h:52, cpu.cpp:12).
+ * origins/directions: count x 3 floats; tfar: count floats.
+ * Outputs: t (inf on miss), hit point p (count x 3), faceforwarded unit normal n
+ * (count x 3), primitive id (-1 on miss) / visible flags (1 = unoccluded). */
+hsr_status hsr_intersect(const hsr_scene *scene, int64_t count, const float *origins,
+                         const float *directions, const float *tfar, float *out_t,
+                         float *out_p, float *out_n, int32_t *out_prim);
+hsr_status hsr_visible(const hsr_scene *scene, int64_t count, const float *origins,
+                       const float *directions, const float *tfar, int32_t *out_visible);
+
+/* One Backend::run call (arch/cpu.h:44-46, arch/gpu.h:26-32) for the plain (unguided)
+ * PathTracer: traces samples index_offset + [0, budget) of the Halton sequence
+ * (path.h:237-238) and ADDS each sample's splats, scaled by sample_weight
+ * (PathTracer::currentSampleWeight, path.h:242), into frame_inout, and
+ * budget*sample_weight into *total_weight_inout (path.h:445, 466-475).
+ * frame_inout: host array of chirpCount*samplesPerChirp*channelCount complex64
+ * values, interleaved (re, im), layout [chirp][sample][channel].
+ * interrupt_flag: optional; when it is non-zero at entry the call returns
+ * HSR_ERR_INTERRUPTED without work (the reference polls it per 256-sample batch,
+ * arch/cpu.h:25). Synchronous. doGuiding must be 0 here (use hsr_path_tracer_run). */
+hsr_status hsr_backend_run(const hsr_scene *scene, const hsr_rf_config *rf,
+                           const hsr_frame_config *frame, const hsr_antenna *tx,
+                           const hsr_antenna *rx, const hsr_tracer_flags *flags,
+                           int64_t budget, int64_t index_offset, float sample_weight,
+                           int32_t phase_mode, float *frame_inout,
+                           double *total_weight_inout, const volatile int32_t *interrupt_flag);
+
+/* Batched simulation: pose_count independent sensor poses (tx[i], rx[i]) with their
+ * own sample budgets, all traced by ONE persistent launch on `stream`
+ * (a cudaStream_t, or NULL for the legacy default stream).
+ * Each pose p traces Halton indices index_offset[p] + [0, budget[p]).
+ * Output (DEVICE pointer): out_rows[p*samplesPerChirp + k] = the normalised
+ * frame row (chirp 0, channel 0) of pose p, i.e. fetchFrame() (path.h:453-455)
+ * restricted to the only row the reference writes (velocity 0, path.h:130; one RX
+ * channel, path.h:291-292); complex64 interleaved.
+ * All pointer arguments are DEVICE pointers (inputs already resident). Asynchronous
+ * on `stream`; scratch is owned by the scene and reused across calls on it, so calls
+ * on one scene must not overlap. */
+hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
+                                     int32_t samples_per_chirp, const hsr_tracer_flags *flags,
+                                     int32_t pose_count, const hsr_antenna *d_tx,
+                                     const hsr_antenna *d_rx, const int64_t *d_budget,
+                                     const int64_t *d_index_offset, int32_t phase_mode,
+                                     int32_t splat_mode, float *d_out_rows, void *stream);
+
+/* As hsr_simulate_batch_device, with HOST inputs and outputs: copies poses and budgets
+ * in, runs, copies the rows out and synchronises. */
+hsr_status hsr_simulate_batch(hsr_scene *scene, const hsr_rf_config *rf,
+                              int32_t samples_per_chirp, const hsr_tracer_flags *flags,
+                              int32_t pose_count, const hsr_antenna *tx,
+                              const hsr_antenna *rx, const int64_t *budget,
+                              const int64_t *index_offset, int32_t phase_mode,
+                              int32_t splat_mode, float *out_rows, void *stream);
+
+/* Timing of the most recent batch launch on this scene: device milliseconds of the
+ * trace kernel alone, measured with CUDA events on the launching stream. */
+hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HSR_GB300_H */

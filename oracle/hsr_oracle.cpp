@@ -1,0 +1,1149 @@
+/*
+ * ORACLE — TEST INFRASTRUCTURE ONLY.
+ *
+ * A CPU restatement of libhussar's plain (unguided) radar path tracer, used only by
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker
+ * and the timed CPU reference. The product (hussar_gb300/, libhsr_gb300.so) never
+ * links, loads or calls anything in this directory.
+ *
+ * What it restates (file:line within the reference project):
+ *   - HaltonSampler / radicalInverse<base>   libhussar/include/hussar/samplers/halton.h:11-67
+ *   - UniformSampleSphere, UniformSpherePdf  libhussar/include/hussar/core/sampling.h:38-47
+ *   - AWRAngularDistribution, NFAntenna      libhussar/include/hussar/core/emitter.h:109-214
+ *   - SurfaceEmitter                         libhussar/include/hussar/core/emitter.h:53-82
+ *   - Ray, Intersection                      libhussar/include/hussar/core/geometry.h:69-143,
+ *                                            libhussar/include/hussar/core/intersection.h:16-57
+ *   - PathTracer::sample                     libhussar/include/hussar/integrators/path.h:235-451
+ *   - Integrator::measureRay/splat/reflect   libhussar/include/hussar/core/integrator.h:107-168
+ *   - Frame::PIndex::setTime/setVelocity     libradar/include/radar/radar.h:232-251
+ *   - Frame::splat<16>                       libradar/include/radar/radar.h:564-626
+ *   - host atomicAdd(float*) (CAS loop)      libradar/include/radar/radar.h:63-83
+ *   - cpu::Backend::run batch scheduler      libhussar/include/hussar/arch/cpu.h:18-46
+ *   - Embree hit semantics (tnear=Epsilon, faceforwarded normalised Ng)
+ *                                            libhussar/src/arch/cpu.cpp:9-87
+ *
+ * Precision: templated on Real. Real=float follows the reference's single-precision
+ * expression order (including the places where the reference widens to double:
+ * std::pow in the AWR pattern, cos/sin in radar::polar, M_PI in Frame::splat).
+ * Real=double is the FP64 oracle: the same estimator, every operation in double.
+ *
+ * Eigen (absent from this container) fixes some operation orders in the reference;
+ * they are restated here as Eigen documents/implements them:
+ *   - a.dot(b) for complex a is sum(conj(a_i) * b_i)          (geometry.h:138)
+ *   - 3-term reductions (dot, squaredNorm, 3x3 mat-vec rows) are x0 + (x1 + x2)
+ *   - v.normalized() is v / sqrt(squaredNorm)
+ *   - cross() of complex vectors conjugates the result
+ * Embree (absent) is replaced by a binned-SAH BVH with a Moller-Trumbore triangle
+ * test; hits are accepted for tnear < t <= tfar, equal-t ties go to the lower
+ * primitive id. Parity with Embree/OptiX/Eigen themselves is unpinned.
+ *
+ * Build: oracle/Makefile (g++ -O3 -ffp-contract=off, no -march: the same bits on
+ * x86-64 and aarch64).
+ */
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "hsr_oracle.h"
+
+namespace oracle {
+
+// ----------------------------------------------------------------------------------
+// Constants (hussar.h:37-52, radar.h:107)
+// ----------------------------------------------------------------------------------
+template <typename R> struct Consts;
+template <> struct Consts<float> {
+    static constexpr float Pi = 3.14159265358979323846f;
+    static constexpr float Inv4Pi = 0.07957747154594766788f;
+    static constexpr float SpeedOfLight = 299792458.f;  // radar.h:107 (float)
+    static constexpr float Epsilon = 5e-5f;             // hussar.h:52
+};
+template <> struct Consts<double> {
+    static constexpr double Pi = 3.14159265358979323846;
+    static constexpr double Inv4Pi = 0.07957747154594766788;
+    static constexpr double SpeedOfLight = 299792458.0;
+    static constexpr double Epsilon = 5e-5;
+};
+
+template <typename R> struct V3 {
+    R x, y, z;
+};
+template <typename R> struct Cx {
+    R re, im;
+};
+template <typename R> struct CV3 {
+    Cx<R> c[3];
+};
+
+template <typename R> static inline V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <typename R> static inline V3<R> add(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename R> static inline V3<R> sub(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename R> static inline V3<R> scale(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <typename R> static inline V3<R> neg(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+// Eigen redux order for 3 terms: x0 + (x1 + x2)
+template <typename R> static inline R dot(V3<R> a, V3<R> b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+template <typename R> static inline R sqnorm(V3<R> a) { return a.x * a.x + (a.y * a.y + a.z * a.z); }
+template <typename R> static inline R norm(V3<R> a) { return std::sqrt(sqnorm(a)); }
+template <typename R> static inline V3<R> cross(V3<R> a, V3<R> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename R> static inline V3<R> normalized(V3<R> a) {
+    R n = sqnorm(a);
+    if (n > R(0)) {
+        R s = std::sqrt(n);
+        return {a.x / s, a.y / s, a.z / s};
+    }
+    return a;
+}
+template <typename R> static inline V3<R> divs(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
+
+// complex (libradar/include/radar/complex.h)
+template <typename R> static inline Cx<R> cadd(Cx<R> a, Cx<R> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename R> static inline Cx<R> csub(Cx<R> a, Cx<R> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename R> static inline Cx<R> cmul(Cx<R> a, Cx<R> b) {  // complex.h:56-61
+    R r = a.re * b.re - a.im * b.im;
+    R i = a.re * b.im + a.im * b.re;
+    return {r, i};
+}
+template <typename R> static inline Cx<R> cscale(Cx<R> a, R s) { return {a.re * s, a.im * s}; }  // complex.h:48-52
+template <typename R> static inline Cx<R> cdivs(Cx<R> a, R s) { return {a.re / s, a.im / s}; }   // complex.h:69-73
+template <typename R> static inline Cx<R> cconj(Cx<R> a) { return {a.re, -a.im}; }
+// radar::polar(1, angle) with the reference's unqualified cos/sin (complex.h:184-187),
+// which resolve to ::cos(double)/::sin(double) for a float angle.
+template <typename R> static inline Cx<R> cexpj(R angle) {
+    double a = double(angle);
+    return {R(std::cos(a)), R(std::sin(a))};
+}
+// std::abs(radar::complex) (complex.h:225-237)
+template <typename R> static inline R cabs(Cx<R> z) {
+    R x = std::abs(z.re), y = std::abs(z.im);
+    R s = x < y ? y : x;
+    if (s == R(0)) return s;
+    x /= s;
+    y /= s;
+    return s * std::sqrt(x * x + y * y);
+}
+
+template <typename R> static inline CV3<R> cv3_real(V3<R> v) {
+    CV3<R> r;
+    r.c[0] = {v.x, R(0)};
+    r.c[1] = {v.y, R(0)};
+    r.c[2] = {v.z, R(0)};
+    return r;
+}
+template <typename R> static inline CV3<R> cv3_scale(CV3<R> a, R s) {
+    for (int i = 0; i < 3; ++i) a.c[i] = cscale(a.c[i], s);
+    return a;
+}
+template <typename R> static inline CV3<R> cv3_divs(CV3<R> a, R s) {
+    for (int i = 0; i < 3; ++i) a.c[i] = cdivs(a.c[i], s);
+    return a;
+}
+template <typename R> static inline CV3<R> cv3_cmul(CV3<R> a, Cx<R> s) {
+    for (int i = 0; i < 3; ++i) a.c[i] = cmul(a.c[i], s);
+    return a;
+}
+template <typename R> static inline CV3<R> cv3_sub(CV3<R> a, CV3<R> b) {
+    for (int i = 0; i < 3; ++i) a.c[i] = csub(a.c[i], b.c[i]);
+    return a;
+}
+// real x complex cross product, conjugated like Eigen's MatrixBase::cross
+template <typename R> static inline CV3<R> cross_rc(V3<R> a, const CV3<R> &b) {
+    auto m = [](R s, Cx<R> z) { return Cx<R>{z.re * s, z.im * s}; };  // float*complex, complex.h:128-132
+    CV3<R> r;
+    r.c[0] = cconj(csub(m(a.y, b.c[2]), m(a.z, b.c[1])));
+    r.c[1] = cconj(csub(m(a.z, b.c[0]), m(a.x, b.c[2])));
+    r.c[2] = cconj(csub(m(a.x, b.c[1]), m(a.y, b.c[0])));
+    return r;
+}
+// real . complex: sum(conj(a_i) b_i) with a real -> sum(a_i b_i), Eigen order
+template <typename R> static inline Cx<R> dot_rc(V3<R> a, const CV3<R> &b) {
+    Cx<R> t0 = cscale(b.c[0], a.x), t1 = cscale(b.c[1], a.y), t2 = cscale(b.c[2], a.z);
+    return cadd(t0, cadd(t1, t2));
+}
+// complex . complex (Hermitian): sum(conj(a_i) b_i) (geometry.h:138)
+template <typename R> static inline Cx<R> dot_cc(const CV3<R> &a, const CV3<R> &b) {
+    Cx<R> t0 = cmul(cconj(a.c[0]), b.c[0]), t1 = cmul(cconj(a.c[1]), b.c[1]),
+          t2 = cmul(cconj(a.c[2]), b.c[2]);
+    return cadd(t0, cadd(t1, t2));
+}
+// Eigen isZero(1e-20): every |coeff|^2 <= prec^2
+template <typename R> static inline bool cv3_is_zero(const CV3<R> &a) {
+    const R prec = R(1e-20);
+    const R lim = prec * prec;
+    for (int i = 0; i < 3; ++i) {
+        R a2 = a.c[i].re * a.c[i].re + a.c[i].im * a.c[i].im;
+        if (!(a2 <= lim)) return false;
+    }
+    return true;
+}
+
+// 3x3 row-major matrix
+template <typename R> struct M33 {
+    R m[9];
+};
+template <typename R> static inline V3<R> mulv(const M33<R> &M, V3<R> v) {
+    return {M.m[0] * v.x + (M.m[1] * v.y + M.m[2] * v.z), M.m[3] * v.x + (M.m[4] * v.y + M.m[5] * v.z),
+            M.m[6] * v.x + (M.m[7] * v.y + M.m[8] * v.z)};
+}
+template <typename R> static inline V3<R> mulTv(const M33<R> &M, V3<R> v) {
+    return {M.m[0] * v.x + (M.m[3] * v.y + M.m[6] * v.z), M.m[1] * v.x + (M.m[4] * v.y + M.m[7] * v.z),
+            M.m[2] * v.x + (M.m[5] * v.y + M.m[8] * v.z)};
+}
+template <typename R> static inline CV3<R> mulcv(const M33<R> &M, const CV3<R> &h) {
+    CV3<R> r;
+    for (int i = 0; i < 3; ++i) {
+        Cx<R> t0 = cscale(h.c[0], M.m[3 * i + 0]);
+        Cx<R> t1 = cscale(h.c[1], M.m[3 * i + 1]);
+        Cx<R> t2 = cscale(h.c[2], M.m[3 * i + 2]);
+        r.c[i] = cadd(t0, cadd(t1, t2));
+    }
+    return r;
+}
+
+// ----------------------------------------------------------------------------------
+// Halton sampler (halton.h:11-67)
+// ----------------------------------------------------------------------------------
+template <typename R, int base> static inline R radical_inverse_b(uint64_t v) {
+    const R invBase = R(1) / R(base);
+    uint64_t reversed = 0;
+    R invBaseN = 1;
+    while (v) {
+        uint64_t next = v / base;
+        uint64_t digit = v - next * base;
+        reversed = reversed * base + digit;
+        invBaseN *= invBase;
+        v = next;
+    }
+    const R ome = std::nextafter(R(1), R(0));
+    return std::min(R(reversed) * invBaseN, ome);
+}
+
+template <typename R> static inline R radical_inverse(uint64_t v, unsigned dim) {
+    switch (dim) {
+        case 0: return radical_inverse_b<R, 2>(v);
+        case 1: return radical_inverse_b<R, 3>(v);
+        case 2: return radical_inverse_b<R, 5>(v);
+        case 3: return radical_inverse_b<R, 7>(v);
+        case 4: return radical_inverse_b<R, 11>(v);
+        case 5: return radical_inverse_b<R, 13>(v);
+        case 6: return radical_inverse_b<R, 17>(v);
+        case 7: return radical_inverse_b<R, 19>(v);
+        case 8: return radical_inverse_b<R, 23>(v);
+        case 9: return radical_inverse_b<R, 29>(v);
+        default: return R(0);  // halton.h:1082-1084: Assert (no-op in release), return 0
+    }
+}
+
+template <typename R> struct Halton {
+    uint64_t index = 0;
+    uint16_t dim = 0;
+    R get1D() { return radical_inverse<R>(index, dim++); }
+};
+
+// ----------------------------------------------------------------------------------
+// Sampling, antenna pattern, antennas (sampling.h:38-47, emitter.h:109-214)
+// ----------------------------------------------------------------------------------
+template <typename R> static inline V3<R> uniform_sample_sphere(R u0, R u1) {
+    R phi = R(2) * Consts<R>::Pi * u0;
+    R y = R(2) * u1 - R(1);
+    R r = std::sqrt(std::max(R(0), R(1) - y * y));
+    return {-r * std::sin(phi), y, -r * std::cos(phi)};
+}
+
+// AWRAngularDistribution::evaluate (emitter.h:126-136)
+template <typename R> static inline CV3<R> awr_evaluate(V3<R> d) {
+    // Vector3c(0,1,0).cross(d): real-valued (d.z, 0, -d.x) (zeros as the conjugated cross gives them)
+    CV3<R> H;
+    H.c[0] = {R(1) * d.z - R(0) * d.y, -(R(0) * d.z - R(0) * d.y)};
+    H.c[1] = {R(0) * d.x - R(0) * d.z, -(R(0) * d.x - R(0) * d.z)};
+    H.c[2] = {R(0) * d.y - R(1) * d.x, -(R(0) * d.y - R(0) * d.x)};
+    R cos_h = std::sqrt(R(1) - d.x * d.x);
+    R cos_e = std::sqrt(R(1) - d.y * d.y);
+    // 2.622 / pow(double, 6) is evaluated in double and converted to the scalar type
+    R s1 = R(2.622 / std::pow(double(cos_h) - 1.8, 6));
+    R s2 = R(0.625 / std::pow(double(cos_e) - 1.5, 4));
+    H = cv3_scale(H, s1);
+    H = cv3_scale(H, s2);
+    return H;
+}
+
+template <typename R> struct Antenna {
+    V3<R> pos;
+    M33<R> rot;
+};
+
+template <typename R> struct Ray {
+    V3<R> o{}, d{};
+    R time = 0;
+    R frequency = 0;
+    int depth = 0;
+    CV3<R> H{};
+    R k0() const { return R(2) * Consts<R>::Pi * frequency / Consts<R>::SpeedOfLight; }
+    R wavelength() const { return Consts<R>::SpeedOfLight / frequency; }
+    void addDistance(R dist) { time += dist / Consts<R>::SpeedOfLight; }
+    V3<R> at(R t) const { return add(o, scale(t, d)); }
+};
+
+template <typename R> struct Isect {
+    R t = std::numeric_limits<R>::infinity();
+    R tMax = std::numeric_limits<R>::infinity();
+    V3<R> p{}, n{};
+    Ray<R> ray;
+    void reset() {
+        t = std::numeric_limits<R>::infinity();
+        tMax = std::numeric_limits<R>::infinity();
+    }
+    bool valid() const { return t < tMax; }
+    V3<R> wi() const { return neg(ray.d); }
+    V3<R> R_() const { return sub(scale(R(2) * dot(n, wi()), n), wi()); }
+    R cosTheta() const { return std::abs(dot(n, wi())); }
+};
+
+// NFAntenna::sample (emitter.h:174-180)
+template <typename R> static inline void antenna_sample(const Antenna<R> &a, R u0, R u1, Ray<R> &ray) {
+    ray.o = a.pos;
+    V3<R> d = uniform_sample_sphere(u0, u1);
+    CV3<R> H = cv3_divs(awr_evaluate(d), Consts<R>::Inv4Pi);
+    ray.d = mulv(a.rot, d);
+    ray.H = mulcv(a.rot, H);
+}
+// NFAntenna::evaluate (emitter.h:182-186)
+template <typename R> static inline void antenna_evaluate(const Antenna<R> &a, Ray<R> &ray) {
+    ray.o = a.pos;
+    CV3<R> H = awr_evaluate(mulTv(a.rot, ray.d));
+    ray.H = mulcv(a.rot, H);
+}
+// NFAntenna::connect (emitter.h:188-193)
+template <typename R> static inline void antenna_connect(Isect<R> &nee) {
+    R r = nee.t;
+    nee.ray.addDistance(r);
+    nee.ray.H = cv3_scale(nee.ray.H, R(1) / (R(4) * Consts<R>::Pi * r));
+}
+// NFAntenna::nee (emitter.h:195-203)
+template <typename R> static inline CV3<R> antenna_nee(const Antenna<R> &a, Isect<R> &nee) {
+    nee.ray.d = sub(a.pos, nee.ray.o);
+    R r = norm(nee.ray.d);
+    nee.ray.d = divs(nee.ray.d, r);
+    nee.tMax = r;
+    CV3<R> H = awr_evaluate(mulTv(a.rot, neg(nee.ray.d)));
+    return mulcv(a.rot, H);
+}
+
+// SurfaceEmitter (emitter.h:53-82)
+template <typename R> static inline void surface_evaluate(const Isect<R> &incoming, Ray<R> &ray) {
+    CV3<R> J = cross_rc(incoming.n, incoming.ray.H);
+    J = cv3_scale(J, R(2));
+    ray.H = cross_rc(ray.d, J);
+    if (dot(ray.d, incoming.n) < R(0)) {
+        for (int i = 0; i < 3; ++i) ray.H.c[i] = {R(0), R(0)};
+    }
+}
+template <typename R> static inline void surface_connect(const Isect<R> &incoming, Isect<R> &outgoing) {
+    R r = outgoing.t;
+    outgoing.ray.addDistance(r);
+    Cx<R> g = {R(1) / std::max(r, R(1e-3)), incoming.ray.k0()};  // Complex(0, k0) + 1/max(r,1e-3)
+    g = cdivs(g, R(4) * Consts<R>::Pi * r);
+    outgoing.ray.H = cv3_cmul(outgoing.ray.H, g);
+}
+template <typename R> static inline void surface_sample(const Isect<R> &incoming, R u0, R u1, Ray<R> &ray) {
+    ray.d = uniform_sample_sphere(u0, u1);
+    ray.H = cv3_scale(ray.H, R(1) / Consts<R>::Inv4Pi);
+    surface_evaluate(incoming, ray);
+}
+
+// ----------------------------------------------------------------------------------
+// Mesh + BVH (replaces Embree; hit semantics of src/arch/cpu.cpp:9-87)
+// ----------------------------------------------------------------------------------
+struct Mesh {
+    std::vector<float> v;    // 3 per vertex
+    std::vector<int32_t> f;  // 3 per triangle
+    int64_t nt = 0;
+};
+
+struct BNode {
+    float lo[3], hi[3];
+    int32_t left;   // internal: index of first child (second = left + 1); leaf: first prim slot
+    int32_t count;  // 0 for internal
+};
+
+struct Bvh {
+    std::vector<BNode> nodes;
+    std::vector<int32_t> prims;  // triangle ids in leaf order
+};
+
+struct Scene {
+    Mesh mesh;
+    Bvh bvh;
+};
+
+static void build_bvh(Scene &s) {
+    const int64_t nt = s.mesh.nt;
+    std::vector<float> lo(3 * nt), hi(3 * nt), cen(3 * nt);
+    for (int64_t t = 0; t < nt; ++t) {
+        for (int a = 0; a < 3; ++a) {
+            float mn = std::numeric_limits<float>::infinity(), mx = -mn;
+            for (int k = 0; k < 3; ++k) {
+                float x = s.mesh.v[3 * s.mesh.f[3 * t + k] + a];
+                mn = std::min(mn, x);
+                mx = std::max(mx, x);
+            }
+            // padding keeps the box test conservative against rounding
+            float pad = (std::abs(mn) + std::abs(mx)) * 1e-6f + 1e-7f;
+            lo[3 * t + a] = mn - pad;
+            hi[3 * t + a] = mx + pad;
+            cen[3 * t + a] = 0.5f * (mn + mx);
+        }
+    }
+    s.bvh.prims.resize(nt);
+    for (int64_t i = 0; i < nt; ++i) s.bvh.prims[i] = int32_t(i);
+    s.bvh.nodes.clear();
+    s.bvh.nodes.reserve(2 * std::max<int64_t>(nt, 1));
+    struct Task {
+        int32_t node, first, count;
+    };
+    std::vector<Task> stack;
+    s.bvh.nodes.push_back(BNode{});
+    stack.push_back({0, 0, int32_t(nt)});
+    const int kBins = 16;
+    while (!stack.empty()) {
+        Task tk = stack.back();
+        stack.pop_back();
+        BNode nd;
+        for (int a = 0; a < 3; ++a) {
+            nd.lo[a] = std::numeric_limits<float>::infinity();
+            nd.hi[a] = -std::numeric_limits<float>::infinity();
+        }
+        float clo[3], chi[3];
+        for (int a = 0; a < 3; ++a) {
+            clo[a] = std::numeric_limits<float>::infinity();
+            chi[a] = -clo[a];
+        }
+        for (int32_t i = tk.first; i < tk.first + tk.count; ++i) {
+            int32_t p = s.bvh.prims[i];
+            for (int a = 0; a < 3; ++a) {
+                nd.lo[a] = std::min(nd.lo[a], lo[3 * p + a]);
+                nd.hi[a] = std::max(nd.hi[a], hi[3 * p + a]);
+                clo[a] = std::min(clo[a], cen[3 * p + a]);
+                chi[a] = std::max(chi[a], cen[3 * p + a]);
+            }
+        }
+        if (tk.count <= 4) {
+            nd.left = tk.first;
+            nd.count = tk.count;
+            s.bvh.nodes[tk.node] = nd;
+            continue;
+        }
+        // binned SAH over the widest centroid axis
+        int axis = 0;
+        float ext = chi[0] - clo[0];
+        for (int a = 1; a < 3; ++a)
+            if (chi[a] - clo[a] > ext) {
+                ext = chi[a] - clo[a];
+                axis = a;
+            }
+        int32_t mid = tk.first + tk.count / 2;
+        if (ext > 0.f) {
+            struct Bin {
+                float lo[3], hi[3];
+                int n;
+            } bins[kBins];
+            for (auto &b : bins) {
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::numeric_limits<float>::infinity();
+                    b.hi[a] = -b.lo[a];
+                }
+                b.n = 0;
+            }
+            auto binOf = [&](int32_t p) {
+                int b = int((cen[3 * p + axis] - clo[axis]) / ext * kBins);
+                return std::min(std::max(b, 0), kBins - 1);
+            };
+            for (int32_t i = tk.first; i < tk.first + tk.count; ++i) {
+                int32_t p = s.bvh.prims[i];
+                Bin &b = bins[binOf(p)];
+                b.n++;
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::min(b.lo[a], lo[3 * p + a]);
+                    b.hi[a] = std::max(b.hi[a], hi[3 * p + a]);
+                }
+            }
+            auto area = [](const float *l, const float *h) {
+                float dx = h[0] - l[0], dy = h[1] - l[1], dz = h[2] - l[2];
+                if (dx < 0) return 0.f;
+                return dx * dy + dy * dz + dz * dx;
+            };
+            float best = std::numeric_limits<float>::infinity();
+            int bestSplit = -1;
+            for (int sp = 1; sp < kBins; ++sp) {
+                float L[3], H[3], L2[3], H2[3];
+                for (int a = 0; a < 3; ++a) {
+                    L[a] = L2[a] = std::numeric_limits<float>::infinity();
+                    H[a] = H2[a] = -L[a];
+                }
+                int nl = 0, nr = 0;
+                for (int b = 0; b < sp; ++b) {
+                    nl += bins[b].n;
+                    for (int a = 0; a < 3; ++a) {
+                        L[a] = std::min(L[a], bins[b].lo[a]);
+                        H[a] = std::max(H[a], bins[b].hi[a]);
+                    }
+                }
+                for (int b = sp; b < kBins; ++b) {
+                    nr += bins[b].n;
+                    for (int a = 0; a < 3; ++a) {
+                        L2[a] = std::min(L2[a], bins[b].lo[a]);
+                        H2[a] = std::max(H2[a], bins[b].hi[a]);
+                    }
+                }
+                if (nl == 0 || nr == 0) continue;
+                float c = area(L, H) * nl + area(L2, H2) * nr;
+                if (c < best) {
+                    best = c;
+                    bestSplit = sp;
+                }
+            }
+            if (bestSplit > 0) {
+                auto it = std::partition(s.bvh.prims.begin() + tk.first, s.bvh.prims.begin() + tk.first + tk.count,
+                                         [&](int32_t p) { return binOf(p) < bestSplit; });
+                mid = int32_t(it - s.bvh.prims.begin());
+            }
+        }
+        if (mid <= tk.first || mid >= tk.first + tk.count) {
+            std::nth_element(s.bvh.prims.begin() + tk.first, s.bvh.prims.begin() + tk.first + tk.count / 2,
+                             s.bvh.prims.begin() + tk.first + tk.count,
+                             [&](int32_t a, int32_t b) { return cen[3 * a + axis] < cen[3 * b + axis]; });
+            mid = tk.first + tk.count / 2;
+        }
+        int32_t l = int32_t(s.bvh.nodes.size());
+        s.bvh.nodes.push_back(BNode{});
+        s.bvh.nodes.push_back(BNode{});
+        nd.left = l;
+        nd.count = 0;
+        s.bvh.nodes[tk.node] = nd;
+        stack.push_back({l, tk.first, mid - tk.first});
+        stack.push_back({l + 1, mid, tk.first + tk.count - mid});
+    }
+}
+
+// Moller-Trumbore in precision R. Accepts tnear < t <= tfar.
+template <typename R>
+static inline bool tri_hit(const Mesh &m, int32_t prim, V3<R> o, V3<R> d, R tnear, R tfar, R &t_out) {
+    const float *v0f = &m.v[3 * m.f[3 * prim + 0]];
+    const float *v1f = &m.v[3 * m.f[3 * prim + 1]];
+    const float *v2f = &m.v[3 * m.f[3 * prim + 2]];
+    V3<R> v0{R(v0f[0]), R(v0f[1]), R(v0f[2])};
+    V3<R> v1{R(v1f[0]), R(v1f[1]), R(v1f[2])};
+    V3<R> v2{R(v2f[0]), R(v2f[1]), R(v2f[2])};
+    V3<R> e1 = sub(v1, v0), e2 = sub(v2, v0);
+    V3<R> pv = cross(d, e2);
+    R det = dot(e1, pv);
+    if (det == R(0)) return false;
+    R inv = R(1) / det;
+    V3<R> tv = sub(o, v0);
+    R u = dot(tv, pv) * inv;
+    if (u < R(0) || u > R(1)) return false;
+    V3<R> qv = cross(tv, e1);
+    R v = dot(d, qv) * inv;
+    if (v < R(0) || u + v > R(1)) return false;
+    R t = dot(e2, qv) * inv;
+    if (!(t > tnear && t <= tfar)) return false;
+    t_out = t;
+    return true;
+}
+
+template <typename R> static inline V3<R> tri_normal(const Mesh &m, int32_t prim) {
+    const float *v0f = &m.v[3 * m.f[3 * prim + 0]];
+    const float *v1f = &m.v[3 * m.f[3 * prim + 1]];
+    const float *v2f = &m.v[3 * m.f[3 * prim + 2]];
+    V3<R> v0{R(v0f[0]), R(v0f[1]), R(v0f[2])};
+    V3<R> v1{R(v1f[0]), R(v1f[1]), R(v1f[2])};
+    V3<R> v2{R(v2f[0]), R(v2f[1]), R(v2f[2])};
+    return normalized(cross(sub(v1, v0), sub(v2, v0)));
+}
+
+template <typename R>
+static inline bool box_hit(const BNode &n, V3<R> o, V3<R> inv, R tnear, R tfar) {
+    R t0x = (R(n.lo[0]) - o.x) * inv.x, t1x = (R(n.hi[0]) - o.x) * inv.x;
+    R t0y = (R(n.lo[1]) - o.y) * inv.y, t1y = (R(n.hi[1]) - o.y) * inv.y;
+    R t0z = (R(n.lo[2]) - o.z) * inv.z, t1z = (R(n.hi[2]) - o.z) * inv.z;
+    // fmin/fmax ignore NaN (0 * inf), which leaves that slab unbounded: conservative
+    R tmin = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)), std::fmax(std::fmin(t0z, t1z), tnear));
+    R tmax = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)), std::fmin(std::fmax(t0z, t1z), tfar));
+    return tmin <= tmax * R(1.0000004);
+}
+
+// closest hit; returns prim or -1
+template <typename R>
+static int32_t closest_hit(const Scene &s, V3<R> o, V3<R> d, R tnear, R tfar, R &t_best) {
+    V3<R> inv{R(1) / d.x, R(1) / d.y, R(1) / d.z};
+    int32_t best = -1;
+    t_best = tfar;
+    if (s.bvh.nodes.empty() || s.mesh.nt == 0) return -1;
+    int32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const BNode &n = s.bvh.nodes[stack[--sp]];
+        if (!box_hit(n, o, inv, tnear, t_best)) continue;
+        if (n.count) {
+            for (int32_t i = n.left; i < n.left + n.count; ++i) {
+                int32_t p = s.bvh.prims[i];
+                R t;
+                if (tri_hit(s.mesh, p, o, d, tnear, tfar, t)) {
+                    if (t < t_best || (t == t_best && (best < 0 || p < best))) {
+                        t_best = t;
+                        best = p;
+                    }
+                }
+            }
+        } else {
+            stack[sp++] = n.left + 1;
+            stack[sp++] = n.left;
+        }
+    }
+    return best;
+}
+
+template <typename R> static bool occluded(const Scene &s, V3<R> o, V3<R> d, R tnear, R tfar) {
+    V3<R> inv{R(1) / d.x, R(1) / d.y, R(1) / d.z};
+    if (s.bvh.nodes.empty() || s.mesh.nt == 0) return false;
+    int32_t stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const BNode &n = s.bvh.nodes[stack[--sp]];
+        if (!box_hit(n, o, inv, tnear, tfar)) continue;
+        if (n.count) {
+            for (int32_t i = n.left; i < n.left + n.count; ++i) {
+                R t;
+                if (tri_hit(s.mesh, s.bvh.prims[i], o, d, tnear, tfar, t)) return true;
+            }
+        } else {
+            stack[sp++] = n.left + 1;
+            stack[sp++] = n.left;
+        }
+    }
+    return false;
+}
+
+// RT::intersect (src/arch/cpu.cpp:63-87)
+template <typename R> static inline void rt_intersect(const Scene &s, Isect<R> &is) {
+    R t;
+    int32_t p = closest_hit(s, is.ray.o, is.ray.d, Consts<R>::Epsilon, is.tMax, t);
+    if (p >= 0) {
+        is.t = t;
+        is.p = is.ray.at(t);
+        is.n = tri_normal<R>(s.mesh, p);
+        if (dot(is.n, is.ray.d) > R(0)) is.n = neg(is.n);
+    }
+}
+// RT::visible (src/arch/cpu.cpp:53-61)
+template <typename R> static inline bool rt_visible(const Scene &s, const Isect<R> &is) {
+    return !occluded(s, is.ray.o, is.ray.d, Consts<R>::Epsilon, is.tMax);
+}
+
+// ----------------------------------------------------------------------------------
+// Frame (radar.h:173-701), accumulated in Real with a CAS loop like radar.h:63-83
+// ----------------------------------------------------------------------------------
+template <typename R> static inline void atomic_add(R *addr, R v) {
+    using U = typename std::conditional<sizeof(R) == 4, uint32_t, uint64_t>::type;
+    auto &bits = *reinterpret_cast<std::atomic<U> *>(addr);
+    U oldBits = bits.load(), newBits;
+    do {
+        R f;
+        std::memcpy(&f, &oldBits, sizeof(R));
+        f = f + v;
+        std::memcpy(&newBits, &f, sizeof(R));
+    } while (!bits.compare_exchange_weak(oldBits, newBits));
+}
+
+template <typename R> struct Frame {
+    int chirps = 1, samples = 1, channels = 1;
+    R *data = nullptr;  // interleaved re, im
+    size_t index(int c, int s, int ch) const { return (size_t(c) * samples + s) * channels + ch; }
+};
+
+// radar.h:91-96 safe_modulo(T a, unsigned b): `a % b` converts a negative int to
+// unsigned first, so a negative a wraps as (a + 2^32) mod b. That equals the true
+// modulo only when b divides 2^32 (powers of two); restated as the reference computes it.
+static inline int safe_mod(int a, int b) {
+    int m = int(unsigned(a) % unsigned(b));
+    if (m < 0) m += b;
+    return m;
+}
+
+// Frame::splat<16> (radar.h:564-626) for an index whose chirp/channel are integral
+template <typename R> static void frame_splat(Frame<R> &f, R idx_chirp, R idx_sample, R idx_channel, Cx<R> value) {
+    R raw[3] = {idx_chirp, idx_sample, idx_channel};
+    int center[3];
+    R shifts[3];
+    R weight = 1;
+    for (int i = 0; i < 3; ++i) {
+        center[i] = int(std::round(raw[i]));
+        R shift = raw[i] - R(center[i]);
+        if (std::abs(shift) < R(1e-4)) {
+            shifts[i] = 0;
+            continue;
+        }
+        shifts[i] = shift;
+        R shiftPi = R(M_PI * double(shift));
+        value = cmul(value, cexpj(shiftPi));
+        weight = R(double(weight) * (double(std::sin(shiftPi)) / M_PI));
+    }
+    const int dims[3] = {f.chirps, f.samples, f.channels};
+    // recursive expansion over the three components (only non-zero shifts expand)
+    int lo[3], hi[3];
+    for (int i = 0; i < 3; ++i) {
+        lo[i] = shifts[i] == R(0) ? 0 : -16;
+        hi[i] = shifts[i] == R(0) ? 0 : 16;
+    }
+    for (int a = lo[0]; a <= hi[0]; ++a) {
+        R w0 = shifts[0] == R(0) ? weight : weight / (shifts[0] - R(a));
+        int c = shifts[0] == R(0) ? center[0] : safe_mod(center[0] + a, dims[0]);
+        for (int b = lo[1]; b <= hi[1]; ++b) {
+            R w1 = shifts[1] == R(0) ? w0 : w0 / (shifts[1] - R(b));
+            int s = shifts[1] == R(0) ? center[1] : safe_mod(center[1] + b, dims[1]);
+            for (int k = lo[2]; k <= hi[2]; ++k) {
+                R w2 = shifts[2] == R(0) ? w1 : w1 / (shifts[2] - R(k));
+                int ch = shifts[2] == R(0) ? center[2] : safe_mod(center[2] + k, dims[2]);
+                // the reference indexes center directly for a delta component; a rounded
+                // index equal to the dimension (e.g. sample >= N-0.5) would be out of
+                // bounds there. It is wrapped here (the spectrum is periodic).
+                c = safe_mod(c, dims[0]);
+                s = safe_mod(s, dims[1]);
+                ch = safe_mod(ch, dims[2]);
+                size_t id = f.index(c, s, ch);
+                atomic_add(&f.data[2 * id + 0], w2 * value.re);
+                atomic_add(&f.data[2 * id + 1], w2 * value.im);
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------
+// Integrator + PathTracer::sample (path.h:235-451, integrator.h:107-168)
+// ----------------------------------------------------------------------------------
+template <typename R> struct Rf {
+    R startFreq, freqSlope, adcRate, idleTime, rampTime, antennaDelay;
+    R bandwidth() const { return freqSlope * rampTime; }
+    R chirpFrequency() const { return R(1) / (idleTime + rampTime); }
+};
+
+struct Flags {
+    bool onlyIndirect, useGO, poDiffraction, doGuiding, correctPhase, filterGuiding, doFiltering,
+        filteringSphere, produceDebugImage;
+    int maxDepth;
+    float filteringMin, filteringMax, filteringRadius;
+};
+
+template <typename R> struct Tracer {
+    const Scene *scene;
+    Rf<R> rf;
+    Antenna<R> tx, rx;
+    Flags fl;
+    Frame<R> frame;
+    R currentSampleWeight = 1;
+    int64_t sampleIndexOffset = 0;
+    oracle_record *records = nullptr;  // optional per-sample event log
+    int maxRecords = 0;
+
+    // Integrator::measureRay (integrator.h:107-110)
+    Cx<R> measureRay(R dt) const {
+        R angle = R(2) * Consts<R>::Pi * (rf.startFreq - dt * rf.freqSlope / R(2)) * dt;
+        return cexpj(angle);
+    }
+
+    // Integrator::splat (integrator.h:113-148) without the debug image
+    void splat(int channel, R delta_t, R dphase, Cx<R> measurement, R weight, oracle_record *rec) {
+        if (!fl.produceDebugImage) {
+            if (weight == R(0) || (measurement.re == R(0) || measurement.im == R(0))) return;
+        }
+        delta_t += rf.antennaDelay;
+        R sample;
+        if (rf.freqSlope == R(0)) {
+            sample = 0;
+        } else {
+            R delta_f = delta_t * rf.freqSlope;
+            R x = delta_f / rf.adcRate;
+            sample = R(frame.samples) * (x - std::floor(x));
+        }
+        R delta_p = R(2) * rf.startFreq * R(0) / Consts<R>::SpeedOfLight;
+        R y = delta_p / rf.chirpFrequency();
+        R chirp = R(frame.chirps) * (y - std::floor(y));
+        Cx<R> contribution = cmul(measurement, measureRay(delta_t));
+        Cx<R> value = cscale(contribution, weight);
+        if (rec) {
+            rec->bin = double(sample);
+            rec->value_re = double(value.re);
+            rec->value_im = double(value.im);
+            rec->splatted = 1;
+        }
+        frame_splat(frame, chirp, sample, R(channel), value);
+    }
+
+    void reflectRay(Ray<R> &ray, const Isect<R> &isect) const {  // integrator.h:164-168
+        CV3<R> H = ray.H;
+        ray.d = isect.R_();
+        Cx<R> nh = dot_rc(isect.n, H);
+        V3<R> n2 = scale(R(2), isect.n);
+        CV3<R> t;
+        for (int i = 0; i < 3; ++i) t.c[i] = cscale(nh, i == 0 ? n2.x : i == 1 ? n2.y : n2.z);
+        ray.H = cv3_sub(t, H);
+    }
+
+    void sample(int64_t index) {
+        Halton<R> sampler;
+        sampler.index = uint64_t(sampleIndexOffset + index);
+        sampler.dim = 0;
+        const R maxDist = rf.adcRate / rf.freqSlope * Consts<R>::SpeedOfLight;
+        const R sampleWeight = currentSampleWeight;
+        R primaryPdf = 1;
+        Isect<R> isect;
+        Ray<R> &ray = isect.ray;
+        ray.frequency = rf.startFreq + sampler.get1D() * rf.bandwidth();
+        Isect<R> incoming;  // SurfaceEmitter::incoming
+        R r = 0;
+        R cosTheta = 1;
+        int nrec = 0;
+        while (true) {
+            V3<R> tmpd = ray.d;
+            if (ray.depth == 0) {
+                R u0 = sampler.get1D();
+                R u1 = sampler.get1D();
+                antenna_sample(tx, u0, u1, ray);
+                ray.H = cv3_scale(ray.H, R(1) / primaryPdf);
+            } else {
+                if (!fl.useGO) {
+                    R u0 = sampler.get1D();
+                    R u1 = sampler.get1D();
+                    surface_sample(incoming, u0, u1, ray);
+                } else {
+                    reflectRay(ray, isect);
+                }
+            }
+
+            // next event estimation (single RX channel, path.h:292)
+            do {
+                if (ray.depth == 0 && fl.onlyIndirect) break;
+                Isect<R> nee = isect;
+                nee.t = std::numeric_limits<R>::infinity();
+                CV3<R> Hrx = antenna_nee(rx, nee);
+                if (!fl.poDiffraction && !rt_visible(*scene, nee)) break;
+                nee.t = nee.tMax;
+                if (ray.depth == 0) {
+                    antenna_evaluate(tx, nee.ray);
+                    antenna_connect(nee);
+                } else {
+                    surface_evaluate(incoming, nee.ray);
+                    surface_connect(incoming, nee);
+                }
+                Cx<R> v = dot_cc(nee.ray.H, Hrx);
+                R dphase = 0;
+                if (ray.depth > 0) {
+                    if (fl.correctPhase) {
+                        V3<R> rxPos = nee.ray.at(nee.t);
+                        V3<R> virtualTx = sub(nee.ray.o, scale(r, ray.d));
+                        R dist = norm(sub(virtualTx, rxPos));
+                        nee.ray.time = dist / Consts<R>::SpeedOfLight;
+                        R pw = Consts<R>::Pi * R(fl.filteringRadius) * nee.ray.wavelength();
+                        v = cdivs(cscale(dot_cc(ray.H, Hrx), Consts<R>::Pi * dist), R(double(pw) * double(pw)));
+                        v = cdivs(v, R(4) * Consts<R>::Pi);
+                    } else if (fl.useGO) {
+                        v = cscale(v, r / cosTheta);
+                        v = cdivs(v, R(4) * Consts<R>::Pi);
+                        if (double(cosTheta) < 1e-3) break;
+                    }
+                    if (fl.filteringSphere) {
+                        V3<R> rxPos = nee.ray.at(nee.t);
+                        R lambda = std::max<R>(R(0), dot(ray.d, sub(rxPos, ray.o)));
+                        R rxDist = norm(sub(ray.at(lambda), rxPos));
+                        dphase = rxDist;
+                    } else {
+                        R c = dot(normalized(sub(nee.ray.d, tmpd)), isect.n);
+                        dphase = r * std::sqrt(R(1) - c * c) / c;
+                    }
+                    dphase /= nee.ray.wavelength();
+                    if (fl.doFiltering) {
+                        if (fl.filteringSphere) {
+                            if (dphase > R(fl.filteringRadius)) {
+                                if (fl.correctPhase) {
+                                    v = {R(0), R(0)};
+                                } else {
+                                    R q = dphase / R(fl.filteringRadius) - R(1);
+                                    R taper = std::max<R>(R(1.0 - 0.20 * double(q)), R(0));
+                                    v = cscale(v, taper);
+                                }
+                            }
+                        } else {
+                            if (dphase > R(fl.filteringMax)) v = {R(0), R(0)};
+                            if (dphase > R(fl.filteringMin))
+                                v = cscale(v, (R(fl.filteringMax) - dphase) / (R(fl.filteringMax) - R(fl.filteringMin)));
+                        }
+                    }
+                }
+                oracle_record *rec = nullptr;
+                if (records && nrec < maxRecords) {
+                    rec = &records[nrec++];
+                    rec->depth = ray.depth;
+                    rec->time = double(nee.ray.time);
+                    rec->v_re = double(v.re);
+                    rec->v_im = double(v.im);
+                    rec->dphase = double(dphase);
+                    rec->splatted = 0;
+                }
+                splat(0, nee.ray.time, dphase, v, sampleWeight, rec);
+            } while (false);
+
+            if (ray.depth >= fl.maxDepth || r >= maxDist) break;
+            if (cv3_is_zero(ray.H)) break;
+            isect.reset();
+            rt_intersect(*scene, isect);
+            if (!isect.valid()) break;
+            cosTheta = isect.cosTheta();
+            if (double(cosTheta) < 1e-3) break;
+            r += isect.t;
+            if (!fl.useGO) {
+                if (ray.depth == 0) {
+                    antenna_connect(isect);
+                } else {
+                    surface_connect(incoming, isect);
+                }
+                ray.H = cv3_scale(ray.H, isect.t * isect.t / cosTheta);
+            } else {
+                ray.addDistance(isect.t);
+            }
+            if (cv3_is_zero(ray.H)) break;
+            incoming = isect;
+            ray.o = isect.p;
+            ray.depth++;
+        }
+    }
+};
+
+template <typename R> static Antenna<R> to_antenna(const hsr_antenna_o &a) {
+    Antenna<R> r;
+    r.pos = {R(a.position[0]), R(a.position[1]), R(a.position[2])};
+    for (int i = 0; i < 9; ++i) r.rot.m[i] = R(a.rotation[i]);
+    return r;
+}
+
+static Flags to_flags(const hsr_tracer_flags_o &f) {
+    Flags r;
+    r.onlyIndirect = f.onlyIndirect != 0;
+    r.maxDepth = f.maxDepth;
+    r.useGO = f.useGeometricalOptics != 0;
+    r.poDiffraction = f.poDiffraction != 0;
+    r.doGuiding = f.doGuiding != 0;
+    r.correctPhase = f.correctPhase != 0;
+    r.filterGuiding = f.filterGuiding != 0;
+    r.doFiltering = f.doFiltering != 0;
+    r.filteringSphere = f.filteringSphere != 0;
+    r.produceDebugImage = f.produceDebugImage != 0;
+    r.filteringMin = f.filteringMin;
+    r.filteringMax = f.filteringMax;
+    r.filteringRadius = f.filteringRadius;
+    return r;
+}
+
+template <typename R>
+static void setup_tracer(Tracer<R> &tr, const Scene *s, const hsr_rf_config_o *rf, const hsr_antenna_o *tx,
+                         const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl) {
+    tr.scene = s;
+    tr.rf = Rf<R>{R(rf->startFreq), R(rf->freqSlope), R(rf->adcRate), R(rf->idleTime), R(rf->rampTime),
+                  R(rf->antennaDelay)};
+    tr.tx = to_antenna<R>(*tx);
+    tr.rx = to_antenna<R>(*rx);
+    tr.fl = to_flags(*fl);
+}
+
+// cpu::Backend::run (arch/cpu.h:21-41): batches of 256 from a mutex-protected counter
+template <typename F> static void run_batches(int64_t budget, int threads, F &&work) {
+    if (threads <= 0) threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    int64_t counter = 0;
+    std::mutex mu;
+    auto worker = [&]() {
+        while (true) {
+            int64_t batch, index;
+            {
+                std::unique_lock<std::mutex> lock(mu);
+                batch = std::min<int64_t>(budget - counter, 256);
+                if (batch <= 0) break;
+                index = counter;
+                counter += batch;
+            }
+            for (int64_t j = 0; j < batch; ++j) work(index + j);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 1; i < threads; ++i) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+}
+
+template <typename R>
+static int simulate(const Scene *s, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
+                    const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
+                    int64_t budget, int64_t offset, float sampleWeight, int threads, double *frame_out,
+                    double *weight_out) {
+    Tracer<R> tr;
+    setup_tracer(tr, s, rf, tx, rx, fl);
+    tr.currentSampleWeight = R(sampleWeight);
+    tr.sampleIndexOffset = offset;
+    tr.frame.chirps = fc->chirpCount;
+    tr.frame.samples = fc->samplesPerChirp;
+    tr.frame.channels = fc->channelCount;
+    size_t n = size_t(fc->chirpCount) * fc->samplesPerChirp * fc->channelCount;
+    std::vector<R> data(2 * n, R(0));
+    tr.frame.data = data.data();
+    run_batches(budget, threads, [&](int64_t i) { tr.sample(i); });
+    for (size_t i = 0; i < 2 * n; ++i) frame_out[i] += double(data[i]);
+    // PathTracer::incrementTotalWeight adds the float sample weight in double per sample
+    double w = 0;
+    for (int64_t i = 0; i < budget; ++i) w += double(float(sampleWeight));
+    *weight_out += w;
+    return 0;
+}
+
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+int oracle_abi_version(void) { return 1; }
+
+float oracle_radical_inverse_f(uint64_t index, int dim) { return radical_inverse<float>(index, unsigned(dim)); }
+double oracle_radical_inverse_d(uint64_t index, int dim) { return radical_inverse<double>(index, unsigned(dim)); }
+
+void *oracle_scene_create(const float *vertices, int64_t nv, const int32_t *indices, int64_t nt) {
+    if ((nv > 0 && !vertices) || (nt > 0 && !indices) || nv < 0 || nt < 0) return nullptr;
+    for (int64_t i = 0; i < 3 * nt; ++i)
+        if (indices[i] < 0 || indices[i] >= nv) return nullptr;
+    Scene *s = new Scene;
+    s->mesh.v.assign(vertices, vertices + 3 * nv);
+    s->mesh.f.assign(indices, indices + 3 * nt);
+    s->mesh.nt = nt;
+    build_bvh(*s);
+    return s;
+}
+
+void oracle_scene_destroy(void *s) { delete static_cast<Scene *>(s); }
+
+int oracle_intersect(void *sp, int64_t count, const float *o, const float *d, const float *tfar, float *t_out,
+                     float *p_out, float *n_out, int32_t *prim_out) {
+    const Scene &s = *static_cast<Scene *>(sp);
+    for (int64_t i = 0; i < count; ++i) {
+        Isect<float> is;
+        is.ray.o = {o[3 * i], o[3 * i + 1], o[3 * i + 2]};
+        is.ray.d = {d[3 * i], d[3 * i + 1], d[3 * i + 2]};
+        is.tMax = tfar[i];
+        float t;
+        int32_t p = closest_hit(s, is.ray.o, is.ray.d, Consts<float>::Epsilon, is.tMax, t);
+        prim_out[i] = p;
+        if (p >= 0) {
+            rt_intersect(s, is);
+            t_out[i] = is.t;
+            p_out[3 * i] = is.p.x;
+            p_out[3 * i + 1] = is.p.y;
+            p_out[3 * i + 2] = is.p.z;
+            n_out[3 * i] = is.n.x;
+            n_out[3 * i + 1] = is.n.y;
+            n_out[3 * i + 2] = is.n.z;
+        } else {
+            t_out[i] = std::numeric_limits<float>::infinity();
+            for (int k = 0; k < 3; ++k) p_out[3 * i + k] = n_out[3 * i + k] = 0.f;
+        }
+    }
+    return 0;
+}
+
+int oracle_visible(void *sp, int64_t count, const float *o, const float *d, const float *tfar, int32_t *vis) {
+    const Scene &s = *static_cast<Scene *>(sp);
+    for (int64_t i = 0; i < count; ++i) {
+        V3<float> oo{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, dd{d[3 * i], d[3 * i + 1], d[3 * i + 2]};
+        vis[i] = occluded(s, oo, dd, Consts<float>::Epsilon, tfar[i]) ? 0 : 1;
+    }
+    return 0;
+}
+
+int oracle_simulate(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc, const hsr_antenna_o *tx,
+                    const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl, int64_t budget, int64_t offset,
+                    float sample_weight, int precision, int threads, double *frame_out, double *weight_out) {
+    if (!sp || !rf || !fc || !tx || !rx || !fl || !frame_out || !weight_out || budget < 0) return 1;
+    if (fc->chirpCount <= 0 || fc->samplesPerChirp <= 0 || fc->channelCount <= 0) return 1;
+    if (fl->doGuiding) return 2;  // guided runs are not restated here
+    const Scene *s = static_cast<Scene *>(sp);
+    if (precision == 64)
+        return simulate<double>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
+    return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
+}
+
+int oracle_records(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc, const hsr_antenna_o *tx,
+                   const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl, int64_t first, int64_t count,
+                   int64_t offset, int max_records, oracle_record *out) {
+    if (!sp || !out || max_records <= 0) return 1;
+    const Scene *s = static_cast<Scene *>(sp);
+    Tracer<float> tr;
+    setup_tracer(tr, s, rf, tx, rx, fl);
+    tr.sampleIndexOffset = offset;
+    tr.frame.chirps = fc->chirpCount;
+    tr.frame.samples = fc->samplesPerChirp;
+    tr.frame.channels = fc->channelCount;
+    size_t n = size_t(fc->chirpCount) * fc->samplesPerChirp * fc->channelCount;
+    std::vector<float> data(2 * n, 0.f);
+    tr.frame.data = data.data();
+    tr.maxRecords = max_records;
+    for (int64_t i = 0; i < count; ++i) {
+        oracle_record *rec = out + i * max_records;
+        for (int k = 0; k < max_records; ++k) {
+            rec[k] = oracle_record{};
+            rec[k].depth = -1;
+        }
+        tr.records = rec;
+        tr.sample(first + i);
+    }
+    return 0;
+}
+
+void oracle_frame_splat(int chirps, int samples, int channels, float ic, float is, float ich, float re, float im,
+                        float *frame) {
+    Frame<float> f;
+    f.chirps = chirps;
+    f.samples = samples;
+    f.channels = channels;
+    f.data = frame;
+    frame_splat(f, ic, is, ich, Cx<float>{re, im});
+}
+
+void oracle_awr_evaluate(const float *d, float *H6) {
+    CV3<float> H = awr_evaluate(V3<float>{d[0], d[1], d[2]});
+    for (int i = 0; i < 3; ++i) {
+        H6[2 * i] = H.c[i].re;
+        H6[2 * i + 1] = H.c[i].im;
+    }
+}
+
+void oracle_uniform_sample_sphere(float u0, float u1, float *d) {
+    V3<float> v = uniform_sample_sphere(u0, u1);
+    d[0] = v.x;
+    d[1] = v.y;
+    d[2] = v.z;
+}
+
+void oracle_measure_ray(float dt, float startFreq, float freqSlope, float *out2) {
+    float angle = 2.f * Consts<float>::Pi * (startFreq - dt * freqSlope / 2.f) * dt;
+    Cx<float> c = cexpj(angle);
+    out2[0] = c.re;
+    out2[1] = c.im;
+}
+
+int64_t oracle_bvh_nodes(void *sp) { return int64_t(static_cast<Scene *>(sp)->bvh.nodes.size()); }
+
+}  // extern "C"
