@@ -1,0 +1,356 @@
+// Device LBVH build: replaces Embree's rtcCommitScene (libhussar/src/arch/cpu.cpp:32-47)
+// and OptiX's optixAccelBuild + compaction (src/arch/gpu.cpp:82-207).
+//
+//   1. per-triangle bounds and centroids, scene centroid bounds (k_bounds, k_centroid_bounds)
+//   2. 63-bit Morton code of each centroid, 21 bits per axis (k_morton)
+//   3. radix sort of (code, triangle id) pairs (CUB DeviceRadixSort)
+//   4. triangle records written in sorted order (k_write_tris)
+//   5. binary radix tree topology from the sorted codes (Karras 2012, k_karras)
+//   6. bottom-up box refit with one arrival counter per node (k_refit)
+// Leaves hold one triangle; node i stores the boxes of both its children.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <limits>
+
+#include "hsr_common.cuh"
+#include "hsr_internal.h"
+
+namespace hsr {
+
+namespace {
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Triangle AABB, padded so the FMA slab test stays conservative.
+__global__ void k_bounds(const float *__restrict__ v, const int32_t *__restrict__ idx, int64_t nt, float *__restrict__ lo,
+                         float *__restrict__ hi, unsigned *__restrict__ cbounds) {
+    int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (t >= nt) return;
+    float c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float x0 = v[3 * int64_t(idx[3 * t + 0]) + a];
+        float x1 = v[3 * int64_t(idx[3 * t + 1]) + a];
+        float x2 = v[3 * int64_t(idx[3 * t + 2]) + a];
+        float mn = fminf(x0, fminf(x1, x2)), mx = fmaxf(x0, fmaxf(x1, x2));
+        float pad = fmaxf(fabsf(mn), fabsf(mx)) * 4e-6f + 1e-6f;
+        lo[3 * t + a] = mn - pad;
+        hi[3 * t + a] = mx + pad;
+        c[a] = 0.5f * mn + 0.5f * mx;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        atomicMin(&cbounds[a], f2ord(c[a]));
+        atomicMax(&cbounds[3 + a], f2ord(c[a]));
+    }
+}
+
+__device__ __forceinline__ uint64_t expand21(uint64_t x) {
+    x &= 0x1fffffull;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float *__restrict__ lo, const float *__restrict__ hi, int64_t nt,
+                         const unsigned *__restrict__ cbounds, uint64_t *__restrict__ keys, int32_t *__restrict__ ids) {
+    int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (t >= nt) return;
+    uint64_t code = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float cmin = ord2f(cbounds[a]), cmax = ord2f(cbounds[3 + a]);
+        float c = 0.5f * lo[3 * t + a] + 0.5f * hi[3 * t + a];
+        float ext = cmax - cmin;
+        float u = ext > 0.f ? (c - cmin) / ext : 0.5f;
+        u = fminf(fmaxf(u, 0.f), 1.f);
+        uint64_t q = uint64_t(fminf(u * 2097152.f, 2097151.f));
+        code |= expand21(q) << (2 - a);
+    }
+    keys[t] = code;
+    ids[t] = int32_t(t);
+}
+
+__global__ void k_write_tris(const float *__restrict__ v, const int32_t *__restrict__ idx,
+                             const int32_t *__restrict__ sorted_ids, int64_t nt, DTri *__restrict__ tris) {
+    int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (s >= nt) return;
+    int64_t t = sorted_ids[s];
+    const float *p0 = v + 3 * int64_t(idx[3 * t + 0]);
+    const float *p1 = v + 3 * int64_t(idx[3 * t + 1]);
+    const float *p2 = v + 3 * int64_t(idx[3 * t + 2]);
+    DTri T;
+    T.v0 = make_float4(p0[0], p0[1], p0[2], __int_as_float(int(t)));
+    T.e1 = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.f);
+    T.e2 = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.f);
+    tris[s] = T;
+}
+
+// common prefix length of sorted keys i and j, with the index as a tie-breaker
+__device__ __forceinline__ int delta(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clzll((unsigned long long)(i ^ j));
+    return __clzll((unsigned long long)(a ^ b));
+}
+
+// Karras 2012: internal node i covers a key range; its split is the highest differing bit.
+__global__ void k_karras(const uint64_t *__restrict__ k, int64_t n, DNode *__restrict__ nodes,
+                         int32_t *__restrict__ parent_internal, int32_t *__restrict__ parent_leaf) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(k, n, i, i - d);
+    int64_t lmax = 2;
+    while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int64_t l = 0;
+    for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int64_t j = i + l * d;
+    int dnode = delta(k, n, i, j);
+    int64_t s = 0;
+    int64_t len = l;
+    int64_t t = (len + 1) >> 1;
+    while (true) {
+        if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+        t = (t + 1) >> 1;
+    }
+    int64_t gamma = i + s * d + (d < 0 ? -1 : 0);
+    int64_t first = i < j ? i : j, last = i < j ? j : i;
+    int c0, c1;
+    if (first == gamma) {
+        c0 = ~int(gamma);
+        parent_leaf[gamma] = int(i);
+    } else {
+        c0 = int(gamma);
+        parent_internal[gamma] = int(i);
+    }
+    if (last == gamma + 1) {
+        c1 = ~int(gamma + 1);
+        parent_leaf[gamma + 1] = int(i);
+    } else {
+        c1 = int(gamma + 1);
+        parent_internal[gamma + 1] = int(i);
+    }
+    nodes[i].d = make_int4(c0, c1, 0, 0);
+}
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Box child_box(const DNode &n, int which) {
+    Box b;
+    if (which == 0) {
+        b.lo[0] = n.a.x; b.hi[0] = n.a.y; b.lo[1] = n.a.z; b.hi[1] = n.a.w; b.lo[2] = n.c.x; b.hi[2] = n.c.y;
+    } else {
+        b.lo[0] = n.b.x; b.hi[0] = n.b.y; b.lo[1] = n.b.z; b.hi[1] = n.b.w; b.lo[2] = n.c.z; b.hi[2] = n.c.w;
+    }
+    return b;
+}
+
+// Bottom-up refit: a leaf's thread climbs while it is the second child to arrive.
+__global__ void k_refit(int64_t n, const int32_t *__restrict__ sorted_ids, const float *__restrict__ lo,
+                        const float *__restrict__ hi, DNode *nodes, const int32_t *__restrict__ parent_internal,
+                        const int32_t *__restrict__ parent_leaf, int *counters, int *depth_out) {
+    int64_t leaf = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (leaf >= n) return;
+    int p = parent_leaf[leaf];
+    int depth = 1;
+    while (p >= 0) {
+        __threadfence();
+        int prev = atomicAdd(&counters[p], 1);
+        if (prev == 0) return;  // the sibling subtree is not finished; its thread continues
+        __threadfence();
+        volatile DNode *vn = nodes;
+        int c[2] = {vn[p].d.x, vn[p].d.y};
+        Box bx[2];
+        for (int w = 0; w < 2; ++w) {
+            if (c[w] < 0) {
+                int64_t t = sorted_ids[~c[w]];
+                for (int a = 0; a < 3; ++a) {
+                    bx[w].lo[a] = lo[3 * t + a];
+                    bx[w].hi[a] = hi[3 * t + a];
+                }
+            } else {
+                DNode cn;
+                cn.a = make_float4(vn[c[w]].a.x, vn[c[w]].a.y, vn[c[w]].a.z, vn[c[w]].a.w);
+                cn.b = make_float4(vn[c[w]].b.x, vn[c[w]].b.y, vn[c[w]].b.z, vn[c[w]].b.w);
+                cn.c = make_float4(vn[c[w]].c.x, vn[c[w]].c.y, vn[c[w]].c.z, vn[c[w]].c.w);
+                Box b0 = child_box(cn, 0), b1 = child_box(cn, 1);
+                for (int a = 0; a < 3; ++a) {
+                    bx[w].lo[a] = fminf(b0.lo[a], b1.lo[a]);
+                    bx[w].hi[a] = fmaxf(b0.hi[a], b1.hi[a]);
+                }
+            }
+        }
+        vn[p].a.x = bx[0].lo[0]; vn[p].a.y = bx[0].hi[0]; vn[p].a.z = bx[0].lo[1]; vn[p].a.w = bx[0].hi[1];
+        vn[p].b.x = bx[1].lo[0]; vn[p].b.y = bx[1].hi[0]; vn[p].b.z = bx[1].lo[1]; vn[p].b.w = bx[1].hi[1];
+        vn[p].c.x = bx[0].lo[2]; vn[p].c.y = bx[0].hi[2]; vn[p].c.z = bx[1].lo[2]; vn[p].c.w = bx[1].hi[2];
+        p = parent_internal[p];
+        depth++;
+    }
+    atomicMax(depth_out, depth);
+}
+
+// Leaf depth statistics: each leaf walks to the root.
+__global__ void k_leaf_depth(int64_t n, const int32_t *__restrict__ parent_internal,
+                             const int32_t *__restrict__ parent_leaf, int *depth_out) {
+    int64_t leaf = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (leaf >= n) return;
+    int p = parent_leaf[leaf];
+    int depth = 1;
+    while (p >= 0 && depth < 1 << 20) {
+        p = parent_internal[p];
+        depth++;
+    }
+    atomicMax(depth_out, depth);
+}
+
+inline unsigned blocks_for(int64_t n, int t) { return unsigned((n + t - 1) / t); }
+
+}  // namespace
+
+// Builds tris/nodes for `scene` from device vertex/index arrays. Returns 0 or an hsr_status.
+int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
+              std::string &err) {
+    (void)nv;
+    s.tri_count = nt;
+    const int64_t n_nodes = nt >= 2 ? nt - 1 : 1;
+    s.node_count = n_nodes;
+    if (!dev_alloc(&s.tris, sizeof(DTri) * (size_t)std::max<int64_t>(nt, 1), err)) return 3;
+    if (!dev_alloc(&s.nodes, sizeof(DNode) * (size_t)n_nodes, err)) return 3;
+    if (nt < 2) {
+        // 0 or 1 triangle: one root whose two children are both slot 0. With no triangle,
+        // slot 0 is all zeros (zero determinant: never hit). A second visit of the only
+        // triangle is harmless. (An inverted box is not empty under the min/max slab test.)
+        if (cudaMemsetAsync(s.tris, 0, sizeof(DTri), st) != cudaSuccess) return 2;
+        DNode root;
+        const float inf = std::numeric_limits<float>::infinity();
+        root.a = make_float4(inf, -inf, inf, -inf);
+        root.b = make_float4(inf, -inf, inf, -inf);
+        root.c = make_float4(inf, -inf, inf, -inf);
+        root.d = make_int4(-1, -1, 0, 0);  // ~0 = slot 0
+        if (nt == 1) {
+            float hv[9];
+            int32_t hi[3];
+            if (cudaMemcpyAsync(hi, d_idx, sizeof(hi), cudaMemcpyDeviceToHost, st) != cudaSuccess) return 2;
+            cudaStreamSynchronize(st);
+            for (int k = 0; k < 3; ++k)
+                if (cudaMemcpyAsync(hv + 3 * k, d_v + 3 * (int64_t)hi[k], 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                                    st) != cudaSuccess)
+                    return 2;
+            cudaStreamSynchronize(st);
+            float lo[3], hiB[3];
+            for (int a = 0; a < 3; ++a) {
+                float mn = std::min(hv[a], std::min(hv[3 + a], hv[6 + a]));
+                float mx = std::max(hv[a], std::max(hv[3 + a], hv[6 + a]));
+                float pad = std::max(std::fabs(mn), std::fabs(mx)) * 4e-6f + 1e-6f;
+                lo[a] = mn - pad;
+                hiB[a] = mx + pad;
+            }
+            root.a = make_float4(lo[0], hiB[0], lo[1], hiB[1]);
+            root.c.x = lo[2];
+            root.c.y = hiB[2];
+            DTri T;
+            T.v0 = make_float4(hv[0], hv[1], hv[2], 0.f);  // bit pattern of int 0
+            T.e1 = make_float4(hv[3] - hv[0], hv[4] - hv[1], hv[5] - hv[2], 0.f);
+            T.e2 = make_float4(hv[6] - hv[0], hv[7] - hv[1], hv[8] - hv[2], 0.f);
+            if (cudaMemcpyAsync(s.tris, &T, sizeof(T), cudaMemcpyHostToDevice, st) != cudaSuccess) return 2;
+        }
+        if (cudaMemcpyAsync(s.nodes, &root, sizeof(root), cudaMemcpyHostToDevice, st) != cudaSuccess) return 2;
+        cudaStreamSynchronize(st);
+        s.max_depth = nt == 1 ? 1 : 0;
+        s.leaf_count = nt;
+        return 0;
+    }
+
+    float *lo = nullptr, *hi = nullptr;
+    unsigned *cb = nullptr;
+    uint64_t *keys = nullptr, *keys2 = nullptr;
+    int32_t *ids = nullptr, *ids2 = nullptr, *par_i = nullptr, *par_l = nullptr;
+    int *counters = nullptr, *depth = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int rc = 0;
+    auto fail = [&](int code) {
+        rc = code;
+        return code;
+    };
+    do {
+        if (!dev_alloc(&lo, sizeof(float) * 3 * nt, err) || !dev_alloc(&hi, sizeof(float) * 3 * nt, err) ||
+            !dev_alloc(&cb, sizeof(unsigned) * 6, err) || !dev_alloc(&keys, sizeof(uint64_t) * nt, err) ||
+            !dev_alloc(&keys2, sizeof(uint64_t) * nt, err) || !dev_alloc(&ids, sizeof(int32_t) * nt, err) ||
+            !dev_alloc(&ids2, sizeof(int32_t) * nt, err) || !dev_alloc(&par_i, sizeof(int32_t) * n_nodes, err) ||
+            !dev_alloc(&par_l, sizeof(int32_t) * nt, err) || !dev_alloc(&counters, sizeof(int) * n_nodes, err) ||
+            !dev_alloc(&depth, sizeof(int) * 2, err)) {
+            fail(3);
+            break;
+        }
+        unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+        cudaMemcpyAsync(cb, init, sizeof(init), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(counters, 0, sizeof(int) * n_nodes, st);
+        cudaMemsetAsync(depth, 0, sizeof(int) * 2, st);
+        cudaMemsetAsync(par_i, 0xff, sizeof(int32_t) * n_nodes, st);  // root keeps -1
+        const int T = 256;
+        k_bounds<<<blocks_for(nt, T), T, 0, st>>>(d_v, d_idx, nt, lo, hi, cb);
+        k_morton<<<blocks_for(nt, T), T, 0, st>>>(lo, hi, nt, cb, keys, ids);
+        note_launches(2);
+        if (cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, ids, ids2, (int)nt, 0, 63, st) !=
+            cudaSuccess) {
+            err = "radix sort size query failed";
+            fail(2);
+            break;
+        }
+        if (!dev_alloc(&tmp, tmp_bytes, err)) {
+            fail(3);
+            break;
+        }
+        if (cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, ids, ids2, (int)nt, 0, 63, st) !=
+            cudaSuccess) {
+            err = "radix sort failed";
+            fail(2);
+            break;
+        }
+        k_write_tris<<<blocks_for(nt, T), T, 0, st>>>(d_v, d_idx, ids2, nt, s.tris);
+        k_karras<<<blocks_for(nt - 1, T), T, 0, st>>>(keys2, nt, s.nodes, par_i, par_l);
+        k_refit<<<blocks_for(nt, T), T, 0, st>>>(nt, ids2, lo, hi, s.nodes, par_i, par_l, counters, depth);
+        k_leaf_depth<<<blocks_for(nt, T), T, 0, st>>>(nt, par_i, par_l, depth + 1);
+        note_launches(4);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            err = std::string("BVH build: ") + cudaGetErrorString(e);
+            fail(2);
+            break;
+        }
+        int hd[2];
+        cudaMemcpy(hd, depth, sizeof(hd), cudaMemcpyDeviceToHost);
+        s.max_depth = hd[1];
+        s.leaf_count = nt;
+    } while (false);
+    cudaFree(lo);
+    cudaFree(hi);
+    cudaFree(cb);
+    cudaFree(keys);
+    cudaFree(keys2);
+    cudaFree(ids);
+    cudaFree(ids2);
+    cudaFree(par_i);
+    cudaFree(par_l);
+    cudaFree(counters);
+    cudaFree(depth);
+    cudaFree(tmp);
+    return rc;
+}
+
+}  // namespace hsr

@@ -1,0 +1,161 @@
+// Device math shared by the GB300 kernels: constants, vectors, complex numbers and
+// the error/status word. Operation orders follow the reference's scalar code
+// (libhussar/include/hussar/core/geometry.h:69-143, libradar/include/radar/complex.h)
+// because the trace kernels are compiled with -fmad=false: every + - * / here rounds
+// exactly like the CPU restatement, so hit/miss decisions agree bit-for-bit.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hsr {
+
+// hussar.h:37-52, radar.h:107
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInv4Pi = 0.07957747154594766788f;
+constexpr float kSpeedOfLight = 299792458.f;
+constexpr float kEpsilon = 5e-5f;
+
+// Device status word bits (checked by the host after each synchronising call).
+enum StatusBits : unsigned {
+    kStatusStackOverflow = 1u << 0,   // traversal stack would have overflowed; ray treated as miss
+    kStatusBadBin = 1u << 1,          // a splat bin was outside the frame (guarded, skipped)
+    kStatusBadWorkItem = 1u << 2,     // work item index out of range (guarded)
+};
+
+struct f3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 scl3(float s, f3 a) { return f3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3 neg3(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+// 3-term reductions in the order x0 + (x1 + x2)
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + (a.y * b.y + a.z * b.z); }
+__device__ __forceinline__ float sqn3(f3 a) { return a.x * a.x + (a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ float nrm3(f3 a) { return sqrtf(sqn3(a)); }
+__device__ __forceinline__ f3 crs3(f3 a, f3 b) {
+    return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 div3(f3 a, float s) { return f3{a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 nrmz3(f3 a) {
+    float n = sqn3(a);
+    if (n > 0.f) {
+        float s = sqrtf(n);
+        return f3{a.x / s, a.y / s, a.z / s};
+    }
+    return a;
+}
+
+struct cf {
+    float re, im;
+};
+__device__ __forceinline__ cf cadd(cf a, cf b) { return cf{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cf csub(cf a, cf b) { return cf{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cf cmul(cf a, cf b) {
+    float r = a.re * b.re - a.im * b.im;
+    float i = a.re * b.im + a.im * b.re;
+    return cf{r, i};
+}
+__device__ __forceinline__ cf cscl(cf a, float s) { return cf{a.re * s, a.im * s}; }
+__device__ __forceinline__ cf cdiv(cf a, float s) { return cf{a.re / s, a.im / s}; }
+__device__ __forceinline__ cf cconj(cf a) { return cf{a.re, -a.im}; }
+
+// complex 3-vector (the ray's H field)
+struct c3 {
+    cf v[3];
+};
+__device__ __forceinline__ c3 c3_real(f3 a) {
+    c3 r;
+    r.v[0] = cf{a.x, 0.f};
+    r.v[1] = cf{a.y, 0.f};
+    r.v[2] = cf{a.z, 0.f};
+    return r;
+}
+__device__ __forceinline__ c3 c3_scl(c3 a, float s) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a.v[i] = cscl(a.v[i], s);
+    return a;
+}
+__device__ __forceinline__ c3 c3_div(c3 a, float s) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a.v[i] = cdiv(a.v[i], s);
+    return a;
+}
+__device__ __forceinline__ c3 c3_cmul(c3 a, cf s) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a.v[i] = cmul(a.v[i], s);
+    return a;
+}
+__device__ __forceinline__ c3 c3_sub(c3 a, c3 b) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a.v[i] = csub(a.v[i], b.v[i]);
+    return a;
+}
+// real x complex cross product with the conjugated result (Eigen MatrixBase::cross)
+__device__ __forceinline__ c3 crs_rc(f3 a, const c3 &b) {
+    c3 r;
+    r.v[0] = cconj(csub(cscl(b.v[2], a.y), cscl(b.v[1], a.z)));
+    r.v[1] = cconj(csub(cscl(b.v[0], a.z), cscl(b.v[2], a.x)));
+    r.v[2] = cconj(csub(cscl(b.v[1], a.x), cscl(b.v[0], a.y)));
+    return r;
+}
+// sum_i a_i b_i for real a
+__device__ __forceinline__ cf dot_rc(f3 a, const c3 &b) {
+    return cadd(cscl(b.v[0], a.x), cadd(cscl(b.v[1], a.y), cscl(b.v[2], a.z)));
+}
+// Hermitian sum_i conj(a_i) b_i (geometry.h:138)
+__device__ __forceinline__ cf dot_cc(const c3 &a, const c3 &b) {
+    return cadd(cmul(cconj(a.v[0]), b.v[0]), cadd(cmul(cconj(a.v[1]), b.v[1]), cmul(cconj(a.v[2]), b.v[2])));
+}
+// Eigen isZero(1e-20): every |h_i|^2 <= 1e-20f * 1e-20f (a float denormal; no FTZ here)
+__device__ __forceinline__ bool c3_is_zero(const c3 &a) {
+    const float prec = 1e-20f;
+    const float lim = prec * prec;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float a2 = a.v[i].re * a.v[i].re + a.v[i].im * a.v[i].im;
+        if (!(a2 <= lim)) return false;
+    }
+    return true;
+}
+
+// Row-major 3x3
+struct m33 {
+    float m[9];
+};
+__device__ __forceinline__ f3 mulv(const m33 &M, f3 v) {
+    return f3{M.m[0] * v.x + (M.m[1] * v.y + M.m[2] * v.z), M.m[3] * v.x + (M.m[4] * v.y + M.m[5] * v.z),
+              M.m[6] * v.x + (M.m[7] * v.y + M.m[8] * v.z)};
+}
+__device__ __forceinline__ f3 mulTv(const m33 &M, f3 v) {
+    return f3{M.m[0] * v.x + (M.m[3] * v.y + M.m[6] * v.z), M.m[1] * v.x + (M.m[4] * v.y + M.m[7] * v.z),
+              M.m[2] * v.x + (M.m[5] * v.y + M.m[8] * v.z)};
+}
+__device__ __forceinline__ c3 mulcv(const m33 &M, const c3 &h) {
+    c3 r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        r.v[i] = cadd(cscl(h.v[0], M.m[3 * i]), cadd(cscl(h.v[1], M.m[3 * i + 1]), cscl(h.v[2], M.m[3 * i + 2])));
+    return r;
+}
+
+// Scene storage on the device -------------------------------------------------------
+// Triangle record: v0, e1 = v1 - v0, e2 = v2 - v0 (exactly the float differences the
+// CPU restatement forms), original primitive id in v0.w. 48 bytes, three 16-byte loads.
+struct __align__(16) DTri {
+    float4 v0;
+    float4 e1;
+    float4 e2;
+};
+
+// Binary BVH node holding both child boxes (64 bytes, four 16-byte loads).
+// child >= 0: internal node index; child < 0: leaf, triangle slot ~child.
+struct __align__(16) DNode {
+    float4 a;  // c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y
+    float4 b;  // c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y
+    float4 c;  // c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z
+    int4 d;    // child0, child1, unused, unused
+};
+
+}  // namespace hsr

@@ -1,0 +1,90 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "../../include/hsr_gb300.h"
+
+namespace hsr {
+
+struct DTri;
+struct DNode;
+
+// A resident scene: triangles + BVH on the device, plus per-scene scratch reused by
+// every simulate call on this scene (calls on one scene must not overlap).
+struct SceneDev {
+    int device = 0;
+    int64_t tri_count = 0;
+    int64_t node_count = 0;
+    int64_t leaf_count = 0;
+    int max_depth = 0;
+    DTri *tris = nullptr;
+    DNode *nodes = nullptr;
+    // scratch
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    unsigned *status = nullptr;  // device status word + work counter
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_kernel_ms = 0.f;
+    bool timing_valid = false;
+    int sm_count = 0;
+};
+
+template <typename T> inline bool dev_alloc(T **p, size_t bytes, std::string &err) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        err = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
+        *p = nullptr;
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+void note_launches(int64_t n);
+
+int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
+              std::string &err);
+
+// Launch parameters of the trace kernel (POD, passed by value).
+struct TraceParams {
+    const DNode *nodes;
+    const DTri *tris;
+    hsr_rf_config rf;
+    hsr_tracer_flags flags;
+    int32_t samples;        // samplesPerChirp (N)
+    int32_t pose_count;
+    const hsr_antenna *tx;  // [pose_count]
+    const hsr_antenna *rx;  // [pose_count]
+    const int64_t *budget;  // [pose_count]
+    const int64_t *offset;  // [pose_count] Halton index offset
+    const int64_t *tile_start;  // [pose_count + 1] prefix sum of tiles per pose
+    float sample_weight;
+    int32_t tile;           // samples per work item
+    double *acc;            // [pose_count][N] complex (re, im) accumulators
+    unsigned *status;       // status word
+    unsigned *work_counter; // dynamic work item counter
+    void *records;          // optional PathRecord[budget][max_rec] (tests)
+    int32_t max_rec;
+    unsigned long long *counters;  // optional [nodes, tris, rays] (counting instantiation)
+    // fine-histogram mode
+    int32_t fine_bins;      // K = N * oversample
+    float *fine;            // [pose_count][3 moments][K] complex, device
+};
+
+// Launches (all asynchronous on `st`).
+int launch_trace(const TraceParams &p, int phase_mode, int splat_mode, int grid, cudaStream_t st, std::string &err);
+int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, int64_t *tile_start, cudaStream_t st);
+int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, const int64_t *budget, float sample_weight,
+                    int normalise, float *out_rows, cudaStream_t st);
+int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,
+                       const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
+                       cudaStream_t st);
+int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
+int trace_blocks_per_sm(int samples, int splat_mode, int fine_bins);
+
+}  // namespace hsr

@@ -200,6 +200,24 @@ hsr_status hsr_simulate_batch(hsr_scene *scene, const hsr_rf_config *rf,
                               const int64_t *index_offset, int32_t phase_mode,
                               int32_t splat_mode, float *out_rows, void *stream);
 
+/* Test support: traces samples index_offset + [0, budget) of one pose and writes one
+ * record per next-event estimate (path.h:292-397) into the HOST array `records`
+ * (budget * max_records entries of 9 x 4 bytes: int32 depth (-1 = unused), int32
+ * splatted, float time, v_re, v_im, dphase, bin, value_re, value_im). */
+hsr_status hsr_debug_records(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
+                             const hsr_tracer_flags *flags, const hsr_antenna *tx, const hsr_antenna *rx,
+                             int64_t budget, int64_t index_offset, int32_t max_records, void *records);
+
+/* Measurement support: runs the counting instantiation of the trace kernel on a batch
+ * (host arrays, as hsr_simulate_batch) and returns the exact traversal work of that
+ * launch: out_counts[0] BVH nodes fetched (64 B each), [1] triangles fetched (48 B each),
+ * [2] rays traced (closest-hit + shadow). */
+hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
+                                      int32_t samples_per_chirp, const hsr_tracer_flags *flags,
+                                      int32_t pose_count, const hsr_antenna *tx,
+                                      const hsr_antenna *rx, const int64_t *budget,
+                                      const int64_t *index_offset, int64_t *out_counts);
+
 /* Timing of the most recent batch launch on this scene: device milliseconds of the
  * trace kernel alone, measured with CUDA events on the launching stream. */
 hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);

@@ -1,0 +1,158 @@
+/*
+ * hussar/gb300.h — C++ drop-in backend over the C ABI (hsr_gb300.h).
+ *
+ * hussar::gb300::Backend has the constructor and run() of the reference backends:
+ *   Backend(const TriangleMesh &mesh, Integrator &integrator)   (arch/cpu.h:18-20, arch/gpu.h:18-20)
+ *   void run(const Scene &scene, long budget, bool *interruptFlag = nullptr)
+ *                                                               (arch/cpu.h:44-46, arch/gpu.h:26-32)
+ * and is used the same way: PathTracer::run<Backend>(backend, scene, samples) calls
+ * backend.run(scene, budget, flag) once per schedule step (integrators/path.h:171-224).
+ *
+ * It is duck-typed like the reference's backends, so it works with
+ *  - libhussar's own types (Eigen vectors, radar::Frame, hussar::PathTracer) once
+ *    PathTracer befriends hussar::gb300::BackendAccess, and
+ *  - the self-contained mirror types in hussar/gb300_types.h.
+ * Requirements on the types:
+ *   mesh.vertexBuffer[i].x()/.y()/.z(), mesh.indexBuffer[i].v0/.v1/.v2
+ *   scene.rfConfig.{startFreq,freqSlope,adcRate,idleTime,rampTime,antennaDelay}
+ *   scene.tx/rx.position().x().., scene.tx/rx.rotation()(row, col)
+ *   integrator: the public flags of path.h:153-169, produceDebugImage, and (through
+ *   BackendAccess) frame, totalWeight, sampleIndexOffset, currentSampleWeight.
+ * Errors: a non-OK hsr_status becomes std::runtime_error (the reference's
+ * sutil::Exception derives from std::runtime_error, Exception.h:243); an interrupted
+ * run returns silently like cpu::Backend (arch/cpu.h:25).
+ */
+#ifndef HUSSAR_GB300_H
+#define HUSSAR_GB300_H
+
+#include <cstdint>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../hsr_gb300.h"
+
+namespace hussar {
+namespace gb300 {
+
+inline void check(hsr_status s) {
+    if (s != HSR_OK && s != HSR_ERR_INTERRUPTED) throw std::runtime_error(std::string("gb300: ") + hsr_last_error());
+}
+
+/* Access to the integrator state the reference keeps protected/private
+ * (path.h:140, 457-464; integrator.h:170). Specialise or befriend as needed. */
+template <typename Integrator> struct BackendAccess {
+    static auto &frame(Integrator &it) { return it.frame; }
+    static double totalWeight(Integrator &it) { return double(it.totalWeight); }
+    static void setTotalWeight(Integrator &it, double w) { it.totalWeight = w; }
+    static long sampleIndexOffset(Integrator &it) { return long(it.sampleIndexOffset); }
+    static float currentSampleWeight(Integrator &it) { return float(it.currentSampleWeight); }
+};
+
+template <typename Vec> inline void put3(float *out, const Vec &v) {
+    out[0] = float(v.x());
+    out[1] = float(v.y());
+    out[2] = float(v.z());
+}
+
+template <typename Antenna> inline hsr_antenna to_hsr(const Antenna &a) {
+    hsr_antenna r;
+    put3(r.position, a.position());
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.rotation[3 * i + j] = float(a.rotation()(i, j));
+    return r;
+}
+
+template <typename Rf> inline hsr_rf_config to_hsr_rf(const Rf &rf) {
+    return hsr_rf_config{float(rf.startFreq), float(rf.freqSlope), float(rf.adcRate),
+                         float(rf.idleTime),  float(rf.rampTime),  float(rf.antennaDelay)};
+}
+
+template <typename Integrator> inline hsr_tracer_flags to_hsr_flags(const Integrator &it) {
+    hsr_tracer_flags f;
+    f.onlyIndirect = it.onlyIndirect;
+    f.maxDepth = it.maxDepth;
+    f.useGeometricalOptics = it.useGeometricalOptics;
+    f.poDiffraction = it.poDiffraction;
+    f.doGuiding = 0;  // the schedule is the integrator's; each backend run is plain
+    f.clearBeforeIteration = it.clearBeforeIteration;
+    f.correctPhase = it.correctPhase;
+    f.filterGuiding = it.filterGuiding;
+    f.doFiltering = it.doFiltering;
+    f.filteringSphere = it.filteringSphere;
+    f.produceDebugImage = it.produceDebugImage;
+    f.filteringMin = float(it.filteringMin);
+    f.filteringMax = float(it.filteringMax);
+    f.filteringRadius = float(it.filteringRadius);
+    return f;
+}
+
+/* The scene as the C ABI sees it. */
+struct SceneView {
+    hsr_rf_config rf;
+    hsr_antenna tx, rx;
+};
+
+struct Backend {
+    template <typename Mesh, typename Integrator>
+    Backend(const Mesh &mesh, Integrator &integrator) {
+        std::vector<float> v(3 * mesh.vertexBuffer.size());
+        for (size_t i = 0; i < mesh.vertexBuffer.size(); ++i) put3(&v[3 * i], mesh.vertexBuffer[i]);
+        std::vector<int32_t> idx(3 * mesh.indexBuffer.size());
+        for (size_t i = 0; i < mesh.indexBuffer.size(); ++i) {
+            idx[3 * i] = mesh.indexBuffer[i].v0;
+            idx[3 * i + 1] = mesh.indexBuffer[i].v1;
+            idx[3 * i + 2] = mesh.indexBuffer[i].v2;
+        }
+        check(hsr_scene_create(v.data(), int64_t(mesh.vertexBuffer.size()), idx.data(),
+                               int64_t(mesh.indexBuffer.size()), &m_scene));
+        // the integrator is held by reference and must outlive the backend (arch/cpu.h:21)
+        m_run = [this, &integrator](const SceneView &sv, long budget, bool *interruptFlag) {
+            using A = BackendAccess<Integrator>;
+            auto &frame = A::frame(integrator);
+            auto fc = frame.config();
+            hsr_frame_config f{fc.chirpCount, fc.samplesPerChirp, fc.channelCount};
+            const size_t n = size_t(fc.chirpCount) * fc.samplesPerChirp * fc.channelCount;
+            std::vector<float> buf(2 * n);
+            for (size_t i = 0; i < n; ++i) {
+                buf[2 * i] = frame(i).real();
+                buf[2 * i + 1] = frame(i).imag();
+            }
+            hsr_tracer_flags fl = to_hsr_flags(integrator);
+            double w = A::totalWeight(integrator);
+            int32_t flag = (interruptFlag && *interruptFlag) ? 1 : 0;
+            hsr_status s = hsr_backend_run(m_scene, &sv.rf, &f, &sv.tx, &sv.rx, &fl, budget,
+                                           A::sampleIndexOffset(integrator), A::currentSampleWeight(integrator),
+                                           HSR_PHASE_REFERENCE_FP32, buf.data(), &w, &flag);
+            check(s);
+            if (s == HSR_ERR_INTERRUPTED) return;
+            for (size_t i = 0; i < n; ++i) {
+                frame(i).real() = buf[2 * i];
+                frame(i).imag() = buf[2 * i + 1];
+            }
+            A::setTotalWeight(integrator, w);
+        };
+    }
+
+    Backend(const Backend &) = delete;
+    Backend &operator=(const Backend &) = delete;
+
+    ~Backend() { hsr_scene_destroy(m_scene); }
+
+    template <typename Scene> void run(const Scene &scene, long budget, bool *interruptFlag = nullptr) {
+        SceneView sv{to_hsr_rf(scene.rfConfig), to_hsr(scene.tx), to_hsr(scene.rx)};
+        m_run(sv, budget, interruptFlag);
+    }
+
+    hsr_scene *handle() const { return m_scene; }
+
+private:
+    hsr_scene *m_scene = nullptr;
+    std::function<void(const SceneView &, long, bool *)> m_run;
+};
+
+}  // namespace gb300
+}  // namespace hussar
+
+#endif

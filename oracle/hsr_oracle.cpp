@@ -244,7 +244,11 @@ template <typename R> static inline R radical_inverse(uint64_t v, unsigned dim) 
 template <typename R> struct Halton {
     uint64_t index = 0;
     uint16_t dim = 0;
-    R get1D() { return radical_inverse<R>(index, dim++); }
+    bool float_samples = false;  // FP64 run of exactly the FP32 run's (float) sample values
+    R get1D() {
+        R u = radical_inverse<R>(index, dim++);
+        return float_samples ? R(float(radical_inverse<float>(index, unsigned(dim - 1)))) : u;
+    }
 };
 
 // ----------------------------------------------------------------------------------
@@ -751,6 +755,7 @@ template <typename R> struct Tracer {
     Frame<R> frame;
     R currentSampleWeight = 1;
     int64_t sampleIndexOffset = 0;
+    bool floatSamples = false;
     oracle_record *records = nullptr;  // optional per-sample event log
     int maxRecords = 0;
 
@@ -802,6 +807,7 @@ template <typename R> struct Tracer {
         Halton<R> sampler;
         sampler.index = uint64_t(sampleIndexOffset + index);
         sampler.dim = 0;
+        sampler.float_samples = floatSamples;
         const R maxDist = rf.adcRate / rf.freqSlope * Consts<R>::SpeedOfLight;
         const R sampleWeight = currentSampleWeight;
         R primaryPdf = 1;
@@ -991,9 +997,10 @@ template <typename R>
 static int simulate(const Scene *s, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
                     int64_t budget, int64_t offset, float sampleWeight, int threads, double *frame_out,
-                    double *weight_out) {
+                    double *weight_out, bool floatSamples = false) {
     Tracer<R> tr;
     setup_tracer(tr, s, rf, tx, rx, fl);
+    tr.floatSamples = floatSamples;
     tr.currentSampleWeight = R(sampleWeight);
     tr.sampleIndexOffset = offset;
     tr.frame.chirps = fc->chirpCount;
@@ -1080,8 +1087,9 @@ int oracle_simulate(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_
     if (fc->chirpCount <= 0 || fc->samplesPerChirp <= 0 || fc->channelCount <= 0) return 1;
     if (fl->doGuiding) return 2;  // guided runs are not restated here
     const Scene *s = static_cast<Scene *>(sp);
-    if (precision == 64)
-        return simulate<double>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
+    if (precision == 64 || precision == 65)
+        return simulate<double>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out,
+                                precision == 65);
     return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
 }
 

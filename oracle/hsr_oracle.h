@@ -52,7 +52,8 @@ int oracle_intersect(void *scene, int64_t count, const float *o, const float *d,
                      float *t_out, float *p_out, float *n_out, int32_t *prim_out);
 int oracle_visible(void *scene, int64_t count, const float *o, const float *d, const float *tfar,
                    int32_t *vis);
-/* precision: 32 (reference single-precision semantics) or 64 (FP64 oracle).
+/* precision: 32 (reference single-precision semantics), 64 (FP64 oracle) or 65 (FP64
+ * oracle fed the float-rounded Halton values of the FP32 run: the same sample set).
  * frame_out: 2*chirps*samples*channels doubles, ADDED to. */
 int oracle_simulate(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
