@@ -241,6 +241,13 @@ def run_gb300(args, rank, world, local_rank, dist):
     ms = max_over_ranks(dist, sum(step_ms) / len(step_ms))
     value = world * S / (ms / 1000.0)
 
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
+                              "steps": args.steps, "ms_per_step": ms, "kernel_only": True,
+                              "gpu_launches": int(launches), "clocks": clk}), flush=True)
+        return
+
     # trace-kernel time alone (events around the kernel inside the library), for the roofline
     kms = ctypes.c_float()
     flush.fill_(1)
@@ -307,6 +314,8 @@ def main():
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
     ap.add_argument("--kernel-times", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="timed steps only (no e2e, counting, CPU baseline): the profiling command")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     dist = init_dist(world)

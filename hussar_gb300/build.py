@@ -23,6 +23,7 @@ UNITS = {
     "hsr_api.cu": [],
     "hsr_bvh.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
+    "hsr_wave.cu": ["-fmad=false"],
 }
 
 

@@ -13,6 +13,7 @@
 namespace hsr {
 
 static thread_local std::string g_err;
+int g_path_kernel = 0;
 static std::atomic<int64_t> g_launches{0};
 
 void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -133,10 +134,15 @@ static hsr_status enqueue_batch(SceneDev &sc, const Scratch &s, const hsr_rf_con
     p.records = records;
     p.max_rec = max_rec;
     p.counters = counters;
-    int grid = sc.sm_count * trace_blocks_per_sm(N, splat_mode, 0);
+    const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
+    int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N) : trace_blocks_per_sm(N, splat_mode, 0));
     cudaEventRecord(sc.ev0, st);
     std::string err;
-    if (launch_trace(p, phase_mode, splat_mode, grid, st, err) != 0) return fail(HSR_ERR_CUDA, err);
+    if (wave) {
+        if (launch_wave(p, phase_mode, grid, st, err) != 0) return fail(HSR_ERR_CUDA, err);
+    } else if (launch_trace(p, phase_mode, splat_mode, grid, st, err) != 0) {
+        return fail(HSR_ERR_CUDA, err);
+    }
     cudaEventRecord(sc.ev1, st);
     sc.timing_valid = true;
     if (launch_finalize(s.acc, P, N, s.budget, sample_weight, normalise, d_out_rows, st) != 0)
@@ -512,6 +518,12 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int
     for (int i = 0; i < 3; ++i) out_counts[i] = int64_t(h[i]);
     if (st == HSR_OK) st = read_status(s->dev, sc, 0);
     return st;
+}
+
+hsr_status hsr_set_path_kernel(int32_t kind) {
+    if (kind != 0 && kind != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "kind must be 0 or 1");
+    g_path_kernel = kind;
+    return HSR_OK;
 }
 
 hsr_status hsr_last_kernel_ms(const hsr_scene *s, float *out_ms) {

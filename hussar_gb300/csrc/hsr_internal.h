@@ -85,6 +85,11 @@ int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, cons
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st);
 int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
+size_t wave_smem_bytes(int samples);
+int wave_blocks_per_sm(int samples);
+int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
+// 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel
+extern int g_path_kernel;
 int trace_blocks_per_sm(int samples, int splat_mode, int fine_bins);
 
 }  // namespace hsr

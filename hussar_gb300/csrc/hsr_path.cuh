@@ -1,0 +1,398 @@
+// Per-path device math shared by the trace kernels: Halton sampling, the antenna
+// model, physical-optics re-radiation, next-event estimation, phase/bin evaluation and
+// the frame splat. Each function restates one piece of libhussar's PathTracer
+// (file:line given per function). Both kernels call the same functions, so they
+// compute identical per-path values.
+#pragma once
+#include <math_constants.h>
+
+#include "hsr_common.cuh"
+#include "hsr_internal.h"
+#include "hsr_traverse.cuh"
+
+namespace hsr {
+
+// radicalInverse<base> (libhussar/include/hussar/samplers/halton.h:38-54)
+template <int kBase> __device__ __forceinline__ float radical_inverse(uint64_t v) {
+    const float invBase = 1.f / float(kBase);
+    float invBaseN = 1.f;
+    uint64_t reversed;
+    if (v < (1ull << 26)) {
+        // below 2^26 the reversed digits of every base <= 29 stay below 29 * 2^26 < 2^32:
+        // the same integer in 32-bit arithmetic (cheaper constant divisions)
+        unsigned w = unsigned(v), rev = 0;
+        while (w) {
+            unsigned next = w / kBase;
+            unsigned digit = w - next * kBase;
+            rev = rev * kBase + digit;
+            invBaseN *= invBase;
+            w = next;
+        }
+        reversed = rev;
+    } else {
+        reversed = 0;
+        while (v) {
+            uint64_t next = v / kBase;
+            uint64_t digit = v - next * kBase;
+            reversed = reversed * kBase + digit;
+            invBaseN *= invBase;
+            v = next;
+        }
+    }
+    const float ome = 0.99999994f;  // nextafter(1.f, 0.f)
+    return fminf(__ull2float_rn(reversed) * invBaseN, ome);
+}
+
+// HaltonSampler::get1D dimension table (halton.h:56-67; dims >= 10 return 0, :1082-1084)
+__device__ __forceinline__ float halton(uint64_t index, int dim) {
+    switch (dim) {
+        case 0: return radical_inverse<2>(index);
+        case 1: return radical_inverse<3>(index);
+        case 2: return radical_inverse<5>(index);
+        case 3: return radical_inverse<7>(index);
+        case 4: return radical_inverse<11>(index);
+        case 5: return radical_inverse<13>(index);
+        case 6: return radical_inverse<17>(index);
+        case 7: return radical_inverse<19>(index);
+        case 8: return radical_inverse<23>(index);
+        case 9: return radical_inverse<29>(index);
+        default: return 0.f;
+    }
+}
+
+struct Ant {
+    f3 pos;
+    m33 rot;
+};
+
+__device__ __forceinline__ Ant load_ant(const hsr_antenna *a) {
+    Ant r;
+    r.pos = mk3(__ldg(&a->position[0]), __ldg(&a->position[1]), __ldg(&a->position[2]));
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.rot.m[i] = __ldg(&a->rotation[i]);
+    return r;
+}
+
+// UniformSampleSphere (libhussar/include/hussar/core/sampling.h:38-43)
+__device__ __forceinline__ f3 uniform_sample_sphere(float u0, float u1) {
+    float phi = 2.f * kPi * u0;
+    float y = 2.f * u1 - 1.f;
+    float r = sqrtf(fmaxf(0.f, 1.f - y * y));
+    float s, c;
+    sincosf(phi, &s, &c);
+    return mk3(-r * s, y, -r * c);
+}
+
+// AWRAngularDistribution::evaluate (libhussar/include/hussar/core/emitter.h:126-136):
+// H = (0,1,0) x d scaled by 2.622/(cos_h-1.8)^6 and 0.625/(cos_e-1.5)^4. The reference
+// forms the two scale factors in double; here they are single precision (a few ulps).
+__device__ __forceinline__ c3 awr_eval(f3 d) {
+    float cos_h = sqrtf(1.f - d.x * d.x);
+    float cos_e = sqrtf(1.f - d.y * d.y);
+    float a = cos_h - 1.8f;
+    float a2 = a * a;
+    float s1 = 2.622f / (a2 * a2 * a2);
+    float b = cos_e - 1.5f;
+    float b2 = b * b;
+    float s2 = 0.625f / (b2 * b2);
+    c3 H;
+    H.v[0] = cf{(d.z * s1) * s2, 0.f};
+    H.v[1] = cf{0.f, 0.f};
+    H.v[2] = cf{((-d.x) * s1) * s2, 0.f};
+    return H;
+}
+
+// NFAntenna::sample (emitter.h:174-180): primary ray from the TX antenna
+__device__ __forceinline__ void antenna_sample(const Ant &tx, float u0, float u1, f3 &d, c3 &H) {
+    f3 ld = uniform_sample_sphere(u0, u1);
+    c3 lH = c3_div(awr_eval(ld), kInv4Pi);
+    d = mulv(tx.rot, ld);
+    H = mulcv(tx.rot, lH);
+}
+
+// SurfaceEmitter::evaluate (emitter.h:64-70): J = 2 n x H_in; H = d x J; zero behind the surface
+__device__ __forceinline__ c3 surface_eval(f3 inc_n, const c3 &inc_H, f3 d) {
+    c3 J = c3_scl(crs_rc(inc_n, inc_H), 2.f);
+    c3 H = crs_rc(d, J);
+    if (dot3(d, inc_n) < 0.f) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) H.v[i] = cf{0.f, 0.f};
+    }
+    return H;
+}
+
+// SurfaceEmitter::connect green's function (emitter.h:72-81)
+__device__ __forceinline__ cf green(float k0, float r) {
+    cf g = cf{1.f / fmaxf(r, 1e-3f), k0};
+    return cdiv(g, 4.f * kPi * r);
+}
+
+// Integrator::reflectRay (integrator.h:164-168): d' = R(), H' = 2 n (n.H) - H
+__device__ __forceinline__ void reflect(f3 n, f3 &d, c3 &H) {
+    f3 wi = neg3(d);
+    d = sub3(scl3(2.f * dot3(n, wi), n), wi);
+    cf nh = dot_rc(n, H);
+    f3 n2 = scl3(2.f, n);
+    c3 t;
+    t.v[0] = cscl(nh, n2.x);
+    t.v[1] = cscl(nh, n2.y);
+    t.v[2] = cscl(nh, n2.z);
+    H = c3_sub(t, H);
+}
+
+// safe_modulo(int, unsigned) of radar.h:91-96, including its unsigned wrap of negative values
+__device__ __forceinline__ int ref_mod(int a, int n) {
+    if (a >= 0) return a < n ? a : a % n;
+    return int(unsigned(a) % unsigned(n));
+}
+
+// One next-event estimate (path.h:292-397 with Integrator::splat's index/phase,
+// integrator.h:113-135): the value the sample adds to the frame and where.
+struct NeeOut {
+    float time;    // nee.ray.time (before antennaDelay)
+    cf v;          // measurement after scaling and filtering
+    float dphase;
+    float sample;  // fractional range bin
+    cf value;      // weight * v * measureRay(dt)
+    bool splat;    // passed the splat early-out
+};
+
+// Returns false when the estimate is occluded or skipped (no record, no splat).
+// depth == 0: direct TX->RX connection (only with onlyIndirect = false).
+template <int kPhase, bool kCount>
+__device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, const Ant &rx, int depth, f3 o, f3 d,
+                                         f3 tmpd, f3 hit_n, const c3 &inc_H, const c3 &H, float time, double plen,
+                                         float r, float cosTheta, float freq, NeeOut &out, TraversalCounters *cnt,
+                                         unsigned *rays) {
+    const hsr_rf_config &rf = p.rf;
+    const hsr_tracer_flags &fl = p.flags;
+    // NFAntenna::nee (emitter.h:195-203)
+    f3 nd = sub3(rx.pos, o);
+    float rr = nrm3(nd);
+    nd = div3(nd, rr);
+    const float tMax = rr;
+    c3 Hrx = mulcv(rx.rot, awr_eval(mulTv(rx.rot, neg3(nd))));
+    if (!fl.poDiffraction) {
+        if (kCount) (*rays)++;
+        if (any_hit<kCount>(p.nodes, p.tris, o, nd, kEpsilon, tMax, p.status, cnt)) return false;
+    }
+    const float nt = tMax;
+    f3 no = o;
+    float ntime = time;
+    double nlen = plen;
+    c3 nH;
+    if (depth == 0) {
+        // NFAntenna::evaluate + connect (emitter.h:182-193)
+        no = tx.pos;
+        nH = mulcv(tx.rot, awr_eval(mulTv(tx.rot, nd)));
+        ntime += nt / kSpeedOfLight;
+        nlen += double(nt);
+        nH = c3_scl(nH, 1.f / (4.f * kPi * nt));
+    } else {
+        nH = surface_eval(hit_n, inc_H, nd);
+        ntime += nt / kSpeedOfLight;
+        nlen += double(nt);
+        nH = c3_cmul(nH, green(2.f * kPi * freq / kSpeedOfLight, nt));
+    }
+    cf v = dot_cc(nH, Hrx);
+    const float wavelength = kSpeedOfLight / freq;
+    float dphase = 0.f;
+    if (depth > 0) {
+        if (fl.correctPhase) {
+            f3 rxPos = add3(no, scl3(nt, nd));
+            f3 virtualTx = sub3(no, scl3(r, d));
+            float dist = nrm3(sub3(virtualTx, rxPos));
+            ntime = dist / kSpeedOfLight;
+            nlen = double(dist);
+            float pw = kPi * fl.filteringRadius * wavelength;
+            v = cdiv(cscl(dot_cc(H, Hrx), kPi * dist), pw * pw);
+            v = cdiv(v, 4.f * kPi);
+        } else if (fl.useGeometricalOptics) {
+            v = cscl(v, r / cosTheta);
+            v = cdiv(v, 4.f * kPi);
+            if (cosTheta < 0.001f) return false;  // (double)cosTheta < 1e-3
+        }
+        if (fl.filteringSphere) {
+            f3 rxPos = add3(no, scl3(nt, nd));
+            float lam = fmaxf(0.f, dot3(d, sub3(rxPos, o)));
+            dphase = nrm3(sub3(add3(o, scl3(lam, d)), rxPos));
+        } else {
+            float c = dot3(nrmz3(sub3(nd, tmpd)), hit_n);
+            dphase = r * sqrtf(1.f - c * c) / c;
+        }
+        dphase /= wavelength;
+        if (fl.doFiltering) {
+            if (fl.filteringSphere) {
+                if (dphase > fl.filteringRadius) {
+                    if (fl.correctPhase) {
+                        v = cf{0.f, 0.f};
+                    } else {
+                        float q = dphase / fl.filteringRadius - 1.f;
+                        float taper = fmaxf(float(1.0 - 0.20 * double(q)), 0.f);
+                        v = cscl(v, taper);
+                    }
+                }
+            } else {
+                if (dphase > fl.filteringMax) v = cf{0.f, 0.f};
+                if (dphase > fl.filteringMin)
+                    v = cscl(v, (fl.filteringMax - dphase) / (fl.filteringMax - fl.filteringMin));
+            }
+        }
+    }
+    out.time = ntime;
+    out.v = v;
+    out.dphase = dphase;
+    out.splat = false;
+    // Integrator::splat (integrator.h:113-135)
+    const float sampleWeight = p.sample_weight;
+    if (!fl.produceDebugImage) {
+        if (sampleWeight == 0.f || v.re == 0.f || v.im == 0.f) return true;
+    }
+    float sample;
+    cf ph;
+    if (kPhase == HSR_PHASE_REFERENCE_FP32) {
+        float dt = ntime + rf.antennaDelay;
+        if (rf.freqSlope == 0.f) {
+            sample = 0.f;
+        } else {
+            float x = dt * rf.freqSlope / rf.adcRate;  // PIndex::setTime (radar.h:232-241)
+            sample = float(p.samples) * (x - floorf(x));
+        }
+        // Integrator::measureRay (integrator.h:107-110)
+        float angle = 2.f * kPi * (rf.startFreq - dt * rf.freqSlope / 2.f) * dt;
+        float s, c;
+        sincosf(angle, &s, &c);
+        ph = cf{c, s};
+    } else {
+        // path length reduced to phase in FP64: cycles = f0 dt - S dt^2 / 2 (mod 1)
+        double dt = nlen / 299792458.0 + double(rf.antennaDelay);
+        if (rf.freqSlope == 0.f) {
+            sample = 0.f;
+        } else {
+            double x = dt * double(rf.freqSlope) / double(rf.adcRate);
+            sample = float(double(p.samples) * (x - floor(x)));
+        }
+        double cyc = (double(rf.startFreq) - dt * double(rf.freqSlope) * 0.5) * dt;
+        float frac = float(cyc - floor(cyc));
+        float s, c;
+        sincospif(2.f * frac, &s, &c);
+        ph = cf{c, s};
+    }
+    out.sample = sample;
+    out.value = cscl(cmul(v, ph), sampleWeight);
+    out.splat = true;
+    return true;
+}
+
+// Frame::splat<16> (libradar/include/radar/radar.h:564-626) restricted to the row the
+// reference writes (chirp and channel indices are exactly 0: delta components).
+// Prepared form: center bin, fractional shift, phase-rotated value and sinc weight.
+struct SplatItem {
+    int center;
+    float shift;  // 0 => delta peak
+    cf value;
+    float w;
+};
+
+__device__ __forceinline__ SplatItem splat_prepare(float sample, cf value) {
+    SplatItem it;
+    it.center = int(roundf(sample));
+    float shift = sample - float(it.center);
+    if (fabsf(shift) < 1e-4f) {
+        it.shift = 0.f;
+        it.value = value;
+        it.w = 1.f;
+        return it;
+    }
+    float shiftPi = float(CUDART_PI * double(shift));
+    float sn, cs;
+    sincosf(shiftPi, &sn, &cs);
+    it.shift = shift;
+    it.value = cmul(value, cf{cs, sn});
+    it.w = sinf(shiftPi) / kPi;
+    return it;
+}
+
+// One thread adds a whole item (33 bins, or 1 for a delta peak).
+__device__ __forceinline__ void splat_serial(float *s_re, float *s_im, int n, const SplatItem &it) {
+    if (it.shift == 0.f) {
+        // the reference indexes `center` unwrapped here; center == N (sample >= N-0.5)
+        // would be out of bounds. Wrapped instead (the spectrum is periodic).
+        int bin = ref_mod(it.center, n);
+        atomicAdd(&s_re[bin], it.value.re);
+        atomicAdd(&s_im[bin], it.value.im);
+        return;
+    }
+    const bool inside = (it.center - 16 >= 0) && (it.center + 16 < n);
+#pragma unroll 11
+    for (int s = -16; s <= 16; ++s) {
+        int bin = inside ? it.center + s : ref_mod(it.center + s, n);
+        float ws = it.w / (it.shift - float(s));
+        atomicAdd(&s_re[bin], ws * it.value.re);
+        atomicAdd(&s_im[bin], ws * it.value.im);
+    }
+}
+
+// A full warp adds the items of the lanes in `mask` cooperatively: lane l owns window
+// offset l - 16 (lane 0 also owns +16), so one item's 33 bins are distinct addresses
+// updated by distinct lanes. Must be called by all 32 lanes.
+__device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, unsigned mask, const SplatItem &mine) {
+    const int lane = threadIdx.x & 31;
+    while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int center = __shfl_sync(0xffffffffu, mine.center, j);
+        const float shift = __shfl_sync(0xffffffffu, mine.shift, j);
+        const float vr = __shfl_sync(0xffffffffu, mine.value.re, j);
+        const float vi = __shfl_sync(0xffffffffu, mine.value.im, j);
+        const float w = __shfl_sync(0xffffffffu, mine.w, j);
+        if (shift == 0.f) {
+            if (lane == 0) {
+                int bin = ref_mod(center, n);
+                atomicAdd(&s_re[bin], vr);
+                atomicAdd(&s_im[bin], vi);
+            }
+            continue;
+        }
+        const bool inside = (center - 16 >= 0) && (center + 16 < n);
+        {
+            const int s = lane - 16;
+            int bin = inside ? center + s : ref_mod(center + s, n);
+            float ws = w / (shift - float(s));
+            atomicAdd(&s_re[bin], ws * vr);
+            atomicAdd(&s_im[bin], ws * vi);
+        }
+        if (lane == 0) {
+            const int s = 16;
+            int bin = inside ? center + s : ref_mod(center + s, n);
+            float ws = w / (shift - float(s));
+            atomicAdd(&s_re[bin], ws * vr);
+            atomicAdd(&s_im[bin], ws * vi);
+        }
+    }
+}
+
+__device__ __forceinline__ int find_pose(const int64_t *__restrict__ tile_start, int pose_count, int64_t item) {
+    int lo = 0, hi = pose_count;  // tile_start[lo] <= item < tile_start[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(&tile_start[mid]) <= item)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Flushes a CTA's shared-memory row into the pose's FP64 accumulators and clears it.
+__device__ __forceinline__ void flush_row(double *acc, float *s_re, float *s_im, int n) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        float re = s_re[k], im = s_im[k];
+        if (re != 0.f) atomicAdd(&acc[2 * k], double(re));
+        if (im != 0.f) atomicAdd(&acc[2 * k + 1], double(im));
+        s_re[k] = 0.f;
+        s_im[k] = 0.f;
+    }
+}
+
+}  // namespace hsr

@@ -1,0 +1,281 @@
+// Wavefront form of the radar path tracer (geometrical-optics mode, the reference's
+// default, path.h:156): the same per-path arithmetic as the one-thread-per-sample
+// kernel, reorganised so that warps stay converged.
+//
+// A persistent CTA of 256 threads keeps a stack of up to 512 live path states in
+// shared memory and alternates two stages:
+//   GENERATE  (stack below 256): 256 new samples, one per thread: Halton point,
+//             antenna ray, closest hit; paths that hit something are pushed.
+//   EXTEND    (otherwise): 256 paths popped, one per thread: specular reflection,
+//             next-event estimate towards RX (shadow ray, PO re-radiation, filtering,
+//             phase), and the next closest hit; survivors are pushed back.
+// Every next-event contribution is splatted by its warp cooperatively: lane l owns
+// window offset l-16 of Frame::splat<16>, so one contribution's 33 bins are 33 distinct
+// shared-memory addresses updated in one pass. The CTA's range row lives in shared
+// memory and is flushed to the pose's FP64 accumulators when the CTA changes pose.
+// Work items are (pose, 4096-sample tile) pairs pulled from a device counter.
+#include "hsr_path.cuh"
+
+namespace hsr {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kStack = 2 * kThreads;
+
+struct WaveShared {
+    float ox[kStack], oy[kStack], oz[kStack];  // hit point (origin of the next segment)
+    float dx[kStack], dy[kStack], dz[kStack];  // incoming direction
+    float h[6][kStack];                        // incoming H field (re, im) x 3
+    float nx[kStack], ny[kStack], nz[kStack];  // faceforwarded normal at the hit
+    float time[kStack], r[kStack], cosT[kStack], freq[kStack];
+    int depth[kStack];
+    double plen[kStack];  // FP64 path length (split-phase mode)
+    int count;
+    int pose, pending_pose, exhausted;
+    long long gen, gen_end, pending_first, pending_last;
+};
+
+__device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H, f3 n, float time, float r,
+                                          float cosT, float freq, int depth, double plen) {
+    const int slot = atomicAdd(&S.count, 1);  // < kStack by construction (see k_wave)
+    S.ox[slot] = o.x;
+    S.oy[slot] = o.y;
+    S.oz[slot] = o.z;
+    S.dx[slot] = d.x;
+    S.dy[slot] = d.y;
+    S.dz[slot] = d.z;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        S.h[2 * i][slot] = H.v[i].re;
+        S.h[2 * i + 1][slot] = H.v[i].im;
+    }
+    S.nx[slot] = n.x;
+    S.ny[slot] = n.y;
+    S.nz[slot] = n.z;
+    S.time[slot] = time;
+    S.r[slot] = r;
+    S.cosT[slot] = cosT;
+    S.freq[slot] = freq;
+    S.depth[slot] = depth;
+    S.plen[slot] = plen;
+}
+
+// Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
+// Returns true (and the new state) when the path continues with a stored hit.
+__device__ __forceinline__ bool walk(const TraceParams &p, f3 o, f3 d, const c3 &H, float &time, float &r,
+                                     double &plen, f3 &hp, f3 &n, float &cosT) {
+    float th;
+    int primh;
+    const int slot = closest_hit<false>(p.nodes, p.tris, o, d, kEpsilon, CUDART_INF_F, th, primh, p.status, nullptr);
+    if (slot < 0) return false;
+    DTri T = load_tri(p.tris, slot);
+    n = hit_normal(T, d);
+    hp = add3(o, scl3(th, d));
+    cosT = fabsf(dot3(n, neg3(d)));
+    if (cosT < 0.001f) return false;
+    r += th;
+    time += th / kSpeedOfLight;
+    plen += double(th);
+    if (c3_is_zero(H)) return false;
+    return true;
+}
+
+template <int kPhase>
+__global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
+    float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
+    float *s_im = s_re + p.samples;
+    const int tid = threadIdx.x;
+    const hsr_rf_config &rf = p.rf;
+    const hsr_tracer_flags &fl = p.flags;
+    const float maxDist = rf.adcRate / rf.freqSlope * kSpeedOfLight;
+    const float bandwidth = rf.freqSlope * rf.rampTime;
+    const long long total = __ldg(&p.tile_start[p.pose_count]);
+
+    for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
+    if (tid == 0) {
+        S.count = 0;
+        S.pose = -1;
+        S.pending_pose = -1;
+        S.exhausted = 0;
+        S.gen = S.gen_end = 0;
+    }
+    __syncthreads();
+
+    Ant tx, rx;
+    int64_t offset = 0;
+    int cur_pose = -1;
+
+    while (true) {
+        // thread 0 pulls work items while the generation range is used up
+        if (tid == 0) {
+            while (S.gen >= S.gen_end && !S.exhausted && S.pending_pose < 0) {
+                const long long item = (long long)atomicAdd((unsigned long long *)p.work_counter, 1ull);
+                if (item >= total) {
+                    S.exhausted = 1;
+                    break;
+                }
+                const int pose = find_pose(p.tile_start, p.pose_count, item);
+                const long long first = (item - __ldg(&p.tile_start[pose])) * p.tile;
+                const long long last = min(first + (long long)p.tile, (long long)__ldg(&p.budget[pose]));
+                if (pose == S.pose) {
+                    S.gen = first;
+                    S.gen_end = last;
+                } else {
+                    S.pending_pose = pose;
+                    S.pending_first = first;
+                    S.pending_last = last;
+                }
+            }
+        }
+        __syncthreads();
+        const int count = S.count;
+        const long long gen = S.gen, gen_end = S.gen_end;
+        const int pending = S.pending_pose;
+        const int exhausted = S.exhausted;
+        __syncthreads();  // every thread has read the shared control words
+
+        if (gen < gen_end && count < kThreads) {
+            // ---------------- GENERATE ----------------
+            if (tid == 0) S.gen = min(gen + (long long)kThreads, gen_end);
+            const long long s = gen + tid;
+            bool has_item = false;
+            SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
+            if (s < gen_end) {
+                const uint64_t hindex = uint64_t(offset + s);
+                const float freq = rf.startFreq + halton(hindex, 0) * bandwidth;
+                const float u0 = halton(hindex, 1);
+                const float u1 = halton(hindex, 2);
+                f3 o = tx.pos, d;
+                c3 H;
+                antenna_sample(tx, u0, u1, d, H);
+                if (!fl.onlyIndirect) {
+                    NeeOut ne;
+                    if (nee_eval<kPhase, false>(p, tx, rx, 0, o, d, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H,
+                                                0.f, 0.0, 0.f, 1.f, freq, ne, nullptr, nullptr) &&
+                        ne.splat) {
+                        item = splat_prepare(ne.sample, ne.value);
+                        has_item = true;
+                    }
+                }
+                if (!(0 >= fl.maxDepth || 0.f >= maxDist) && !c3_is_zero(H)) {
+                    float time = 0.f, r = 0.f, cosT;
+                    double plen = 0.0;
+                    f3 hp, n;
+                    if (walk(p, o, d, H, time, r, plen, hp, n, cosT))
+                        push_path(S, hp, d, H, n, time, r, cosT, freq, 1, plen);
+                }
+            }
+            if (!fl.onlyIndirect) splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
+            __syncthreads();
+            continue;
+        }
+
+        if (count > 0) {
+            // ---------------- EXTEND ----------------
+            const int n = min(count, kThreads);
+            const bool mine = tid < n;
+            f3 o, din, nrm;
+            c3 Hin;
+            float time = 0.f, r = 0.f, cosT = 1.f, freq = 0.f;
+            int depth = 0;
+            double plen = 0.0;
+            if (mine) {
+                const int slot = count - 1 - tid;
+                o = mk3(S.ox[slot], S.oy[slot], S.oz[slot]);
+                din = mk3(S.dx[slot], S.dy[slot], S.dz[slot]);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) Hin.v[i] = cf{S.h[2 * i][slot], S.h[2 * i + 1][slot]};
+                nrm = mk3(S.nx[slot], S.ny[slot], S.nz[slot]);
+                time = S.time[slot];
+                r = S.r[slot];
+                cosT = S.cosT[slot];
+                freq = S.freq[slot];
+                depth = S.depth[slot];
+                plen = S.plen[slot];
+            }
+            __syncthreads();  // all pops read before the stack shrinks
+            if (tid == 0) S.count = count - n;
+            __syncthreads();
+            bool has_item = false;
+            SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
+            if (mine) {
+                f3 d = din;
+                c3 H = Hin;
+                reflect(nrm, d, H);
+                NeeOut ne;
+                if (nee_eval<kPhase, false>(p, tx, rx, depth, o, d, din, nrm, Hin, H, time, plen, r, cosT, freq, ne,
+                                            nullptr, nullptr) &&
+                    ne.splat) {
+                    item = splat_prepare(ne.sample, ne.value);
+                    has_item = true;
+                }
+                if (!(depth >= fl.maxDepth || r >= maxDist) && !c3_is_zero(H)) {
+                    f3 hp, n2;
+                    float cosT2;
+                    if (walk(p, o, d, H, time, r, plen, hp, n2, cosT2))
+                        push_path(S, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen);
+                }
+            }
+            splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
+            __syncthreads();
+            continue;
+        }
+
+        if (pending >= 0) {
+            // stack drained: finish the old pose's row and switch to the new pose
+            if (cur_pose >= 0) flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
+            cur_pose = pending;
+            tx = load_ant(p.tx + cur_pose);
+            rx = load_ant(p.rx + cur_pose);
+            offset = __ldg(&p.offset[cur_pose]);
+            __syncthreads();
+            if (tid == 0) {
+                S.pose = pending;
+                S.gen = S.pending_first;
+                S.gen_end = S.pending_last;
+                S.pending_pose = -1;
+            }
+            __syncthreads();
+            continue;
+        }
+        if (exhausted) break;
+    }
+    if (cur_pose >= 0) {
+        __syncthreads();
+        flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
+    }
+}
+
+}  // namespace
+
+size_t wave_smem_bytes(int samples) { return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float); }
+
+int wave_blocks_per_sm(int samples) {
+    int nb = 0;
+    const size_t smem = wave_smem_bytes(samples);
+    cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_wave<HSR_PHASE_REFERENCE_FP32>, kThreads, smem);
+    return nb > 0 ? nb : 1;
+}
+
+int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err) {
+    const size_t smem = wave_smem_bytes(p.samples);
+    cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaFuncSetAttribute(k_wave<HSR_PHASE_SPLIT_FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (phase_mode == HSR_PHASE_SPLIT_FP64)
+        k_wave<HSR_PHASE_SPLIT_FP64><<<grid, kThreads, smem, st>>>(p);
+    else
+        k_wave<HSR_PHASE_REFERENCE_FP32><<<grid, kThreads, smem, st>>>(p);
+    note_launches(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("wave launch: ") + cudaGetErrorString(e);
+        return 2;
+    }
+    return 0;
+}
+
+}  // namespace hsr

@@ -218,6 +218,11 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
                                       const hsr_antenna *rx, const int64_t *budget,
                                       const int64_t *index_offset, int64_t *out_counts);
 
+/* Which trace kernel the simulate calls use (process-wide): 0 (default) = the wavefront
+ * kernel whenever geometrical optics is on, 1 = always the one-thread-per-sample kernel.
+ * Both compute the same per-path values; tests use this to check each one. */
+hsr_status hsr_set_path_kernel(int32_t kind);
+
 /* Timing of the most recent batch launch on this scene: device milliseconds of the
  * trace kernel alone, measured with CUDA events on the launching stream. */
 hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);
