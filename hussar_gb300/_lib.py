@@ -95,6 +95,8 @@ def lib():
         "hsr_backend_run": [vp, P(RFConfigC), P(FrameConfigC), P(AntennaC), P(AntennaC), P(FlagsC),
                             ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_int32, vp,
                             P(ctypes.c_double), vp],
+        "hsr_path_tracer_run": [vp, P(RFConfigC), P(FrameConfigC), P(AntennaC), P(AntennaC), P(FlagsC),
+                                ctypes.c_int64, ctypes.c_int32, vp, P(ctypes.c_double), vp],
         "hsr_simulate_batch_device": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp,
                                       vp, ctypes.c_int32, ctypes.c_int32, vp, vp],
         "hsr_simulate_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,

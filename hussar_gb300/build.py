@@ -22,6 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "hsr_api.cu": [],
     "hsr_bvh.cu": [],
+    "hsr_guide.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
 }

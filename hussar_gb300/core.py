@@ -158,16 +158,15 @@ class PathTracer:
 
     def run(self, backend, scene, samples, interruptFlag=None):
         """PathTracer::run (path.h:171-224). The plain schedule traces Halton indices
-        [0, samples) in one backend.run call."""
+        [0, samples) in one backend.run call; the guided schedule (doGuiding) runs the
+        doubling iterations with device path guiding inside the backend."""
         self.clearFrame()
         self.sampleIndexOffset = 0
         self.currentSampleWeight = 1.0
         if not self.doGuiding:
             backend.run(scene, samples, interruptFlag)
             return
-        raise _lib.HsrError(_lib.HSR_ERR_NOT_SUPPORTED,
-                            "doGuiding=True needs the guided schedule, which this build does not provide; "
-                            "set doGuiding=False for the plain method")
+        backend.run_path_tracer(scene, samples, interruptFlag)
 
     def fetchFrame(self):
         """path.h:453-455: frame / totalWeight."""
@@ -220,6 +219,24 @@ class _GB300:
                                          ctypes.byref(it.flags_c()), int(budget), int(it.sampleIndexOffset),
                                          float(it.currentSampleWeight), int(it.phaseMode), _lib.ptr(buf),
                                          ctypes.byref(tw), _lib.ptr(flag)))
+            it.frame.data = buf.view(np.complex64).reshape(it.frame.data.shape)
+            it.totalWeight = tw.value
+
+        def run_path_tracer(self, scene, samples, interruptFlag=None):
+            """The whole PathTracer::run schedule on the device (hsr_path_tracer_run):
+            sets the integrator's frame and total weight."""
+            it = self._integrator
+            fc = it.frame.config()
+            buf = np.zeros(2 * fc.sampleCount(), np.float32)
+            tw = ctypes.c_double(0.0)
+            flag = None
+            if interruptFlag is not None:
+                flag = np.array([1 if (interruptFlag() if callable(interruptFlag) else interruptFlag) else 0],
+                                np.int32)
+            _lib.check(_lib.lib().hsr_path_tracer_run(
+                self._scene, ctypes.byref(scene.rfConfig.to_c()), ctypes.byref(fc.to_c()),
+                ctypes.byref(scene.tx.to_c()), ctypes.byref(scene.rx.to_c()), ctypes.byref(it.flags_c()),
+                int(samples), int(it.phaseMode), _lib.ptr(buf), ctypes.byref(tw), _lib.ptr(flag)))
             it.frame.data = buf.view(np.complex64).reshape(it.frame.data.shape)
             it.totalWeight = tw.value
 

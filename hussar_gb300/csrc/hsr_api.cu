@@ -1,6 +1,7 @@
-// The C ABI (include/hsr_gb300.h): scene residency, ray queries and simulate calls.
-// Every entry point returns an hsr_status; the message of the last failure on the
-// calling thread is available from hsr_last_error(). No exception crosses the ABI.
+// The C ABI (include/hsr_gb300.h): scene residency, ray queries, backend runs, batched
+// and guided simulations. Every entry point returns an hsr_status; the message of the
+// last failure on the calling thread is available from hsr_last_error(). No exception
+// crosses the ABI.
 #include <atomic>
 #include <cstring>
 #include <mutex>
@@ -8,6 +9,7 @@
 #include <vector>
 
 #include "hsr_common.cuh"
+#include "hsr_guide.cuh"
 #include "hsr_internal.h"
 
 namespace hsr {
@@ -46,18 +48,27 @@ static hsr_status validate_common(const hsr_rf_config *rf, int32_t samples, cons
     if (samples <= 0 || samples > 4096)
         return fail(HSR_ERR_INVALID_ARGUMENT, "samplesPerChirp must be in [1, 4096]");
     if (fl->maxDepth < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "maxDepth must be >= 0");
-    if (fl->doGuiding)
-        return fail(HSR_ERR_NOT_SUPPORTED, "doGuiding=1 runs through the guided schedule, not a plain backend run");
     return HSR_OK;
 }
 
-// Scratch layout for a batch of P poses with N bins, carved from one allocation.
+static hsr_status validate_phase(int32_t phase_mode, int32_t splat_mode) {
+    if (phase_mode != HSR_PHASE_REFERENCE_FP32 && phase_mode != HSR_PHASE_SPLIT_FP64)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
+    if (splat_mode != HSR_SPLAT_DIRICHLET16)
+        return fail(HSR_ERR_NOT_SUPPORTED, "splat mode not available in this build");
+    return HSR_OK;
+}
+
+// Per-batch scratch for P poses with N bins, carved from one allocation owned by the scene.
 struct Scratch {
     hsr_antenna *tx, *rx;
     int64_t *budget, *offset, *tile_start;
+    float *weights;
+    int *train, *active, *clear;
+    double *tw;
     double *acc;
     float *rows;
-    unsigned *counters;  // [0] status, [2..3] 64-bit work counter
+    unsigned *counters;  // [0] status word, [2..3] 64-bit work counter
     size_t bytes;
 };
 
@@ -78,6 +89,11 @@ static Scratch carve(void *base, int32_t P, int32_t N) {
     s.budget = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * P));
     s.offset = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * P));
     s.tile_start = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * (P + 1)));
+    s.weights = reinterpret_cast<float *>(take(sizeof(float) * P));
+    s.train = reinterpret_cast<int *>(take(sizeof(int) * P));
+    s.active = reinterpret_cast<int *>(take(sizeof(int) * P));
+    s.clear = reinterpret_cast<int *>(take(sizeof(int) * P));
+    s.tw = reinterpret_cast<double *>(take(sizeof(double) * P));
     s.acc = reinterpret_cast<double *>(take(sizeof(double) * 2 * size_t(P) * N));
     s.rows = reinterpret_cast<float *>(take(sizeof(float) * 2 * size_t(P) * N));
     s.bytes = off;
@@ -87,7 +103,10 @@ static Scratch carve(void *base, int32_t P, int32_t N) {
 static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &out) {
     Scratch need = carve(nullptr, P, N);
     if (need.bytes > sc.scratch_bytes) {
-        if (sc.scratch) cudaFree(sc.scratch);
+        if (sc.scratch) {
+            cudaDeviceSynchronize();
+            cudaFree(sc.scratch);
+        }
         sc.scratch = nullptr;
         sc.scratch_bytes = 0;
         cudaError_t e = cudaMalloc(&sc.scratch, need.bytes);
@@ -101,16 +120,62 @@ static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &ou
     return HSR_OK;
 }
 
-static constexpr int32_t kTile = 4096;  // samples per work item (16 per thread at 256 threads)
+// Guiding trees for P poses.
+struct GuideMem {
+    int *samp_child;
+    float *samp_p;
+    int *train_child;
+    float *train_acc;
+    int *train_count;
+    float *scratch_e;
+    int *scratch_i;
+};
 
-// Enqueues one batch: poses/budgets already in scratch (device), accumulators zeroed here.
-static hsr_status enqueue_batch(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
-                                const hsr_tracer_flags *fl, int32_t P, float sample_weight, int32_t phase_mode,
-                                int32_t splat_mode, int normalise, float *d_out_rows, cudaStream_t st,
-                                void *records, int max_rec, unsigned long long *counters = nullptr) {
+static GuideMem carve_guide(void *base, int P) {
+    GuideMem g;
+    char *p = static_cast<char *>(base);
+    size_t off = 0;
+    const size_t M = size_t(P) * kGuideMaxNodes;
+    auto take = [&](size_t bytes) {
+        char *r = p + off;
+        off += align256(bytes);
+        return r;
+    };
+    g.samp_child = reinterpret_cast<int *>(take(4 * M));
+    g.samp_p = reinterpret_cast<float *>(take(4 * M));
+    g.train_child = reinterpret_cast<int *>(take(4 * M));
+    g.train_acc = reinterpret_cast<float *>(take(12 * M));
+    g.train_count = reinterpret_cast<int *>(take(4 * size_t(P)));
+    g.scratch_e = reinterpret_cast<float *>(take(4 * M));
+    g.scratch_i = reinterpret_cast<int *>(take(8 * M));
+    return g;
+}
+
+static hsr_status ensure_guide(SceneDev &sc, int P, GuideMem &out) {
+    if (P > sc.guide_cap) {
+        if (sc.guide) {
+            cudaDeviceSynchronize();
+            cudaFree(sc.guide);
+        }
+        sc.guide = nullptr;
+        sc.guide_cap = 0;
+        const size_t bytes = guide_bytes_per_pose() * size_t(P) + 8 * 256;
+        cudaError_t e = cudaMalloc(&sc.guide, bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "guiding allocation");
+        sc.guide_cap = P;
+    }
+    out = carve_guide(sc.guide, P);
+    return HSR_OK;
+}
+
+static constexpr int32_t kTile = 4096;  // samples per work item
+
+// One trace launch over the poses' current budgets/offsets/weights in scratch.
+static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
+                               const hsr_tracer_flags *fl, int32_t P, float sample_weight, bool per_pose_weights,
+                               int32_t phase_mode, int32_t splat_mode, cudaStream_t st, const GuideMem *g,
+                               void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr) {
     cudaError_t e;
-    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess)
-        return cuda_fail(e, "memset accumulators");
     if ((e = cudaMemsetAsync(s.counters + 2, 0, 8, st)) != cudaSuccess) return cuda_fail(e, "memset counter");
     if (launch_tile_prefix(s.budget, P, kTile, s.tile_start, st) != 0)
         return cuda_fail(cudaGetLastError(), "tile prefix launch");
@@ -134,6 +199,17 @@ static hsr_status enqueue_batch(SceneDev &sc, const Scratch &s, const hsr_rf_con
     p.records = records;
     p.max_rec = max_rec;
     p.counters = counters;
+    p.weights = per_pose_weights ? s.weights : nullptr;
+    p.do_guide = (fl->doGuiding && g) ? 1 : 0;
+    if (p.do_guide) {
+        p.train = s.train;
+        p.g_samp_child = g->samp_child;
+        p.g_samp_p = g->samp_p;
+        p.g_train_child = g->train_child;
+        p.g_train_acc = g->train_acc;
+    } else {
+        p.flags.doGuiding = 0;
+    }
     const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
     int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N) : trace_blocks_per_sm(N, splat_mode, 0));
     cudaEventRecord(sc.ev0, st);
@@ -145,12 +221,142 @@ static hsr_status enqueue_batch(SceneDev &sc, const Scratch &s, const hsr_rf_con
     }
     cudaEventRecord(sc.ev1, st);
     sc.timing_valid = true;
-    if (launch_finalize(s.acc, P, N, s.budget, sample_weight, normalise, d_out_rows, st) != 0)
+    return HSR_OK;
+}
+
+// Plain run of every pose over its whole budget (doGuiding = 0), then fetchFrame rows.
+static hsr_status run_plain(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
+                            const hsr_tracer_flags *fl, int32_t P, float sample_weight, int32_t phase_mode,
+                            int32_t splat_mode, int normalise, float *d_out_rows, cudaStream_t st,
+                            void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess)
+        return cuda_fail(e, "memset accumulators");
+    hsr_tracer_flags plain = *fl;
+    plain.doGuiding = 0;
+    hsr_status r = enqueue_pass(sc, s, rf, N, &plain, P, sample_weight, false, phase_mode, splat_mode, st, nullptr,
+                                records, max_rec, counters);
+    if (r != HSR_OK) return r;
+    if (launch_finalize(s.acc, P, N, s.budget, sample_weight, nullptr, normalise, d_out_rows, st) != 0)
         return cuda_fail(cudaGetLastError(), "finalize launch");
     return HSR_OK;
 }
 
-static hsr_status read_status(SceneDev &sc, const Scratch &s, cudaStream_t st) {
+// PathTracer::run's schedule (path.h:171-224) for one pose: per iteration the
+// backend-run budget, Halton offset, sample weight, whether the frame is cleared
+// before it, and whether it trains the guiding tree (not in the final iteration).
+struct Iter {
+    int64_t budget, offset;
+    float weight;
+    bool clear, train;
+};
+
+static std::vector<Iter> schedule(int64_t samples, bool clearBeforeIteration) {
+    std::vector<Iter> it;
+    int64_t milestone = 16384, remaining = samples, offset = 0;
+    float weight = 1.f;
+    bool final_iter = false, clear = true;
+    while (true) {
+        milestone = std::min(milestone, remaining);
+        it.push_back(Iter{milestone, offset, weight, clear, !final_iter});
+        offset += milestone;
+        remaining -= milestone;
+        if (remaining == 0) break;
+        milestone *= 2;
+        if (remaining < milestone * 2) {
+            final_iter = true;
+            milestone = remaining;
+        }
+        if (clearBeforeIteration) {
+            clear = true;
+            offset = 0;
+        } else {
+            clear = false;
+            weight = 10.f * weight;
+        }
+    }
+    return it;
+}
+
+// The guided schedule for every pose (host budgets); writes fetchFrame rows (normalise)
+// or raw sums, and the total weights (h_total_weight, optional).
+static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
+                             const hsr_tracer_flags *fl, int32_t P, const std::vector<int64_t> &budgets,
+                             const std::vector<int64_t> &offsets, int32_t phase_mode, int32_t splat_mode,
+                             int normalise, float *d_out_rows, cudaStream_t st, double *h_total_weight,
+                             const volatile int32_t *interrupt_flag) {
+    GuideMem g;
+    hsr_status r = ensure_guide(sc, P, g);
+    if (r != HSR_OK) return r;
+    std::vector<std::vector<Iter>> sched(P);
+    size_t K = 0;
+    for (int p = 0; p < P; ++p) {
+        sched[p] = schedule(budgets[p], fl->clearBeforeIteration != 0);
+        K = std::max(K, sched[p].size());
+    }
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess)
+        return cuda_fail(e, "memset accumulators");
+    if (launch_guide_reset(P, g.samp_child, g.samp_p, g.train_child, g.train_acc, g.train_count, st) != 0)
+        return cuda_fail(cudaGetLastError(), "guide reset");
+    std::vector<int64_t> b(P), o(P);
+    std::vector<float> w(P);
+    std::vector<int> train(P), active(P), clear(P);
+    std::vector<double> tw(P, 0.0);
+    for (size_t k = 0; k < K; ++k) {
+        if (interrupt_flag && *interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted between iterations");
+        bool any_clear = false, any_active = false;
+        for (int p = 0; p < P; ++p) {
+            if (k < sched[p].size()) {
+                const Iter &it = sched[p][k];
+                b[p] = it.budget;
+                // the caller's index offset shifts every iteration's Halton range
+                o[p] = it.offset + offsets[p];
+                w[p] = it.weight;
+                train[p] = it.train ? 1 : 0;
+                clear[p] = (k > 0 && it.clear) ? 1 : 0;
+                if (it.clear) tw[p] = 0.0;
+                tw[p] += double(it.budget) * double(it.weight);  // path.h:445, 466-475
+                active[p] = k + 1 < sched[p].size() ? 1 : 0;
+            } else {
+                b[p] = 0;
+                o[p] = 0;
+                w[p] = 0.f;
+                train[p] = 0;
+                clear[p] = 0;
+                active[p] = 0;
+            }
+            any_clear |= clear[p] != 0;
+            any_active |= active[p] != 0;
+        }
+        if ((e = cudaMemcpyAsync(s.budget, b.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(s.offset, o.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(s.weights, w.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(s.train, train.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(s.clear, clear.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(s.active, active.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_fail(e, "schedule upload");
+        if (any_clear && launch_clear_rows(s.acc, P, N, s.clear, st) != 0)
+            return cuda_fail(cudaGetLastError(), "clear rows");
+        r = enqueue_pass(sc, s, rf, N, fl, P, 1.f, true, phase_mode, splat_mode, st, &g);
+        if (r != HSR_OK) return r;
+        if (any_active && launch_guide_step(P, s.active, g.samp_child, g.samp_p, g.train_child, g.train_acc,
+                                            g.train_count, g.scratch_e, g.scratch_i, st) != 0)
+            return cuda_fail(cudaGetLastError(), "guide step");
+        // the host schedule arrays are rewritten next iteration: let this one's copies land
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "guided iteration");
+    }
+    if ((e = cudaMemcpyAsync(s.tw, tw.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(e, "weight upload");
+    if (launch_finalize(s.acc, P, N, s.budget, 1.f, s.tw, normalise, d_out_rows, st) != 0)
+        return cuda_fail(cudaGetLastError(), "finalize launch");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "guided finalize");
+    if (h_total_weight)
+        for (int p = 0; p < P; ++p) h_total_weight[p] = tw[p];
+    return HSR_OK;
+}
+
+static hsr_status read_status(const Scratch &s, cudaStream_t st) {
     unsigned bits = 0;
     cudaError_t e = cudaMemcpyAsync(&bits, s.counters, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -164,7 +370,17 @@ static hsr_status read_status(SceneDev &sc, const Scratch &s, cudaStream_t st) {
         if (bits & kStatusBadWorkItem) m += " bad-work-item";
         return fail(HSR_ERR_DEVICE, m);
     }
-    (void)sc;
+    return HSR_OK;
+}
+
+static hsr_status upload_poses(const Scratch &s, int32_t P, const hsr_antenna *tx, const hsr_antenna *rx,
+                               const int64_t *budget, const int64_t *offset, cudaMemcpyKind kind, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(s.tx, tx, sizeof(hsr_antenna) * P, kind, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s.rx, rx, sizeof(hsr_antenna) * P, kind, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s.budget, budget, sizeof(int64_t) * P, kind, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s.offset, offset, sizeof(int64_t) * P, kind, st)) != cudaSuccess)
+        return cuda_fail(e, "pose upload");
     return HSR_OK;
 }
 
@@ -271,6 +487,7 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
     cudaFree(s->dev.tris);
     cudaFree(s->dev.nodes);
     cudaFree(s->dev.scratch);
+    cudaFree(s->dev.guide);
     if (s->dev.ev0) cudaEventDestroy(s->dev.ev0);
     if (s->dev.ev1) cudaEventDestroy(s->dev.ev1);
     delete s;
@@ -280,7 +497,8 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
 hsr_status hsr_scene_footprint(const hsr_scene *s, int64_t *out_bytes) {
     if (!s || !out_bytes) return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
     *out_bytes = int64_t(sizeof(DTri)) * std::max<int64_t>(s->dev.tri_count, 1) +
-                 int64_t(sizeof(DNode)) * s->dev.node_count + int64_t(s->dev.scratch_bytes);
+                 int64_t(sizeof(DNode)) * s->dev.node_count + int64_t(s->dev.scratch_bytes) +
+                 int64_t(guide_bytes_per_pose()) * s->dev.guide_cap;
     return HSR_OK;
 }
 
@@ -343,8 +561,6 @@ hsr_status hsr_visible(const hsr_scene *s, int64_t count, const float *o, const 
     return ray_queries(s, count, o, d, tfar, nullptr, nullptr, nullptr, nullptr, vis);
 }
 
-// Records of individual next-event estimates (tests): records is a HOST array of
-// budget * max_rec PathRecord-sized entries (9 x 4 bytes each).
 hsr_status hsr_debug_records(hsr_scene *s, const hsr_rf_config *rf, int32_t samples, const hsr_tracer_flags *fl,
                              const hsr_antenna *tx, const hsr_antenna *rx, int64_t budget, int64_t index_offset,
                              int32_t max_rec, void *records) {
@@ -359,23 +575,22 @@ hsr_status hsr_debug_records(hsr_scene *s, const hsr_rf_config *rf, int32_t samp
     void *d_rec = nullptr;
     std::string err;
     if (!dev_alloc(&d_rec, rec_bytes, err)) return fail(HSR_ERR_OUT_OF_MEMORY, err);
-    // unused slots: depth = -1
-    std::vector<int32_t> init(rec_bytes / 4, 0);
+    std::vector<int32_t> init(rec_bytes / 4, 0);  // unused slots: depth = -1
     for (size_t i = 0; i < init.size(); i += 9) init[i] = -1;
     cudaMemcpy(d_rec, init.data(), rec_bytes, cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.tx, tx, sizeof(hsr_antenna), cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.rx, rx, sizeof(hsr_antenna), cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.budget, &budget, sizeof(int64_t), cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.offset, &index_offset, sizeof(int64_t), cudaMemcpyHostToDevice);
-    st = enqueue_batch(s->dev, sc, rf, samples, fl, 1, 1.f, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, 0,
-                       sc.rows, 0, d_rec, max_rec);
+    if ((st = upload_poses(sc, 1, tx, rx, &budget, &index_offset, cudaMemcpyHostToDevice, 0)) != HSR_OK) {
+        cudaFree(d_rec);
+        return st;
+    }
+    st = run_plain(s->dev, sc, rf, samples, fl, 1, 1.f, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, 0, sc.rows,
+                   0, d_rec, max_rec);
     if (st == HSR_OK) {
         cudaError_t e = cudaDeviceSynchronize();
         if (e != cudaSuccess) st = cuda_fail(e, "record run");
     }
     if (st == HSR_OK) cudaMemcpy(records, d_rec, rec_bytes, cudaMemcpyDeviceToHost);
     cudaFree(d_rec);
-    if (st == HSR_OK) st = read_status(s->dev, sc, 0);
+    if (st == HSR_OK) st = read_status(sc, 0);
     return st;
 }
 
@@ -390,9 +605,11 @@ hsr_status hsr_backend_run(const hsr_scene *cs, const hsr_rf_config *rf, const h
         return fail(HSR_ERR_INVALID_ARGUMENT, "frame dimensions must be positive");
     hsr_status st = validate_common(rf, frame->samplesPerChirp, fl);
     if (st != HSR_OK) return st;
+    if (fl->doGuiding)
+        return fail(HSR_ERR_NOT_SUPPORTED,
+                    "a guided backend run needs the sampling tree of the schedule: use hsr_path_tracer_run");
     if (budget < 0 || index_offset < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
-    if (phase_mode != HSR_PHASE_REFERENCE_FP32 && phase_mode != HSR_PHASE_SPLIT_FP64)
-        return fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
+    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
     if (interrupt_flag && *interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted before start");
     if (budget == 0) return HSR_OK;
     const int32_t N = frame->samplesPerChirp;
@@ -400,22 +617,16 @@ hsr_status hsr_backend_run(const hsr_scene *cs, const hsr_rf_config *rf, const h
     Scratch sc;
     if ((st = ensure_scratch(s->dev, 1, N, sc)) != HSR_OK) return st;
     cudaStream_t strm = 0;
-    cudaError_t e;
-    if ((e = cudaMemcpyAsync(sc.tx, tx, sizeof(hsr_antenna), cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.rx, rx, sizeof(hsr_antenna), cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.budget, &budget, sizeof(int64_t), cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.offset, &index_offset, sizeof(int64_t), cudaMemcpyHostToDevice, strm)) !=
-            cudaSuccess)
-        return cuda_fail(e, "pose upload");
-    st = enqueue_batch(s->dev, sc, rf, N, fl, 1, sample_weight, phase_mode, HSR_SPLAT_DIRICHLET16, 0, sc.rows, strm,
-                       nullptr, 0);
+    if ((st = upload_poses(sc, 1, tx, rx, &budget, &index_offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
+    st = run_plain(s->dev, sc, rf, N, fl, 1, sample_weight, phase_mode, HSR_SPLAT_DIRICHLET16, 0, sc.rows, strm);
     if (st != HSR_OK) return st;
     std::vector<float> row(2 * size_t(N));
+    cudaError_t e;
     if ((e = cudaMemcpyAsync(row.data(), sc.rows, sizeof(float) * 2 * N, cudaMemcpyDeviceToHost, strm)) !=
         cudaSuccess)
         return cuda_fail(e, "row download");
     if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "backend run");
-    if ((st = read_status(s->dev, sc, strm)) != HSR_OK) return st;
+    if ((st = read_status(sc, strm)) != HSR_OK) return st;
     // the reference writes only chirp 0 / channel 0 (path.h:130, 291-292)
     const int C = frame->channelCount;
     for (int32_t k = 0; k < N; ++k) {
@@ -429,6 +640,54 @@ hsr_status hsr_backend_run(const hsr_scene *cs, const hsr_rf_config *rf, const h
     return HSR_OK;
 }
 
+hsr_status hsr_path_tracer_run(hsr_scene *s, const hsr_rf_config *rf, const hsr_frame_config *frame,
+                               const hsr_antenna *tx, const hsr_antenna *rx, const hsr_tracer_flags *fl,
+                               int64_t samples, int32_t phase_mode, float *frame_out, double *total_weight_out,
+                               const volatile int32_t *interrupt_flag) {
+    if (!s || !frame || !tx || !rx || !frame_out || !total_weight_out)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    if (frame->chirpCount <= 0 || frame->samplesPerChirp <= 0 || frame->channelCount <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "frame dimensions must be positive");
+    hsr_status st = validate_common(rf, frame->samplesPerChirp, fl);
+    if (st != HSR_OK) return st;
+    if (samples < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative sample count");
+    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
+    const size_t n = size_t(frame->chirpCount) * frame->samplesPerChirp * frame->channelCount;
+    std::memset(frame_out, 0, sizeof(float) * 2 * n);  // clearFrame (path.h:174)
+    *total_weight_out = 0.0;
+    if (interrupt_flag && *interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted before start");
+    if (!fl->doGuiding) {
+        return hsr_backend_run(s, rf, frame, tx, rx, fl, samples, 0, 1.f, phase_mode, frame_out, total_weight_out,
+                               interrupt_flag);
+    }
+    const int32_t N = frame->samplesPerChirp;
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scratch sc;
+    if ((st = ensure_scratch(s->dev, 1, N, sc)) != HSR_OK) return st;
+    cudaStream_t strm = 0;
+    int64_t zero = 0;
+    if ((st = upload_poses(sc, 1, tx, rx, &samples, &zero, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
+    double tw = 0.0;
+    st = run_guided(s->dev, sc, rf, N, fl, 1, std::vector<int64_t>{samples}, std::vector<int64_t>{0}, phase_mode,
+                    HSR_SPLAT_DIRICHLET16, 0, sc.rows, strm, &tw, interrupt_flag);
+    if (st != HSR_OK) return st;
+    std::vector<float> row(2 * size_t(N));
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(row.data(), sc.rows, sizeof(float) * 2 * N, cudaMemcpyDeviceToHost, strm)) !=
+        cudaSuccess)
+        return cuda_fail(e, "row download");
+    if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "guided run");
+    if ((st = read_status(sc, strm)) != HSR_OK) return st;
+    const int C = frame->channelCount;
+    for (int32_t k = 0; k < N; ++k) {
+        size_t id = size_t(k) * C;
+        frame_out[2 * id] = row[2 * k];
+        frame_out[2 * id + 1] = row[2 * k + 1];
+    }
+    *total_weight_out = tw;
+    return HSR_OK;
+}
+
 hsr_status hsr_simulate_batch_device(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,
                                      int32_t P, const hsr_antenna *d_tx, const hsr_antenna *d_rx,
                                      const int64_t *d_budget, const int64_t *d_offset, int32_t phase_mode,
@@ -437,22 +696,23 @@ hsr_status hsr_simulate_batch_device(hsr_scene *s, const hsr_rf_config *rf, int3
         return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no poses");
     hsr_status st = validate_common(rf, N, fl);
     if (st != HSR_OK) return st;
-    if (phase_mode != HSR_PHASE_REFERENCE_FP32 && phase_mode != HSR_PHASE_SPLIT_FP64)
-        return fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
-    if (splat_mode != HSR_SPLAT_DIRICHLET16)
-        return fail(HSR_ERR_NOT_SUPPORTED, "splat mode not available in this build");
+    if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
     if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    if ((st = upload_poses(sc, P, d_tx, d_rx, d_budget, d_offset, cudaMemcpyDeviceToDevice, strm)) != HSR_OK)
+        return st;
+    if (!fl->doGuiding)
+        return run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, d_out_rows, strm);
+    // the guided schedule is planned on the host: it reads the budgets back (synchronising)
+    std::vector<int64_t> b(P), o(P);
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(sc.tx, d_tx, sizeof(hsr_antenna) * P, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.rx, d_rx, sizeof(hsr_antenna) * P, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.budget, d_budget, sizeof(int64_t) * P, cudaMemcpyDeviceToDevice, strm)) !=
-            cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.offset, d_offset, sizeof(int64_t) * P, cudaMemcpyDeviceToDevice, strm)) != cudaSuccess)
-        return cuda_fail(e, "pose staging");
-    return enqueue_batch(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, d_out_rows, strm, nullptr, 0);
+    if ((e = cudaMemcpyAsync(b.data(), d_budget, 8 * P, cudaMemcpyDeviceToHost, strm)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(o.data(), d_offset, 8 * P, cudaMemcpyDeviceToHost, strm)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(strm)) != cudaSuccess)
+        return cuda_fail(e, "budget read-back");
+    return run_guided(s->dev, sc, rf, N, fl, P, b, o, phase_mode, splat_mode, 1, d_out_rows, strm, nullptr, nullptr);
 }
 
 hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl, int32_t P,
@@ -465,27 +725,26 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     if (st != HSR_OK) return st;
     for (int32_t i = 0; i < P; ++i)
         if (budget[i] < 0 || offset[i] < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
-    if (phase_mode != HSR_PHASE_REFERENCE_FP32 && phase_mode != HSR_PHASE_SPLIT_FP64)
-        return fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
-    if (splat_mode != HSR_SPLAT_DIRICHLET16)
-        return fail(HSR_ERR_NOT_SUPPORTED, "splat mode not available in this build");
+    if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
     if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
-    cudaError_t e;
-    if ((e = cudaMemcpyAsync(sc.tx, tx, sizeof(hsr_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.rx, rx, sizeof(hsr_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.budget, budget, sizeof(int64_t) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(sc.offset, offset, sizeof(int64_t) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess)
-        return cuda_fail(e, "pose upload");
-    st = enqueue_batch(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, sc.rows, strm, nullptr, 0);
+    if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
+    if (!fl->doGuiding) {
+        st = run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, sc.rows, strm);
+    } else {
+        st = run_guided(s->dev, sc, rf, N, fl, P, std::vector<int64_t>(budget, budget + P),
+                        std::vector<int64_t>(offset, offset + P), phase_mode, splat_mode, 1, sc.rows, strm, nullptr,
+                        nullptr);
+    }
     if (st != HSR_OK) return st;
+    cudaError_t e;
     if ((e = cudaMemcpyAsync(out_rows, sc.rows, sizeof(float) * 2 * size_t(P) * N, cudaMemcpyDeviceToHost, strm)) !=
         cudaSuccess)
         return cuda_fail(e, "row download");
     if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "batch run");
-    return read_status(s->dev, sc, strm);
+    return read_status(sc, strm);
 }
 
 hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,
@@ -502,12 +761,12 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int
     std::string err;
     if (!dev_alloc(&d_cnt, 4 * sizeof(unsigned long long), err)) return fail(HSR_ERR_OUT_OF_MEMORY, err);
     cudaMemset(d_cnt, 0, 4 * sizeof(unsigned long long));
-    cudaMemcpy(sc.tx, tx, sizeof(hsr_antenna) * P, cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.rx, rx, sizeof(hsr_antenna) * P, cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.budget, budget, sizeof(int64_t) * P, cudaMemcpyHostToDevice);
-    cudaMemcpy(sc.offset, offset, sizeof(int64_t) * P, cudaMemcpyHostToDevice);
-    st = enqueue_batch(s->dev, sc, rf, N, fl, P, 1.f, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, 1, sc.rows, 0,
-                       nullptr, 0, d_cnt);
+    if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, 0)) != HSR_OK) {
+        cudaFree(d_cnt);
+        return st;
+    }
+    st = run_plain(s->dev, sc, rf, N, fl, P, 1.f, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, 1, sc.rows, 0,
+                   nullptr, 0, d_cnt);
     unsigned long long h[4] = {0, 0, 0, 0};
     if (st == HSR_OK) {
         cudaError_t e = cudaDeviceSynchronize();
@@ -516,7 +775,7 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int
     if (st == HSR_OK) cudaMemcpy(h, d_cnt, sizeof(h), cudaMemcpyDeviceToHost);
     cudaFree(d_cnt);
     for (int i = 0; i < 3; ++i) out_counts[i] = int64_t(h[i]);
-    if (st == HSR_OK) st = read_status(s->dev, sc, 0);
+    if (st == HSR_OK) st = read_status(sc, 0);
     return st;
 }
 

@@ -28,6 +28,8 @@ struct SceneDev {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     unsigned *status = nullptr;  // device status word + work counter
+    void *guide = nullptr;       // guiding trees + step scratch, sized for guide_cap poses
+    int guide_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_kernel_ms = 0.f;
     bool timing_valid = false;
@@ -71,16 +73,33 @@ struct TraceParams {
     void *records;          // optional PathRecord[budget][max_rec] (tests)
     int32_t max_rec;
     unsigned long long *counters;  // optional [nodes, tris, rays] (counting instantiation)
+    // per-pose sample weight (PathTracer::currentSampleWeight); nullptr: sample_weight for all
+    const float *weights;
+    // path guiding (doGuiding): trees [pose][kGuideMaxNodes]; train[pose] = 1 splats into
+    // the training tree (every iteration but the final one, path.h:448)
+    int32_t do_guide;
+    const int *train;
+    const int *g_samp_child;
+    const float *g_samp_p;
+    const int *g_train_child;
+    float *g_train_acc;
     // fine-histogram mode
     int32_t fine_bins;      // K = N * oversample
     float *fine;            // [pose_count][3 moments][K] complex, device
 };
 
+size_t guide_bytes_per_pose();
+int launch_guide_reset(int P, int *samp_child, float *samp_p, int *train_child, float *train_acc, int *train_count,
+                       cudaStream_t st);
+int launch_guide_step(int P, const int *active, int *samp_child, float *samp_p, int *train_child, float *train_acc,
+                      int *train_count, float *scratch_e, int *scratch_i, cudaStream_t st);
+
 // Launches (all asynchronous on `st`).
 int launch_trace(const TraceParams &p, int phase_mode, int splat_mode, int grid, cudaStream_t st, std::string &err);
 int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, int64_t *tile_start, cudaStream_t st);
 int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, const int64_t *budget, float sample_weight,
-                    int normalise, float *out_rows, cudaStream_t st);
+                    const double *total_weight, int normalise, float *out_rows, cudaStream_t st);
+int launch_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *clear, cudaStream_t st);
 int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st);

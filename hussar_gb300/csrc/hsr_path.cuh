@@ -8,6 +8,7 @@
 
 #include "hsr_common.cuh"
 #include "hsr_internal.h"
+#include "hsr_guide.cuh"
 #include "hsr_traverse.cuh"
 
 namespace hsr {
@@ -154,6 +155,7 @@ struct NeeOut {
     float dphase;
     float sample;  // fractional range bin
     cf value;      // weight * v * measureRay(dt)
+    cf gw_add;     // what this estimate adds to guidingWeight (path.h:363-394)
     bool splat;    // passed the splat early-out
 };
 
@@ -162,8 +164,8 @@ struct NeeOut {
 template <int kPhase, bool kCount>
 __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, const Ant &rx, int depth, f3 o, f3 d,
                                          f3 tmpd, f3 hit_n, const c3 &inc_H, const c3 &H, float time, double plen,
-                                         float r, float cosTheta, float freq, NeeOut &out, TraversalCounters *cnt,
-                                         unsigned *rays) {
+                                         float r, float cosTheta, float freq, float sampleWeight, NeeOut &out,
+                                         TraversalCounters *cnt, unsigned *rays) {
     const hsr_rf_config &rf = p.rf;
     const hsr_tracer_flags &fl = p.flags;
     // NFAntenna::nee (emitter.h:195-203)
@@ -197,6 +199,7 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
     cf v = dot_cc(nH, Hrx);
     const float wavelength = kSpeedOfLight / freq;
     float dphase = 0.f;
+    cf gw = cf{0.f, 0.f};
     if (depth > 0) {
         if (fl.correctPhase) {
             f3 rxPos = add3(no, scl3(nt, nd));
@@ -225,6 +228,10 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
             if (fl.filteringSphere) {
                 if (dphase > fl.filteringRadius) {
                     if (fl.correctPhase) {
+                        if (fl.filterGuiding) {
+                            const float q = dphase / fl.filteringRadius;
+                            gw = cadd(gw, cdiv(v, float(double(q) * double(q) + 1.0)));
+                        }
                         v = cf{0.f, 0.f};
                     } else {
                         float q = dphase / fl.filteringRadius - 1.f;
@@ -233,18 +240,27 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
                     }
                 }
             } else {
-                if (dphase > fl.filteringMax) v = cf{0.f, 0.f};
+                if (dphase > fl.filteringMax) {
+                    if (fl.filterGuiding) {
+                        const float q = dphase / fl.filteringMax;
+                        gw = cadd(gw, cdiv(v, float(double(q) * double(q) + 1.0)));
+                    }
+                    v = cf{0.f, 0.f};
+                }
                 if (dphase > fl.filteringMin)
                     v = cscl(v, (fl.filteringMax - dphase) / (fl.filteringMax - fl.filteringMin));
             }
         }
     }
+    if (depth > 0) gw = cadd(gw, v);
     out.time = ntime;
     out.v = v;
     out.dphase = dphase;
+    out.gw_add = gw;
     out.splat = false;
+    out.sample = 0.f;
+    out.value = cf{0.f, 0.f};
     // Integrator::splat (integrator.h:113-135)
-    const float sampleWeight = p.sample_weight;
     if (!fl.produceDebugImage) {
         if (sampleWeight == 0.f || v.re == 0.f || v.im == 0.f) return true;
     }
@@ -393,6 +409,55 @@ __device__ __forceinline__ void flush_row(double *acc, float *s_re, float *s_im,
         s_re[k] = 0.f;
         s_im[k] = 0.f;
     }
+}
+
+}  // namespace hsr
+
+namespace hsr {
+
+// Per-pose state a CTA loads when it starts on a pose.
+struct PoseCtx {
+    Ant tx, rx;
+    int64_t offset;
+    float weight;
+    int train;
+    const int *samp_child;
+    const float *samp_p;
+    const int *train_child;
+    float *train_acc;
+};
+
+__device__ __forceinline__ PoseCtx load_pose(const TraceParams &p, int pose) {
+    PoseCtx c;
+    c.tx = load_ant(p.tx + pose);
+    c.rx = load_ant(p.rx + pose);
+    c.offset = __ldg(&p.offset[pose]);
+    c.weight = p.weights ? __ldg(&p.weights[pose]) : p.sample_weight;
+    c.train = (p.do_guide && p.train) ? __ldg(&p.train[pose]) : 0;
+    const size_t g = size_t(pose) * kGuideMaxNodes;
+    c.samp_child = p.do_guide ? p.g_samp_child + g : nullptr;
+    c.samp_p = p.do_guide ? p.g_samp_p + g : nullptr;
+    c.train_child = p.do_guide ? p.g_train_child + g : nullptr;
+    c.train_acc = p.do_guide ? p.g_train_acc + 3 * g : nullptr;
+    return c;
+}
+
+// guiding.splat(|guidingWeight| * primaryPdf, {}, 1 / primaryPdf, primary) (path.h:448-450).
+// Only the second moment drives the tree, so zero-density samples add nothing.
+__device__ __forceinline__ void guide_train(const PoseCtx &c, cf gw, float pdf, float x0, float x1) {
+    if (!c.train || !(pdf > 0.f)) return;
+    // std::abs(radar::complex) (complex.h:225-237)
+    float ax = fabsf(gw.re), ay = fabsf(gw.im);
+    float s = ax < ay ? ay : ax;
+    float mag = 0.f;
+    if (s != 0.f) {
+        ax /= s;
+        ay /= s;
+        mag = s * sqrtf(ax * ax + ay * ay);
+    }
+    const float density = mag * pdf;
+    if (density == 0.f) return;
+    guide_splat(c.train_child, c.train_acc, density, 1.f / pdf, x0, x1);
 }
 
 }  // namespace hsr

@@ -28,14 +28,18 @@ struct PathRecord {  // one next-event estimate (tests only)
 
 // One sample, one thread: PathTracer::sample (path.h:235-451) for every flag combination.
 template <int kPhase, bool kRecord, bool kCount>
-__device__ void trace_sample(const TraceParams &p, const Ant &tx, const Ant &rx, uint64_t hindex, float *s_re,
-                             float *s_im, PathRecord *rec, int max_rec, TraversalCounters *cnt, unsigned *rays) {
+__device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t hindex, float *s_re, float *s_im,
+                             PathRecord *rec, int max_rec, TraversalCounters *cnt, unsigned *rays) {
+    const Ant &tx = pc.tx;
+    const Ant &rx = pc.rx;
     const hsr_rf_config &rf = p.rf;
     const hsr_tracer_flags &fl = p.flags;
     const float inf = CUDART_INF_F;
     int dim = 0;
     const float maxDist = rf.adcRate / rf.freqSlope * kSpeedOfLight;
-    const float primaryPdf = 1.f;
+    float primaryPdf = 1.f;
+    float px = 0.f, py = 0.f;
+    cf gw = cf{0.f, 0.f};
     const float bandwidth = rf.freqSlope * rf.rampTime;
     const float freq = rf.startFreq + halton(hindex, dim++) * bandwidth;
     const float k0 = 2.f * kPi * freq / kSpeedOfLight;
@@ -53,10 +57,11 @@ __device__ void trace_sample(const TraceParams &p, const Ant &tx, const Ant &rx,
     while (true) {
         const f3 tmpd = d;
         if (depth == 0) {
-            float u0 = halton(hindex, dim++);
-            float u1 = halton(hindex, dim++);
+            px = halton(hindex, dim++);
+            py = halton(hindex, dim++);
+            if (fl.doGuiding) primaryPdf = guide_sample(pc.samp_child, pc.samp_p, px, py);
             o = tx.pos;
-            antenna_sample(tx, u0, u1, d, H);
+            antenna_sample(tx, px, py, d, H);
             H = c3_scl(H, 1.f / primaryPdf);
         } else if (!fl.useGeometricalOptics) {
             float u0 = halton(hindex, dim++);
@@ -71,7 +76,8 @@ __device__ void trace_sample(const TraceParams &p, const Ant &tx, const Ant &rx,
         if (!(depth == 0 && fl.onlyIndirect)) {
             NeeOut ne;
             if (nee_eval<kPhase, kCount>(p, tx, rx, depth, o, d, tmpd, hit_n, inc_H, H, time, plen, r, cosTheta,
-                                         freq, ne, cnt, rays)) {
+                                         freq, pc.weight, ne, cnt, rays)) {
+                gw = cadd(gw, ne.gw_add);
                 if (kRecord && nrec < max_rec) {
                     PathRecord *rc = rec + nrec++;
                     rc->depth = depth;
@@ -117,6 +123,7 @@ __device__ void trace_sample(const TraceParams &p, const Ant &tx, const Ant &rx,
         o = hp;
         depth++;
     }
+    guide_train(pc, gw, primaryPdf, px, py);
 }
 
 template <int kPhase, bool kRecord, bool kCount>
@@ -130,8 +137,7 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
     float *s_re = smem, *s_im = smem + p.samples;
     for (int k = threadIdx.x; k < 2 * p.samples; k += blockDim.x) smem[k] = 0.f;
     int cur_pose = -1;
-    Ant tx, rx;
-    int64_t offset = 0;
+    PoseCtx pc;
     while (true) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = (long long)atomicAdd((unsigned long long *)p.work_counter, 1ull);
@@ -145,15 +151,13 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
                 __syncthreads();
             }
             cur_pose = pose;
-            tx = load_ant(p.tx + pose);
-            rx = load_ant(p.rx + pose);
-            offset = __ldg(&p.offset[pose]);
+            pc = load_pose(p, pose);
         }
         const int64_t budget = __ldg(&p.budget[pose]);
         const int64_t first = (item - __ldg(&p.tile_start[pose])) * p.tile;
         const int64_t last = min(first + p.tile, budget);
         for (int64_t s = first + threadIdx.x; s < last; s += blockDim.x) {
-            trace_sample<kPhase, kRecord, kCount>(p, tx, rx, uint64_t(offset + s), s_re, s_im,
+            trace_sample<kPhase, kRecord, kCount>(p, pc, uint64_t(pc.offset + s), s_re, s_im,
                                                   kRecord ? records + s * max_rec : nullptr, max_rec, &cnt, &rays);
         }
     }
@@ -199,17 +203,18 @@ __global__ void k_tile_prefix(const int64_t *__restrict__ budget, int32_t pose_c
     if (threadIdx.x == 0) tile_start[pose_count] = s_base;
 }
 
-// fetchFrame (path.h:453-455): frame / totalWeight with totalWeight = budget * weight
+// fetchFrame (path.h:453-455): frame / totalWeight, with totalWeight = budget * weight
+// (plain runs) or the schedule's accumulated weight (total_weight, guided runs)
 __global__ void k_finalize(const double *__restrict__ acc, int32_t pose_count, int32_t samples,
-                           const int64_t *__restrict__ budget, float sample_weight, int normalise,
-                           float *__restrict__ out) {
+                           const int64_t *__restrict__ budget, float sample_weight,
+                           const double *__restrict__ total_weight, int normalise, float *__restrict__ out) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     int64_t n = int64_t(pose_count) * samples;
     if (i >= n) return;
     int pose = int(i / samples);
     float re = float(acc[2 * i]), im = float(acc[2 * i + 1]);
     if (normalise) {
-        double tw = double(budget[pose]) * double(sample_weight);
+        double tw = total_weight ? total_weight[pose] : double(budget[pose]) * double(sample_weight);
         float inv = 1.f / float(tw);
         re *= inv;
         im *= inv;
@@ -297,6 +302,23 @@ int launch_trace(const TraceParams &p, int phase_mode, int splat_mode, int grid,
     return 0;
 }
 
+// Zeroes the accumulator rows of the poses with clear[pose] != 0 (clearFrame, path.h:147-150).
+__global__ void k_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *__restrict__ clear) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= int64_t(pose_count) * samples) return;
+    if (clear[i / samples]) {
+        acc[2 * i] = 0.0;
+        acc[2 * i + 1] = 0.0;
+    }
+}
+
+int launch_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *clear, cudaStream_t st) {
+    int64_t n = int64_t(pose_count) * samples;
+    k_clear_rows<<<unsigned((n + 255) / 256), 256, 0, st>>>(acc, pose_count, samples, clear);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, int64_t *tile_start, cudaStream_t st) {
     k_tile_prefix<<<1, 1024, 0, st>>>(budget, pose_count, tile, tile_start);
     note_launches(1);
@@ -304,10 +326,10 @@ int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, 
 }
 
 int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, const int64_t *budget, float sample_weight,
-                    int normalise, float *out_rows, cudaStream_t st) {
+                    const double *total_weight, int normalise, float *out_rows, cudaStream_t st) {
     int64_t n = int64_t(pose_count) * samples;
-    k_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(acc, pose_count, samples, budget, sample_weight, normalise,
-                                                           out_rows);
+    k_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(acc, pose_count, samples, budget, sample_weight,
+                                                           total_weight, normalise, out_rows);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

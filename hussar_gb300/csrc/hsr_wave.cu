@@ -29,6 +29,7 @@ struct WaveShared {
     float h[6][kStack];                        // incoming H field (re, im) x 3
     float nx[kStack], ny[kStack], nz[kStack];  // faceforwarded normal at the hit
     float time[kStack], r[kStack], cosT[kStack], freq[kStack];
+    float px[kStack], py[kStack], pdf[kStack], gwr[kStack], gwi[kStack];  // guiding: primary, pdf, weight
     int depth[kStack];
     double plen[kStack];  // FP64 path length (split-phase mode)
     int count;
@@ -36,8 +37,13 @@ struct WaveShared {
     long long gen, gen_end, pending_first, pending_last;
 };
 
+struct Guided {  // the guiding part of a path's state
+    float x0, x1, pdf;
+    cf gw;
+};
+
 __device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H, f3 n, float time, float r,
-                                          float cosT, float freq, int depth, double plen) {
+                                          float cosT, float freq, int depth, double plen, const Guided &g) {
     const int slot = atomicAdd(&S.count, 1);  // < kStack by construction (see k_wave)
     S.ox[slot] = o.x;
     S.oy[slot] = o.y;
@@ -59,6 +65,11 @@ __device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H
     S.freq[slot] = freq;
     S.depth[slot] = depth;
     S.plen[slot] = plen;
+    S.px[slot] = g.x0;
+    S.py[slot] = g.x1;
+    S.pdf[slot] = g.pdf;
+    S.gwr[slot] = g.gw.re;
+    S.gwi[slot] = g.gw.im;
 }
 
 // Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
@@ -104,8 +115,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
     }
     __syncthreads();
 
-    Ant tx, rx;
-    int64_t offset = 0;
+    PoseCtx pc;
     int cur_pose = -1;
 
     while (true) {
@@ -144,29 +154,34 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
             bool has_item = false;
             SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
             if (s < gen_end) {
-                const uint64_t hindex = uint64_t(offset + s);
+                const uint64_t hindex = uint64_t(pc.offset + s);
                 const float freq = rf.startFreq + halton(hindex, 0) * bandwidth;
-                const float u0 = halton(hindex, 1);
-                const float u1 = halton(hindex, 2);
-                f3 o = tx.pos, d;
+                Guided g{halton(hindex, 1), halton(hindex, 2), 1.f, cf{0.f, 0.f}};
+                if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
+                f3 o = pc.tx.pos, d;
                 c3 H;
-                antenna_sample(tx, u0, u1, d, H);
+                antenna_sample(pc.tx, g.x0, g.x1, d, H);
+                H = c3_scl(H, 1.f / g.pdf);
                 if (!fl.onlyIndirect) {
                     NeeOut ne;
-                    if (nee_eval<kPhase, false>(p, tx, rx, 0, o, d, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H,
-                                                0.f, 0.0, 0.f, 1.f, freq, ne, nullptr, nullptr) &&
+                    if (nee_eval<kPhase, false>(p, pc.tx, pc.rx, 0, o, d, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H,
+                                                H, 0.f, 0.0, 0.f, 1.f, freq, pc.weight, ne, nullptr, nullptr) &&
                         ne.splat) {
                         item = splat_prepare(ne.sample, ne.value);
                         has_item = true;
                     }
                 }
+                bool alive = false;
                 if (!(0 >= fl.maxDepth || 0.f >= maxDist) && !c3_is_zero(H)) {
                     float time = 0.f, r = 0.f, cosT;
                     double plen = 0.0;
                     f3 hp, n;
-                    if (walk(p, o, d, H, time, r, plen, hp, n, cosT))
-                        push_path(S, hp, d, H, n, time, r, cosT, freq, 1, plen);
+                    if (walk(p, o, d, H, time, r, plen, hp, n, cosT)) {
+                        push_path(S, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
+                        alive = true;
+                    }
                 }
+                if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
             }
             if (!fl.onlyIndirect) splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
@@ -182,8 +197,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
             float time = 0.f, r = 0.f, cosT = 1.f, freq = 0.f;
             int depth = 0;
             double plen = 0.0;
+            Guided g{0.f, 0.f, 1.f, cf{0.f, 0.f}};
             if (mine) {
                 const int slot = count - 1 - tid;
+                g = Guided{S.px[slot], S.py[slot], S.pdf[slot], cf{S.gwr[slot], S.gwi[slot]}};
                 o = mk3(S.ox[slot], S.oy[slot], S.oz[slot]);
                 din = mk3(S.dx[slot], S.dy[slot], S.dz[slot]);
 #pragma unroll
@@ -206,18 +223,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                 c3 H = Hin;
                 reflect(nrm, d, H);
                 NeeOut ne;
-                if (nee_eval<kPhase, false>(p, tx, rx, depth, o, d, din, nrm, Hin, H, time, plen, r, cosT, freq, ne,
-                                            nullptr, nullptr) &&
-                    ne.splat) {
-                    item = splat_prepare(ne.sample, ne.value);
-                    has_item = true;
+                if (nee_eval<kPhase, false>(p, pc.tx, pc.rx, depth, o, d, din, nrm, Hin, H, time, plen, r, cosT, freq,
+                                            pc.weight, ne, nullptr, nullptr)) {
+                    g.gw = cadd(g.gw, ne.gw_add);
+                    if (ne.splat) {
+                        item = splat_prepare(ne.sample, ne.value);
+                        has_item = true;
+                    }
                 }
+                bool alive = false;
                 if (!(depth >= fl.maxDepth || r >= maxDist) && !c3_is_zero(H)) {
                     f3 hp, n2;
                     float cosT2;
-                    if (walk(p, o, d, H, time, r, plen, hp, n2, cosT2))
-                        push_path(S, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen);
+                    if (walk(p, o, d, H, time, r, plen, hp, n2, cosT2)) {
+                        push_path(S, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
+                        alive = true;
+                    }
                 }
+                if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
             }
             splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
@@ -228,9 +251,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
             // stack drained: finish the old pose's row and switch to the new pose
             if (cur_pose >= 0) flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
             cur_pose = pending;
-            tx = load_ant(p.tx + cur_pose);
-            rx = load_ant(p.rx + cur_pose);
-            offset = __ldg(&p.offset[cur_pose]);
+            pc = load_pose(p, cur_pose);
             __syncthreads();
             if (tid == 0) {
                 S.pose = pending;

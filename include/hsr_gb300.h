@@ -173,6 +173,23 @@ hsr_status hsr_backend_run(const hsr_scene *scene, const hsr_rf_config *rf,
                            int32_t phase_mode, float *frame_inout,
                            double *total_weight_inout, const volatile int32_t *interrupt_flag);
 
+/* PathTracer::run (path.h:171-224) for one pose, guided or plain: clears the frame,
+ * then (doGuiding = 0) one backend run over Halton indices [0, samples), or (doGuiding =
+ * 1) the doubling schedule from 16384 samples with device path guiding of the primary
+ * sample square (GuidingWrapper, path.h:17-131, settings path.h:229-232) trained on
+ * every iteration but the final one, clearing the frame between iterations when
+ * clearBeforeIteration is set (else weighting later samples 10x, path.h:212-220).
+ * Outputs the frame's raw sums (host, complex64 [chirp][sample][channel], overwritten)
+ * and its total weight; fetchFrame() is frame_out / *total_weight_out. The guided
+ * estimator is the reference's; its tree (a 2-D adaptive binary tree with the same
+ * uniform mixture, split threshold and second-moment criterion) is this library's own,
+ * libguiding not being part of the reference sources. */
+hsr_status hsr_path_tracer_run(hsr_scene *scene, const hsr_rf_config *rf,
+                               const hsr_frame_config *frame, const hsr_antenna *tx,
+                               const hsr_antenna *rx, const hsr_tracer_flags *flags,
+                               int64_t samples, int32_t phase_mode, float *frame_out,
+                               double *total_weight_out, const volatile int32_t *interrupt_flag);
+
 /* Batched simulation: pose_count independent sensor poses (tx[i], rx[i]) with their
  * own sample budgets, all traced by ONE persistent launch on `stream`
  * (a cudaStream_t, or NULL for the legacy default stream).
@@ -183,7 +200,9 @@ hsr_status hsr_backend_run(const hsr_scene *scene, const hsr_rf_config *rf,
  * channel, path.h:291-292); complex64 interleaved.
  * All pointer arguments are DEVICE pointers (inputs already resident). Asynchronous
  * on `stream`; scratch is owned by the scene and reused across calls on it, so calls
- * on one scene must not overlap. */
+ * on one scene must not overlap. With flags->doGuiding every pose runs the guided
+ * schedule of hsr_path_tracer_run (its own tree); the schedule is planned on the host,
+ * so that form reads the budgets back and synchronises between iterations. */
 hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
                                      int32_t samples_per_chirp, const hsr_tracer_flags *flags,
                                      int32_t pose_count, const hsr_antenna *d_tx,
