@@ -106,6 +106,7 @@ def lib():
         "hsr_debug_traversal_counts": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp,
                                        vp, vp],
         "hsr_set_path_kernel": [ctypes.c_int32],
+        "hsr_set_synth_engine": [ctypes.c_int32],
         "hsr_last_kernel_ms": [vp, P(ctypes.c_float)],
     }
     for name, args in sigs.items():

@@ -23,6 +23,7 @@ UNITS = {
     "hsr_api.cu": [],
     "hsr_bvh.cu": [],
     "hsr_guide.cu": [],
+    "hsr_synth.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
 }

@@ -16,6 +16,7 @@ namespace hsr {
 
 static thread_local std::string g_err;
 int g_path_kernel = 0;
+int g_synth_engine = 0;
 static std::atomic<int64_t> g_launches{0};
 
 void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -54,8 +55,8 @@ static hsr_status validate_common(const hsr_rf_config *rf, int32_t samples, cons
 static hsr_status validate_phase(int32_t phase_mode, int32_t splat_mode) {
     if (phase_mode != HSR_PHASE_REFERENCE_FP32 && phase_mode != HSR_PHASE_SPLIT_FP64)
         return fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
-    if (splat_mode != HSR_SPLAT_DIRICHLET16)
-        return fail(HSR_ERR_NOT_SUPPORTED, "splat mode not available in this build");
+    if (splat_mode != HSR_SPLAT_DIRICHLET16 && splat_mode != HSR_SPLAT_FINE_SYNTH)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "unknown splat mode");
     return HSR_OK;
 }
 
@@ -67,6 +68,7 @@ struct Scratch {
     int *train, *active, *clear;
     double *tw;
     double *acc;
+    float *fine;  // fine-histogram rows (HSR_SPLAT_FINE_SYNTH), P x kFineRowPerBin N floats
     float *rows;
     unsigned *counters;  // [0] status word, [2..3] 64-bit work counter
     size_t bytes;
@@ -74,7 +76,7 @@ struct Scratch {
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-static Scratch carve(void *base, int32_t P, int32_t N) {
+static Scratch carve(void *base, int32_t P, int32_t N, bool fine) {
     Scratch s;
     char *p = static_cast<char *>(base);
     size_t off = 0;
@@ -95,13 +97,14 @@ static Scratch carve(void *base, int32_t P, int32_t N) {
     s.clear = reinterpret_cast<int *>(take(sizeof(int) * P));
     s.tw = reinterpret_cast<double *>(take(sizeof(double) * P));
     s.acc = reinterpret_cast<double *>(take(sizeof(double) * 2 * size_t(P) * N));
+    s.fine = fine ? reinterpret_cast<float *>(take(sizeof(float) * kFineRowPerBin * size_t(P) * N)) : nullptr;
     s.rows = reinterpret_cast<float *>(take(sizeof(float) * 2 * size_t(P) * N));
     s.bytes = off;
     return s;
 }
 
-static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &out) {
-    Scratch need = carve(nullptr, P, N);
+static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &out, bool fine = false) {
+    Scratch need = carve(nullptr, P, N, fine);
     if (need.bytes > sc.scratch_bytes) {
         if (sc.scratch) {
             cudaDeviceSynchronize();
@@ -116,7 +119,41 @@ static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &ou
         if (e != cudaSuccess) return cuda_fail(e, "scratch clear");
         sc.scratch_bytes = need.bytes;
     }
-    out = carve(sc.scratch, P, N);
+    out = carve(sc.scratch, P, N, fine);
+    return HSR_OK;
+}
+
+// Twiddle operand for N bins (cached per scene) and the synthesis scratch for P poses.
+static hsr_status ensure_synth(SceneDev &sc, int32_t N, int32_t P, cudaStream_t st) {
+    if (sc.synth.N != N) {
+        cudaDeviceSynchronize();
+        synth_free_operand(sc.synth);
+        std::string err;
+        const int rc = synth_build_operand(sc.synth, N, st, err);
+        if (rc != 0) {
+            synth_free_operand(sc.synth);
+            return fail(rc == 3 ? HSR_ERR_OUT_OF_MEMORY : HSR_ERR_CUDA, err);
+        }
+    }
+    const size_t need = synth_scratch_bytes(sc.synth, P);
+    if (need > sc.synth_scratch_bytes) {
+        cudaDeviceSynchronize();
+        cudaFree(sc.synth_scratch);
+        sc.synth_scratch = nullptr;
+        sc.synth_scratch_bytes = 0;
+        cudaError_t e = cudaMalloc(&sc.synth_scratch, need);
+        if (e != cudaSuccess) return cuda_fail(e, "synthesis scratch");
+        sc.synth_scratch_bytes = need;
+    }
+    return HSR_OK;
+}
+
+static hsr_status synthesise(SceneDev &sc, const Scratch &s, int32_t P, float sample_weight, const double *tw,
+                             int normalise, float *d_out_rows, cudaStream_t st) {
+    std::string err;
+    if (synth_run(sc.synth, s.fine, P, sc.synth_scratch, g_synth_engine, s.budget, sample_weight, tw, normalise,
+                  d_out_rows, s.counters, st, err) != 0)
+        return fail(HSR_ERR_CUDA, err);
     return HSR_OK;
 }
 
@@ -200,6 +237,8 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     p.max_rec = max_rec;
     p.counters = counters;
     p.weights = per_pose_weights ? s.weights : nullptr;
+    p.fine = splat_mode == HSR_SPLAT_FINE_SYNTH ? s.fine : nullptr;
+    p.fine_bins = kFineOS * N;
     p.do_guide = (fl->doGuiding && g) ? 1 : 0;
     if (p.do_guide) {
         p.train = s.train;
@@ -230,13 +269,21 @@ static hsr_status run_plain(SceneDev &sc, const Scratch &s, const hsr_rf_config 
                             int32_t splat_mode, int normalise, float *d_out_rows, cudaStream_t st,
                             void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr) {
     cudaError_t e;
-    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess)
+    const bool fine = splat_mode == HSR_SPLAT_FINE_SYNTH;
+    if (fine) {
+        hsr_status r = ensure_synth(sc, N, P, st);
+        if (r != HSR_OK) return r;
+        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(float) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
+            return cuda_fail(e, "memset fine histogram");
+    } else if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess) {
         return cuda_fail(e, "memset accumulators");
+    }
     hsr_tracer_flags plain = *fl;
     plain.doGuiding = 0;
     hsr_status r = enqueue_pass(sc, s, rf, N, &plain, P, sample_weight, false, phase_mode, splat_mode, st, nullptr,
                                 records, max_rec, counters);
     if (r != HSR_OK) return r;
+    if (fine) return synthesise(sc, s, P, sample_weight, nullptr, normalise, d_out_rows, st);
     if (launch_finalize(s.acc, P, N, s.budget, sample_weight, nullptr, normalise, d_out_rows, st) != 0)
         return cuda_fail(cudaGetLastError(), "finalize launch");
     return HSR_OK;
@@ -295,8 +342,15 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
         K = std::max(K, sched[p].size());
     }
     cudaError_t e;
-    if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess)
+    const bool fine = splat_mode == HSR_SPLAT_FINE_SYNTH;
+    if (fine) {
+        r = ensure_synth(sc, N, P, st);
+        if (r != HSR_OK) return r;
+        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(float) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
+            return cuda_fail(e, "memset fine histogram");
+    } else if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess) {
         return cuda_fail(e, "memset accumulators");
+    }
     if (launch_guide_reset(P, g.samp_child, g.samp_p, g.train_child, g.train_acc, g.train_count, st) != 0)
         return cuda_fail(cudaGetLastError(), "guide reset");
     std::vector<int64_t> b(P), o(P);
@@ -336,8 +390,11 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
             (e = cudaMemcpyAsync(s.clear, clear.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
             (e = cudaMemcpyAsync(s.active, active.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
             return cuda_fail(e, "schedule upload");
-        if (any_clear && launch_clear_rows(s.acc, P, N, s.clear, st) != 0)
-            return cuda_fail(cudaGetLastError(), "clear rows");
+        if (any_clear) {
+            const int rc = fine ? launch_clear_rows_f(s.fine, P, kFineRowPerBin * N, s.clear, st)
+                                : launch_clear_rows(s.acc, P, N, s.clear, st);
+            if (rc != 0) return cuda_fail(cudaGetLastError(), "clear rows");
+        }
         r = enqueue_pass(sc, s, rf, N, fl, P, 1.f, true, phase_mode, splat_mode, st, &g);
         if (r != HSR_OK) return r;
         if (any_active && launch_guide_step(P, s.active, g.samp_child, g.samp_p, g.train_child, g.train_acc,
@@ -348,8 +405,12 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
     }
     if ((e = cudaMemcpyAsync(s.tw, tw.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return cuda_fail(e, "weight upload");
-    if (launch_finalize(s.acc, P, N, s.budget, 1.f, s.tw, normalise, d_out_rows, st) != 0)
+    if (fine) {
+        r = synthesise(sc, s, P, 1.f, s.tw, normalise, d_out_rows, st);
+        if (r != HSR_OK) return r;
+    } else if (launch_finalize(s.acc, P, N, s.budget, 1.f, s.tw, normalise, d_out_rows, st) != 0) {
         return cuda_fail(cudaGetLastError(), "finalize launch");
+    }
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "guided finalize");
     if (h_total_weight)
         for (int p = 0; p < P; ++p) h_total_weight[p] = tw[p];
@@ -368,6 +429,7 @@ static hsr_status read_status(const Scratch &s, cudaStream_t st) {
         if (bits & kStatusStackOverflow) m += " traversal-stack-overflow";
         if (bits & kStatusBadBin) m += " bin-out-of-range";
         if (bits & kStatusBadWorkItem) m += " bad-work-item";
+        if (bits & (1u << 3)) m += " synthesis-wait-timeout";
         return fail(HSR_ERR_DEVICE, m);
     }
     return HSR_OK;
@@ -488,6 +550,8 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
     cudaFree(s->dev.nodes);
     cudaFree(s->dev.scratch);
     cudaFree(s->dev.guide);
+    synth_free_operand(s->dev.synth);
+    cudaFree(s->dev.synth_scratch);
     if (s->dev.ev0) cudaEventDestroy(s->dev.ev0);
     if (s->dev.ev1) cudaEventDestroy(s->dev.ev1);
     delete s;
@@ -699,7 +763,7 @@ hsr_status hsr_simulate_batch_device(hsr_scene *s, const hsr_rf_config *rf, int3
     if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
+    if ((st = ensure_scratch(s->dev, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
     if ((st = upload_poses(sc, P, d_tx, d_rx, d_budget, d_offset, cudaMemcpyDeviceToDevice, strm)) != HSR_OK)
         return st;
@@ -728,7 +792,7 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
+    if ((st = ensure_scratch(s->dev, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
     if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
     if (!fl->doGuiding) {
@@ -782,6 +846,12 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int
 hsr_status hsr_set_path_kernel(int32_t kind) {
     if (kind != 0 && kind != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "kind must be 0 or 1");
     g_path_kernel = kind;
+    return HSR_OK;
+}
+
+hsr_status hsr_set_synth_engine(int32_t engine) {
+    if (engine != 0 && engine != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "engine must be 0 or 1");
+    g_synth_engine = engine;
     return HSR_OK;
 }
 

@@ -14,6 +14,18 @@ namespace hsr {
 struct DTri;
 struct DNode;
 
+// Fine range histogram: 8 sub-bins per range bin and moments 0..3 of the sub-bin offset.
+constexpr int kFineOS = 8;
+constexpr int kFineMoments = 4;
+constexpr int kFineRowPerBin = 2 * kFineMoments * kFineOS;  // floats per range bin per pose
+
+// Twiddle operand of the fine-histogram synthesis for N range bins (hsr_synth.cu).
+struct SynthOperand {
+    int N = 0, K = 0, KK = 0, KKpad = 0, NCpad = 0;
+    float *bt = nullptr;  // FP32 B^T [NCpad x KKpad]
+    void *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;  // its three BF16 terms
+};
+
 // A resident scene: triangles + BVH on the device, plus per-scene scratch reused by
 // every simulate call on this scene (calls on one scene must not overlap).
 struct SceneDev {
@@ -30,6 +42,9 @@ struct SceneDev {
     unsigned *status = nullptr;  // device status word + work counter
     void *guide = nullptr;       // guiding trees + step scratch, sized for guide_cap poses
     int guide_cap = 0;
+    SynthOperand synth;          // cached twiddle operand (fine-histogram synthesis)
+    void *synth_scratch = nullptr;
+    size_t synth_scratch_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_kernel_ms = 0.f;
     bool timing_valid = false;
@@ -83,9 +98,10 @@ struct TraceParams {
     const float *g_samp_p;
     const int *g_train_child;
     float *g_train_acc;
-    // fine-histogram mode
-    int32_t fine_bins;      // K = N * oversample
-    float *fine;            // [pose_count][3 moments][K] complex, device
+    // fine-histogram mode (HSR_SPLAT_FINE_SYNTH): per pose a row of 8K floats,
+    // [Re h0 .. Re h3 | Im h0 .. Im h3], K = 8 N; nullptr: Dirichlet splat
+    int32_t fine_bins;      // K
+    float *fine;
 };
 
 size_t guide_bytes_per_pose();
@@ -93,6 +109,16 @@ int launch_guide_reset(int P, int *samp_child, float *samp_p, int *train_child, 
                        cudaStream_t st);
 int launch_guide_step(int P, const int *active, int *samp_child, float *samp_p, int *train_child, float *train_acc,
                       int *train_count, float *scratch_e, int *scratch_i, cudaStream_t st);
+
+int synth_build_operand(SynthOperand &op, int N, cudaStream_t st, std::string &err);
+void synth_free_operand(SynthOperand &op);
+size_t synth_scratch_bytes(const SynthOperand &op, int P);
+int synth_run(const SynthOperand &op, const float *fine, int P, void *scratch, int engine, const int64_t *budget,
+              float sample_weight, const double *tw, int normalise, float *out_rows, unsigned *status, cudaStream_t st,
+              std::string &err);
+int launch_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st);
+// 0: tensor cores (tcgen05, split BF16); 1: CUDA cores (FP32)
+extern int g_synth_engine;
 
 // Launches (all asynchronous on `st`).
 int launch_trace(const TraceParams &p, int phase_mode, int splat_mode, int grid, cudaStream_t st, std::string &err);

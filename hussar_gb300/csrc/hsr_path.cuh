@@ -388,6 +388,27 @@ __device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, unsi
     }
 }
 
+// Fine range histogram (HSR_SPLAT_FINE_SYNTH): 8 sub-bins per range bin with moments
+// h_d += c eps^d / d! (d = 0..3) of the sub-bin offset eps (in bins); the spectrum is
+// synthesised from it afterwards (hsr_synth.cu). `row` is the pose's
+// [Re h0..h3 | Im h0..h3] row, K = 8 N.
+__device__ __forceinline__ void splat_fine(float *row, int K, float sample, cf value) {
+    const float bs = sample * float(kFineOS);
+    const float kk = rintf(bs);
+    const float eps = (bs - kk) * (1.f / float(kFineOS));
+    int k = int(kk);
+    if (k >= K) k -= K;
+    if (k < 0) k += K;
+    if (k < 0 || k >= K) k = 0;  // NaN/inf samples land in bin 0 rather than out of bounds
+    float m = 1.f;
+#pragma unroll
+    for (int d = 0; d < kFineMoments; ++d) {
+        atomicAdd(row + d * K + k, value.re * m);
+        atomicAdd(row + (kFineMoments + d) * K + k, value.im * m);
+        m = m * eps / float(d + 1);
+    }
+}
+
 __device__ __forceinline__ int find_pose(const int64_t *__restrict__ tile_start, int pose_count, int64_t item) {
     int lo = 0, hi = pose_count;  // tile_start[lo] <= item < tile_start[hi]
     while (hi - lo > 1) {
@@ -419,6 +440,7 @@ namespace hsr {
 struct PoseCtx {
     Ant tx, rx;
     int64_t offset;
+    float *fine_row;  // fine-histogram row of the pose (nullptr: Dirichlet splat)
     float weight;
     int train;
     const int *samp_child;
@@ -432,6 +454,7 @@ __device__ __forceinline__ PoseCtx load_pose(const TraceParams &p, int pose) {
     c.tx = load_ant(p.tx + pose);
     c.rx = load_ant(p.rx + pose);
     c.offset = __ldg(&p.offset[pose]);
+    c.fine_row = p.fine ? p.fine + size_t(pose) * 2 * kFineMoments * p.fine_bins : nullptr;
     c.weight = p.weights ? __ldg(&p.weights[pose]) : p.sample_weight;
     c.train = (p.do_guide && p.train) ? __ldg(&p.train[pose]) : 0;
     const size_t g = size_t(pose) * kGuideMaxNodes;

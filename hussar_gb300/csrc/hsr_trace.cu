@@ -90,7 +90,12 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
                     rc->value_re = ne.value.re;
                     rc->value_im = ne.value.im;
                 }
-                if (ne.splat) splat_serial(s_re, s_im, p.samples, splat_prepare(ne.sample, ne.value));
+                if (ne.splat) {
+                    if (pc.fine_row)
+                        splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
+                    else
+                        splat_serial(s_re, s_im, p.samples, splat_prepare(ne.sample, ne.value));
+                }
             }
         }
 
@@ -310,6 +315,20 @@ __global__ void k_clear_rows(double *acc, int32_t pose_count, int32_t samples, c
         acc[2 * i] = 0.0;
         acc[2 * i + 1] = 0.0;
     }
+}
+
+// Zeroes the fine-histogram rows (len floats each) of the poses with clear[pose] != 0.
+__global__ void k_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *__restrict__ clear) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= int64_t(pose_count) * len) return;
+    if (clear[i / len]) rows[i] = 0.f;
+}
+
+int launch_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st) {
+    int64_t n = int64_t(pose_count) * len;
+    k_clear_rows_f<<<unsigned((n + 255) / 256), 256, 0, st>>>(rows, pose_count, len, clear);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *clear, cudaStream_t st) {

@@ -167,8 +167,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                     if (nee_eval<kPhase, false>(p, pc.tx, pc.rx, 0, o, d, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H,
                                                 H, 0.f, 0.0, 0.f, 1.f, freq, pc.weight, ne, nullptr, nullptr) &&
                         ne.splat) {
-                        item = splat_prepare(ne.sample, ne.value);
-                        has_item = true;
+                        if (pc.fine_row) {
+                            splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
+                        } else {
+                            item = splat_prepare(ne.sample, ne.value);
+                            has_item = true;
+                        }
                     }
                 }
                 bool alive = false;
@@ -227,8 +231,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                                             pc.weight, ne, nullptr, nullptr)) {
                     g.gw = cadd(g.gw, ne.gw_add);
                     if (ne.splat) {
-                        item = splat_prepare(ne.sample, ne.value);
-                        has_item = true;
+                        if (pc.fine_row) {
+                            splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
+                        } else {
+                            item = splat_prepare(ne.sample, ne.value);
+                            has_item = true;
+                        }
                     }
                 }
                 bool alive = false;

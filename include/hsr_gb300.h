@@ -242,6 +242,11 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
  * Both compute the same per-path values; tests use this to check each one. */
 hsr_status hsr_set_path_kernel(int32_t kind);
 
+/* Engine of the fine-histogram synthesis GEMM (process-wide): 0 (default) = tensor cores
+ * (tcgen05.mma, operands split into three BF16 terms, FP32 accumulation), 1 = CUDA cores
+ * in FP32. Both compute the same product; tests use this to check one against the other. */
+hsr_status hsr_set_synth_engine(int32_t engine);
+
 /* Timing of the most recent batch launch on this scene: device milliseconds of the
  * trace kernel alone, measured with CUDA events on the launching stream. */
 hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);

@@ -671,6 +671,7 @@ template <typename R> static inline void atomic_add(R *addr, R v) {
 template <typename R> struct Frame {
     int chirps = 1, samples = 1, channels = 1;
     R *data = nullptr;  // interleaved re, im
+    bool exact = false; // exact finite-N Dirichlet synthesis instead of Frame::splat<16>
     size_t index(int c, int s, int ch) const { return (size_t(c) * samples + s) * channels + ch; }
 };
 
@@ -728,6 +729,35 @@ template <typename R> static void frame_splat(Frame<R> &f, R idx_chirp, R idx_sa
                 atomic_add(&f.data[2 * id + 1], w2 * value.im);
             }
         }
+    }
+}
+
+// The spectrum of one sampled complex exponential, without truncation: the value the
+// contribution adds to range bin m is value * D_N(b - m) / N with
+// D_N(x) = sum_{n<N} exp(j 2 pi x n / N) = exp(j pi x (N-1)/N) sin(pi x) / sin(pi x / N).
+// (Frame::splat<16>, radar.h:564-626, is its N -> infinity limit truncated to +-16 bins.)
+// Evaluated in double; used by the FP64 oracle of the fine-histogram synthesis mode.
+template <typename R> static void frame_splat_exact(Frame<R> &f, double b, Cx<R> value) {
+    const int N = f.samples;
+    const double pi = 3.14159265358979323846;
+    for (int m = 0; m < N; ++m) {
+        double x = b - double(m);
+        double xr = std::fmod(x, double(N));
+        if (xr < 0) xr += N;
+        double re, im;
+        if (std::abs(std::sin(pi * xr / N)) < 1e-12) {
+            re = 1.0;  // D_N / N at multiples of N
+            im = 0.0;
+        } else {
+            double mag = std::sin(pi * xr) / std::sin(pi * xr / N) / N;
+            double ph = pi * xr * (N - 1) / N;
+            re = mag * std::cos(ph);
+            im = mag * std::sin(ph);
+        }
+        double vr = double(value.re), vi = double(value.im);
+        size_t id = f.index(0, m, 0);
+        atomic_add(&f.data[2 * id + 0], R(vr * re - vi * im));
+        atomic_add(&f.data[2 * id + 1], R(vr * im + vi * re));
     }
 }
 
@@ -790,7 +820,10 @@ template <typename R> struct Tracer {
             rec->value_im = double(value.im);
             rec->splatted = 1;
         }
-        frame_splat(frame, chirp, sample, R(channel), value);
+        if (frame.exact)
+            frame_splat_exact(frame, double(sample), value);
+        else
+            frame_splat(frame, chirp, sample, R(channel), value);
     }
 
     void reflectRay(Ray<R> &ray, const Isect<R> &isect) const {  // integrator.h:164-168
@@ -997,10 +1030,11 @@ template <typename R>
 static int simulate(const Scene *s, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
                     int64_t budget, int64_t offset, float sampleWeight, int threads, double *frame_out,
-                    double *weight_out, bool floatSamples = false) {
+                    double *weight_out, bool floatSamples = false, bool exact = false) {
     Tracer<R> tr;
     setup_tracer(tr, s, rf, tx, rx, fl);
     tr.floatSamples = floatSamples;
+    tr.frame.exact = exact;
     tr.currentSampleWeight = R(sampleWeight);
     tr.sampleIndexOffset = offset;
     tr.frame.chirps = fc->chirpCount;
@@ -1087,9 +1121,14 @@ int oracle_simulate(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_
     if (fc->chirpCount <= 0 || fc->samplesPerChirp <= 0 || fc->channelCount <= 0) return 1;
     if (fl->doGuiding) return 2;  // guided runs are not restated here
     const Scene *s = static_cast<Scene *>(sp);
+    const bool exact = (precision & 0x100) != 0;  // exact finite-N synthesis instead of splat<16>
+    precision &= 0xff;
     if (precision == 64 || precision == 65)
         return simulate<double>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out,
-                                precision == 65);
+                                precision == 65, exact);
+    if (exact)
+        return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out,
+                               false, true);
     return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
 }
 

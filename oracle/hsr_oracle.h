@@ -53,7 +53,9 @@ int oracle_intersect(void *scene, int64_t count, const float *o, const float *d,
 int oracle_visible(void *scene, int64_t count, const float *o, const float *d, const float *tfar,
                    int32_t *vis);
 /* precision: 32 (reference single-precision semantics), 64 (FP64 oracle) or 65 (FP64
- * oracle fed the float-rounded Halton values of the FP32 run: the same sample set).
+ * oracle fed the float-rounded Halton values of the FP32 run: the same sample set);
+ * OR 0x100 to replace Frame::splat<16> by the exact finite-N Dirichlet synthesis (the
+ * estimator of the fine-histogram mode).
  * frame_out: 2*chirps*samples*channels doubles, ADDED to. */
 int oracle_simulate(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,

@@ -151,11 +151,12 @@ class Scene:
         frame = out.view(np.complex128).reshape(fc.chirpCount, fc.samplesPerChirp, fc.channelCount)
         return frame, w.value
 
-    def fetch_row(self, rf, samples, tx, rx, tracer, budget, precision=32, threads=0, offset=0):
-        """fetchFrame() row (chirp 0, channel 0) of a plain run: frame / totalWeight."""
+    def fetch_row(self, rf, samples, tx, rx, tracer, budget, precision=32, threads=0, offset=0, exact=False):
+        """fetchFrame() row (chirp 0, channel 0) of a plain run: frame / totalWeight.
+        exact: the untruncated finite-N Dirichlet synthesis instead of Frame::splat<16>."""
         from hussar_gb300.radar import FrameConfig
         fr, w = self.simulate(rf, FrameConfig(1, samples, 1), tx, rx, tracer, budget, offset=offset,
-                              precision=precision, threads=threads)
+                              precision=precision | (0x100 if exact else 0), threads=threads)
         return fr[0, :, 0] / w
 
     def records(self, rf, fc, tx, rx, tracer, first, count, offset=0, max_records=None):
