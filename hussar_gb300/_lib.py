@@ -101,6 +101,8 @@ def lib():
                                       vp, ctypes.c_int32, ctypes.c_int32, vp, vp],
         "hsr_simulate_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                ctypes.c_int32, ctypes.c_int32, vp, vp],
+        "hsr_simulate_batch_device_noalloc": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp,
+                                              vp, vp, ctypes.c_int32, vp, vp],
         "hsr_debug_records": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), P(AntennaC), P(AntennaC),
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_traversal_counts": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp,

@@ -24,6 +24,7 @@ UNITS = {
     "hsr_bvh.cu": [],
     "hsr_guide.cu": [],
     "hsr_synth.cu": [],
+    "hsr_noalloc.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
 }

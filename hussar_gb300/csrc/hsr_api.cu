@@ -455,6 +455,13 @@ struct hsr_scene {
     std::mutex mu;
 };
 
+namespace hsr {
+// Read access to a scene's device state, and the calling thread's error message, for
+// entry points defined in other translation units.
+const SceneDev *scene_device_state(const hsr_scene *s) { return s ? &s->dev : nullptr; }
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace hsr
+
 extern "C" {
 
 int32_t hsr_abi_version(void) { return HSR_ABI_VERSION; }

@@ -63,6 +63,8 @@ template <typename T> inline bool dev_alloc(T **p, size_t bytes, std::string &er
 }
 
 void note_launches(int64_t n);
+const SceneDev *scene_device_state(const hsr_scene *s);
+void set_last_error(const std::string &msg);
 
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
               std::string &err);

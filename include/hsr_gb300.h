@@ -210,6 +210,26 @@ hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
                                      const int64_t *d_index_offset, int32_t phase_mode,
                                      int32_t splat_mode, float *d_out_rows, void *stream);
 
+/* Allocation-free form of hsr_simulate_batch_device, for callers that cannot allocate
+ * device memory while they simulate (a real-time loop, work recorded into a larger
+ * asynchronous pipeline, a framework whose memory pool must own every allocation).
+ * It has no counterpart in the reference. Same arguments and output as
+ * hsr_simulate_batch_device for the plain method (doGuiding = 0, the 33-bin frame
+ * splat); its scratch (status, work counter, tile prefix, FP64 accumulators) lives in a
+ * fixed file-scope device array of the library (about 1 MiB per device, held for the
+ * life of the program), so the call performs no allocation. Limits: at most 64 poses
+ * and 1024 range bins per call; larger requests return HSR_ERR_INVALID_ARGUMENT.
+ * The array is shared by all calls on a device and keeps the last call's contents:
+ * calls that overlap on the GPU race and must be serialised by the caller. The first
+ * call on a device looks the array's address up (make it before any stream capture). */
+hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const hsr_rf_config *rf,
+                                             int32_t samples_per_chirp,
+                                             const hsr_tracer_flags *flags, int32_t pose_count,
+                                             const hsr_antenna *d_tx, const hsr_antenna *d_rx,
+                                             const int64_t *d_budget,
+                                             const int64_t *d_index_offset, int32_t phase_mode,
+                                             float *d_out_rows, void *stream);
+
 /* As hsr_simulate_batch_device, with HOST inputs and outputs: copies poses and budgets
  * in, runs, copies the rows out and synchronises. */
 hsr_status hsr_simulate_batch(hsr_scene *scene, const hsr_rf_config *rf,
