@@ -38,6 +38,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "paths/s"
+# DRAM bytes (read + write) of one trace launch, from the ncu capture summarised in
+# profiles/k_wave_sphere_ground_2p22.md (dram__bytes_read.sum + dram__bytes_write.sum)
+NCU_TRAFFIC = {"sphere": 3.899904e6 + 1.024e3}
 WORKLOAD = "icosphere-L6 (81,920 tris) + 20x20 m ground, sensor 10 m / 0.5 m, 3 bounces, 2^22 samples, N=512"
 
 
@@ -53,6 +56,22 @@ def init_dist(world):
     os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
     dist.init_process_group("gloo")
     return dist
+
+
+def replica_range(rank, samples_per_rank):
+    """Halton index range of one replica: rank r traces [r * S, (r + 1) * S), so the union
+    over ranks is exactly the single-process sample set [0, world * S)."""
+    return rank * samples_per_rank, samples_per_rank
+
+
+def sum_frames(dist, frame):
+    """Host-side sum of the replicas' raw frames (KB-sized; outside any timed region)."""
+    if dist is None:
+        return frame
+    import torch
+    t = torch.from_numpy(frame.astype(np.complex128).view(np.float64).copy())
+    dist.all_reduce(t)
+    return t.numpy().view(np.complex128).reshape(frame.shape)
 
 
 def max_over_ranks(dist, x):
@@ -176,42 +195,83 @@ def run_reference(args, rank, world, dist):
     print(json.dumps(line), flush=True)
 
 
+def load_workload(name, poses=None):
+    """The bench workloads: the sphere+ground scene (the headline) or the boxes batch
+    (4096 poses; --poses takes the first P of them)."""
+    from hussar_gb300 import scenes
+    if name == "boxes":
+        w = scenes.boxes_workload()
+        if poses:
+            w.tx, w.rx, w.budget = w.tx[:poses], w.rx[:poses], w.budget[:poses]
+        desc = ("boxes ~1M tris on 100x100 m ground, %d of 4096 poses at 1 m with random yaw, log-uniform "
+                "budgets 2^16..2^22, 4 bounces, N=256" % len(w.tx))
+        return w, desc
+    return scenes.sphere_ground_workload(samples=1 << 22), WORKLOAD
+
+
+class DeviceBatch:
+    """A workload's poses, budgets and output rows resident on the device."""
+
+    def __init__(self, w, dev, rank, torch, _lib):
+        P = len(w.tx)
+        self.P, self.N = P, w.frame.samplesPerChirp
+        self.paths = int(w.budget.sum())
+
+        def to_dev(arr):
+            return torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+
+        self.h_tx = (_lib.AntennaC * P)(*[a.to_c() for a in w.tx])
+        self.h_rx = (_lib.AntennaC * P)(*[a.to_c() for a in w.rx])
+        self.d_tx, self.d_rx = to_dev(self.h_tx), to_dev(self.h_rx)
+        self.d_budget = torch.from_numpy(w.budget.astype(np.int64)).to(dev)
+        # each rank traces its own Halton range of every pose: replicas, weak scaling
+        off = np.array([replica_range(rank, int(b))[0] for b in w.budget], np.int64)
+        self.d_offset = torch.from_numpy(off).to(dev)
+        self.h_budget = torch.from_numpy(w.budget.astype(np.int64)).pin_memory()
+        self.h_offset = torch.from_numpy(off).pin_memory()
+        self.d_rows = torch.zeros(2 * P * self.N, dtype=torch.float32, device=dev)
+        self.h_rows = torch.zeros(2 * P * self.N, dtype=torch.float32).pin_memory()
+
+
 def run_gb300(args, rank, world, local_rank, dist):
     import ctypes
 
     import torch
 
-    from hussar_gb300 import PathTracer, _lib, gb300, scenes
+    from hussar_gb300 import PathTracer, _lib, gb300
 
     torch.cuda.set_device(local_rank)
     L = _lib.lib()
-    w = scenes.sphere_ground_workload(samples=1 << 22)
-    S = int(w.budget[0])
+    w, desc = load_workload(args.workload, args.poses)
     t = PathTracer()
     t.doGuiding = False
     t.maxDepth = w.max_depth
     be = gb300.Backend(w.mesh, None)
-    N = w.frame.samplesPerChirp
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    txa = w.tx[0].to_c()
-    ant_bytes = bytes(txa)
-    d_tx = torch.frombuffer(bytearray(ant_bytes), dtype=torch.uint8).to(dev)
-    d_rx = d_tx.clone()
-    d_budget = torch.tensor([S], dtype=torch.int64, device=dev)
-    # each rank traces its own Halton range [rank*S, (rank+1)*S): replicas, weak scaling
-    d_offset = torch.tensor([rank * S], dtype=torch.int64, device=dev)
-    d_rows = torch.zeros(2 * N, dtype=torch.float32, device=dev)
+    B = DeviceBatch(w, dev, rank, torch, _lib)
+    N, P = B.N, B.P
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     rf_c = w.rf.to_c()
     fl_c = t.flags_c()
+    vp = ctypes.c_void_p
 
-    def step():
+    def step(splat=_lib.HSR_SPLAT_DIRICHLET16, flags=fl_c):
         _lib.check(L.hsr_simulate_batch_device(
-            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), 1, ctypes.c_void_p(d_tx.data_ptr()),
-            ctypes.c_void_p(d_rx.data_ptr()), ctypes.c_void_p(d_budget.data_ptr()),
-            ctypes.c_void_p(d_offset.data_ptr()), _lib.HSR_PHASE_REFERENCE_FP32, _lib.HSR_SPLAT_DIRICHLET16,
-            ctypes.c_void_p(d_rows.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
+            be.handle, ctypes.byref(rf_c), N, ctypes.byref(flags), P, vp(B.d_tx.data_ptr()), vp(B.d_rx.data_ptr()),
+            vp(B.d_budget.data_ptr()), vp(B.d_offset.data_ptr()), _lib.HSR_PHASE_REFERENCE_FP32, splat,
+            vp(B.d_rows.data_ptr()), vp(stream.cuda_stream)))
+
+    def timed(fn, steps):
+        """Device time per step (CUDA events on the launching stream, L2 flushed between steps)."""
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.fill_(k & 0xff)  # > L2 (129 MB), outside the timed events
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in ev]
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -222,29 +282,17 @@ def run_gb300(args, rank, world, local_rank, dist):
     torch.cuda.synchronize()
     clocks.start()
     launches0 = L.hsr_launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    kernel_ms = []
-    for k in range(args.steps):
-        flush.fill_(k & 0xff)  # > L2 (129 MB), outside the timed events
-        ev[k][0].record(stream)
-        step()
-        ev[k][1].record(stream)
-        if args.kernel_times:
-            kms = ctypes.c_float()
-            _lib.check(L.hsr_last_kernel_ms(be.handle, ctypes.byref(kms)))
-            kernel_ms.append(kms.value)
-    torch.cuda.synchronize()
+    step_ms = timed(step, args.steps)
     launches = L.hsr_launch_count() - launches0
     barrier(dist)
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = max_over_ranks(dist, sum(step_ms) / len(step_ms))
-    value = world * S / (ms / 1000.0)
+    value = world * B.paths / (ms / 1000.0)
 
     if args.kernel_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
-                              "steps": args.steps, "ms_per_step": ms, "kernel_only": True,
+                              "steps": args.steps, "ms_per_step": ms, "kernel_only": True, "workload": desc,
                               "gpu_launches": int(launches), "clocks": clk}), flush=True)
         return
 
@@ -255,50 +303,88 @@ def run_gb300(args, rank, world, local_rank, dist):
     _lib.check(L.hsr_last_kernel_ms(be.handle, ctypes.byref(kms)))
     trace_ms = kms.value
 
-    # e2e through the public host-buffer API: pinned poses in, normalised row out, synchronous
-    P = 1
-    h_tx = (_lib.AntennaC * P)(txa)
-    h_rx = (_lib.AntennaC * P)(txa)
-    h_budget = torch.tensor([S], dtype=torch.int64).pin_memory()
-    h_offset = torch.tensor([rank * S], dtype=torch.int64).pin_memory()
-    h_rows = torch.zeros(2 * N, dtype=torch.float32).pin_memory()
+    # e2e through the public host-buffer API: pinned poses in, normalised rows out, synchronous
     e2e_times = []
     for k in range(args.steps):
         flush.fill_(k & 0xff)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         _lib.check(L.hsr_simulate_batch(
-            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), P, ctypes.cast(h_tx, ctypes.c_void_p),
-            ctypes.cast(h_rx, ctypes.c_void_p), ctypes.c_void_p(h_budget.data_ptr()),
-            ctypes.c_void_p(h_offset.data_ptr()), _lib.HSR_PHASE_REFERENCE_FP32, _lib.HSR_SPLAT_DIRICHLET16,
-            ctypes.c_void_p(h_rows.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
+            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), P, ctypes.cast(B.h_tx, vp),
+            ctypes.cast(B.h_rx, vp), vp(B.h_budget.data_ptr()), vp(B.h_offset.data_ptr()),
+            _lib.HSR_PHASE_REFERENCE_FP32, _lib.HSR_SPLAT_DIRICHLET16, vp(B.h_rows.data_ptr()),
+            vp(stream.cuda_stream)))
         e2e_times.append(time.perf_counter() - t0)
     e2e_ms = max_over_ranks(dist, 1000.0 * sum(e2e_times) / len(e2e_times))
     h2d = 2 * ctypes.sizeof(_lib.AntennaC) * P + 16 * P
     d2h = 8 * N * P
 
+    # the other estimator forms on the same inputs: fine-histogram synthesis and guiding
+    modes = {}
+    for _ in range(2):  # warm-up: builds and caches the twiddle operand for N bins
+        step(_lib.HSR_SPLAT_FINE_SYNTH)
+    torch.cuda.synchronize()
+    fine_ms = timed(lambda: step(_lib.HSR_SPLAT_FINE_SYNTH), max(2, args.steps // 2))
+    fine_ms = max_over_ranks(dist, sum(fine_ms) / len(fine_ms))
+    flush.fill_(2)
+    step(_lib.HSR_SPLAT_FINE_SYNTH)
+    _lib.check(L.hsr_last_kernel_ms(be.handle, ctypes.byref(kms)))
+    fine_trace_ms = kms.value
+    kk = 2 * 4 * 8 * N  # reduction length of the real synthesis GEMM (4 moments, 8 sub-bins)
+    useful = 2.0 * P * (kk // 2) * (2 * N) * 2  # complex [P x 32N] x [32N x N]: 8 P (32N) N real flops
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tc_peak = peaks.get("bf16_tflops", 1900.0)
+    synth_ms = max(fine_ms - fine_trace_ms, 1e-6)
+    modes["fine_synth"] = {"value": world * B.paths / (fine_ms / 1000.0), "unit": "paths/s", "ms_per_step": fine_ms,
+                           "trace_ms": fine_trace_ms, "synthesis_ms": synth_ms,
+                           "synthesis_gemm": {"bound": "tensor", "useful_tflop": useful / 1e12,
+                                              "achieved_tflops": useful / (synth_ms / 1000.0) / 1e12,
+                                              "peak_tflops": tc_peak,
+                                              "note": "step time minus trace-kernel time; split-BF16 products "
+                                                      "(6x) not counted as useful"}}
+    if args.workload == "sphere":
+        gfl = t.flags_c()
+        gfl.doGuiding = 1
+        step(_lib.HSR_SPLAT_DIRICHLET16, gfl)
+        g_ms = timed(lambda: step(_lib.HSR_SPLAT_DIRICHLET16, gfl), 2)
+        g_ms = max_over_ranks(dist, sum(g_ms) / len(g_ms))
+        modes["guided"] = {"value": world * B.paths / (g_ms / 1000.0), "unit": "paths/s", "ms_per_step": g_ms,
+                           "note": "PathTracer::run doubling schedule with device guiding over the same budget"}
+
     if rank != 0:
         return
-    counts = be.traversal_counts(w.rf, N, t, w.tx, w.rx, [S], [0])
+    # exact traversal work of the same launch (counting instantiation); the boxes batch is
+    # counted on a subsample of poses and scaled by paths
+    if P == 1:
+        counts = be.traversal_counts(w.rf, N, t, w.tx, w.rx, w.budget, [0])
+        scale = 1.0
+    else:
+        sub = np.arange(0, P, max(1, P // 64))
+        counts = be.traversal_counts(w.rf, N, t, [w.tx[i] for i in sub], [w.rx[i] for i in sub], w.budget[sub])
+        scale = B.paths / float(w.budget[sub].sum())
+    alg_bytes = counts["bytes"] * scale
     peak, peak_kind = measured_peaks()
-    achieved = counts["bytes"] / (trace_ms / 1000.0) / 1e9
-    cores = os.cpu_count()
+    achieved = alg_bytes / (trace_ms / 1000.0) / 1e9
     cpu_val, cpu_cores, cpu_s = cpu_baseline(w, t, args.cpu_samples)
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "paths_per_step_per_gpu": S, "poses": 1, "max_bounces": 3,
+        "config": {"workload": desc, "paths_per_step_per_gpu": B.paths, "poses": P, "max_bounces": w.max_depth,
                    "range_bins": N, "phase": "reference-fp32", "splat": "dirichlet16",
                    "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas x%d" % world},
-        "e2e": {"value": world * S / (e2e_ms / 1000.0), "unit": "paths/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": world * B.paths / (e2e_ms / 1000.0), "unit": "paths/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "k_trace",
-                     "kernel_ms": trace_ms, "algorithmic_bytes": counts["bytes"], "rays": counts["rays"],
-                     "nodes": counts["nodes"], "tris": counts["tris"], "peak_source": peak_kind},
+                     "frac": achieved / peak,
+                     "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get(args.workload),
+                     "kernel": "k_wave",
+                     "kernel_ms": trace_ms, "algorithmic_bytes": alg_bytes, "rays": counts["rays"] * scale,
+                     "nodes": counts["nodes"] * scale, "tris": counts["tris"] * scale, "peak_source": peak_kind},
         "cpu_baseline": {"value": cpu_val, "unit": "paths/s", "cores": cpu_cores, "kind": "port",
-                         "sample": "%d Halton samples of the same pose (%.1f s wall)" % (args.cpu_samples, cpu_s)},
+                         "sample": "%d Halton samples of pose 0 (%.1f s wall)" % (args.cpu_samples, cpu_s)},
+        "modes": modes,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -313,7 +399,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--kernel-times", action="store_true")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes"])
+    ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
     ap.add_argument("--kernel-only", action="store_true",
                     help="timed steps only (no e2e, counting, CPU baseline): the profiling command")
     args = ap.parse_args()

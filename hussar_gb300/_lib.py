@@ -109,6 +109,7 @@ def lib():
                                        vp, vp],
         "hsr_set_path_kernel": [ctypes.c_int32],
         "hsr_set_synth_engine": [ctypes.c_int32],
+        "hsr_set_bvh_builder": [ctypes.c_int32],
         "hsr_last_kernel_ms": [vp, P(ctypes.c_float)],
     }
     for name, args in sigs.items():

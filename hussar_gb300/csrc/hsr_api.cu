@@ -856,6 +856,12 @@ hsr_status hsr_set_path_kernel(int32_t kind) {
     return HSR_OK;
 }
 
+hsr_status hsr_set_bvh_builder(int32_t builder) {
+    if (builder != 0 && builder != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "builder must be 0 or 1");
+    g_bvh_builder = builder;
+    return HSR_OK;
+}
+
 hsr_status hsr_set_synth_engine(int32_t engine) {
     if (engine != 0 && engine != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "engine must be 0 or 1");
     g_synth_engine = engine;

@@ -1,14 +1,21 @@
-// Device LBVH build: replaces Embree's rtcCommitScene (libhussar/src/arch/cpu.cpp:32-47)
+// Device BVH build: replaces Embree's rtcCommitScene (libhussar/src/arch/cpu.cpp:32-47)
 // and OptiX's optixAccelBuild + compaction (src/arch/gpu.cpp:82-207).
 //
-//   1. per-triangle bounds and centroids, scene centroid bounds (k_bounds, k_centroid_bounds)
+//   1. per-triangle bounds and centroids, scene centroid bounds (k_bounds)
 //   2. 63-bit Morton code of each centroid, 21 bits per axis (k_morton)
 //   3. radix sort of (code, triangle id) pairs (CUB DeviceRadixSort)
 //   4. triangle records written in sorted order (k_write_tris)
-//   5. binary radix tree topology from the sorted codes (Karras 2012, k_karras)
-//   6. bottom-up box refit with one arrival counter per node (k_refit)
-// Leaves hold one triangle; node i stores the boxes of both its children.
+//   5. topology, one of:
+//      PLOC (default): parallel locally-ordered clustering over the Morton order
+//        (Meister and Bittner 2018): every cluster finds, within +-16 positions, the
+//        neighbour whose merged box has the smallest surface area; mutual nearest pairs
+//        merge; survivors are compacted in order; repeat until one cluster is left.
+//        Surface-area-driven like an SAH build, robust to large overlapping triangles.
+//      LBVH: binary radix tree from the sorted codes (Karras 2012, k_karras) and a
+//        bottom-up box refit (k_refit).
+// Leaves hold one triangle; node i stores the boxes of both its children; node 0 is the root.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
 
 #include <limits>
 
@@ -217,9 +224,174 @@ __global__ void k_leaf_depth(int64_t n, const int32_t *__restrict__ parent_inter
     atomicMax(depth_out, depth);
 }
 
+// ---------------- PLOC ----------------
+constexpr int kPlocRadius = 16;
+
+struct Cluster {
+    int id;       // node encoding: >= 0 internal node, < 0 leaf slot (~slot)
+    float b[6];   // lo.xyz, hi.xyz
+};
+
+__global__ void k_ploc_init(int64_t n, const int32_t *__restrict__ sorted_ids, const float *__restrict__ lo,
+                            const float *__restrict__ hi, Cluster *__restrict__ cl) {
+    int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const int64_t t = sorted_ids[i];
+    Cluster c;
+    c.id = ~int(i);
+    for (int a = 0; a < 3; ++a) {
+        c.b[a] = lo[3 * t + a];
+        c.b[3 + a] = hi[3 * t + a];
+    }
+    cl[i] = c;
+}
+
+__device__ __forceinline__ float merged_area(const float *a, const float *b) {
+    const float dx = fmaxf(a[3], b[3]) - fminf(a[0], b[0]);
+    const float dy = fmaxf(a[4], b[4]) - fminf(a[1], b[1]);
+    const float dz = fmaxf(a[5], b[5]) - fminf(a[2], b[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// nearest[i]: the cluster within +-R whose union with i has the smallest surface area
+// (ties: the lower index), read through a shared-memory window.
+__global__ void __launch_bounds__(256) k_ploc_nearest(int n, const Cluster *__restrict__ cl, int *__restrict__ nearest) {
+    __shared__ float sb[256 + 2 * kPlocRadius][6];
+    const int base = blockIdx.x * 256;
+    for (int k = threadIdx.x; k < 256 + 2 * kPlocRadius; k += 256) {
+        const int j = base - kPlocRadius + k;
+        if (j >= 0 && j < n) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a) sb[k][a] = cl[j].b[a];
+        }
+    }
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    if (i >= n) return;
+    const float *bi = sb[threadIdx.x + kPlocRadius];
+    float best = __int_as_float(0x7f800000);
+    int bj = -1;
+    const int j0 = max(0, i - kPlocRadius), j1 = min(n - 1, i + kPlocRadius);
+    for (int j = j0; j <= j1; ++j) {
+        if (j == i) continue;
+        const float a = merged_area(bi, sb[j - base + kPlocRadius]);
+        if (a < best) {
+            best = a;
+            bj = j;
+        }
+    }
+    nearest[i] = bj;
+}
+
+// Mutual nearest pairs merge into a new internal node (allocated from the top so that the
+// last merge, the root, is node 0); the lower index keeps the merged cluster.
+__global__ void k_ploc_merge(int n, const int *__restrict__ nearest, Cluster *cl, char *__restrict__ keep,
+                             DNode *__restrict__ nodes, int *__restrict__ node_counter, int internal_total,
+                             int32_t *__restrict__ parent_internal, int32_t *__restrict__ parent_leaf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int j = nearest[i];
+    if (j < 0 || nearest[j] != i) {
+        keep[i] = 1;
+        return;
+    }
+    if (i > j) {
+        keep[i] = 0;
+        return;
+    }
+    const Cluster a = cl[i], b = cl[j];
+    const int id = internal_total - 1 - atomicAdd(node_counter, 1);
+    DNode nd;
+    nd.a = make_float4(a.b[0], a.b[3], a.b[1], a.b[4]);
+    nd.b = make_float4(b.b[0], b.b[3], b.b[1], b.b[4]);
+    nd.c = make_float4(a.b[2], a.b[5], b.b[2], b.b[5]);
+    nd.d = make_int4(a.id, b.id, 0, 0);
+    nodes[id] = nd;
+    if (a.id >= 0) parent_internal[a.id] = id; else parent_leaf[~a.id] = id;
+    if (b.id >= 0) parent_internal[b.id] = id; else parent_leaf[~b.id] = id;
+    Cluster m;
+    m.id = id;
+    for (int k = 0; k < 3; ++k) {
+        m.b[k] = fminf(a.b[k], b.b[k]);
+        m.b[3 + k] = fmaxf(a.b[3 + k], b.b[3 + k]);
+    }
+    cl[i] = m;
+    keep[i] = 1;
+}
+
 inline unsigned blocks_for(int64_t n, int t) { return unsigned((n + t - 1) / t); }
 
 }  // namespace
+
+int g_bvh_builder = 0;  // 0: PLOC, 1: LBVH (Karras)
+
+// PLOC topology over the sorted leaves. Returns 0 or an hsr_status-like code.
+static int build_ploc(SceneDev &s, int64_t nt, const int32_t *ids2, const float *lo, const float *hi,
+                      int32_t *par_i, int32_t *par_l, int *depth, cudaStream_t st, std::string &err) {
+    const int n0 = int(nt);
+    Cluster *c0 = nullptr, *c1 = nullptr;
+    int *nearest = nullptr, *counter = nullptr, *num_sel = nullptr;
+    char *keep = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    int rc = 0;
+    do {
+        if (!dev_alloc(&c0, sizeof(Cluster) * n0, err) || !dev_alloc(&c1, sizeof(Cluster) * n0, err) ||
+            !dev_alloc(&nearest, sizeof(int) * n0, err) || !dev_alloc(&counter, sizeof(int) * 2, err) ||
+            !dev_alloc(&num_sel, sizeof(int) * 2, err) || !dev_alloc(&keep, size_t(n0), err)) {
+            rc = 3;
+            break;
+        }
+        cub::DeviceSelect::Flagged(nullptr, tmp_bytes, c0, keep, c1, num_sel, n0, st);
+        if (!dev_alloc(&tmp, tmp_bytes, err)) {
+            rc = 3;
+            break;
+        }
+        cudaMemsetAsync(counter, 0, sizeof(int), st);
+        k_ploc_init<<<blocks_for(nt, 256), 256, 0, st>>>(nt, ids2, lo, hi, c0);
+        note_launches(1);
+        int n = n0;
+        int iterations = 0;
+        while (n > 1 && iterations < 100000) {
+            k_ploc_nearest<<<blocks_for(n, 256), 256, 0, st>>>(n, c0, nearest);
+            k_ploc_merge<<<blocks_for(n, 256), 256, 0, st>>>(n, nearest, c0, keep, s.nodes, counter, n0 - 1, par_i,
+                                                             par_l);
+            if (cub::DeviceSelect::Flagged(tmp, tmp_bytes, c0, keep, c1, num_sel, n, st) != cudaSuccess) {
+                err = "PLOC compaction failed";
+                rc = 2;
+                break;
+            }
+            note_launches(3);
+            int h = 0;
+            if (cudaMemcpyAsync(&h, num_sel, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                err = "PLOC iteration failed";
+                rc = 2;
+                break;
+            }
+            if (h >= n) {  // no pair merged: impossible for a correct nearest search; stop safely
+                err = "PLOC made no progress";
+                rc = 2;
+                break;
+            }
+            std::swap(c0, c1);
+            n = h;
+            ++iterations;
+        }
+        if (rc) break;
+        k_leaf_depth<<<blocks_for(nt, 256), 256, 0, st>>>(nt, par_i, par_l, depth + 1);
+        note_launches(1);
+    } while (false);
+    cudaStreamSynchronize(st);
+    cudaFree(c0);
+    cudaFree(c1);
+    cudaFree(nearest);
+    cudaFree(counter);
+    cudaFree(num_sel);
+    cudaFree(keep);
+    cudaFree(tmp);
+    return rc;
+}
 
 // Builds tris/nodes for `scene` from device vertex/index arrays. Returns 0 or an hsr_status.
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
@@ -323,10 +495,19 @@ int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, i
             break;
         }
         k_write_tris<<<blocks_for(nt, T), T, 0, st>>>(d_v, d_idx, ids2, nt, s.tris);
-        k_karras<<<blocks_for(nt - 1, T), T, 0, st>>>(keys2, nt, s.nodes, par_i, par_l);
-        k_refit<<<blocks_for(nt, T), T, 0, st>>>(nt, ids2, lo, hi, s.nodes, par_i, par_l, counters, depth);
-        k_leaf_depth<<<blocks_for(nt, T), T, 0, st>>>(nt, par_i, par_l, depth + 1);
-        note_launches(4);
+        if (g_bvh_builder == 0) {
+            note_launches(1);
+            const int prc = build_ploc(s, nt, ids2, lo, hi, par_i, par_l, depth, st, err);
+            if (prc) {
+                fail(prc);
+                break;
+            }
+        } else {
+            k_karras<<<blocks_for(nt - 1, T), T, 0, st>>>(keys2, nt, s.nodes, par_i, par_l);
+            k_refit<<<blocks_for(nt, T), T, 0, st>>>(nt, ids2, lo, hi, s.nodes, par_i, par_l, counters, depth);
+            k_leaf_depth<<<blocks_for(nt, T), T, 0, st>>>(nt, par_i, par_l, depth + 1);
+            note_launches(4);
+        }
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             err = std::string("BVH build: ") + cudaGetErrorString(e);

@@ -137,6 +137,8 @@ int wave_blocks_per_sm(int samples);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel
 extern int g_path_kernel;
+// BVH topology of new scenes: 0 = PLOC (default), 1 = LBVH (Karras radix tree)
+extern int g_bvh_builder;
 int trace_blocks_per_sm(int samples, int splat_mode, int fine_bins);
 
 }  // namespace hsr

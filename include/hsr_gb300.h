@@ -262,6 +262,11 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
  * Both compute the same per-path values; tests use this to check each one. */
 hsr_status hsr_set_path_kernel(int32_t kind);
 
+/* BVH topology for scenes created afterwards (process-wide): 0 (default) = PLOC
+ * clustering over the Morton order (surface-area driven), 1 = LBVH radix tree. Both
+ * give bit-identical ray-query results; only the traversal cost differs. */
+hsr_status hsr_set_bvh_builder(int32_t builder);
+
 /* Engine of the fine-histogram synthesis GEMM (process-wide): 0 (default) = tensor cores
  * (tcgen05.mma, operands split into three BF16 terms, FP32 accumulation), 1 = CUDA cores
  * in FP32. Both compute the same product; tests use this to check one against the other. */
