@@ -18,6 +18,12 @@ samples — traced by one persistent launch of the plain FP32 path with the refe
   cpu_baseline  the oracle's FP32 restatement with its own BVH, on all host cores, on a
          bounded sample of the same workload.
 
+--workload serve: the serving loop (hsr_server_*): 8 resident scenes of 100 k .. 5 M
+triangles (boxes and urban-canyon generators), a Poisson request stream (--rate req/s
+for --duration s) with random scene, pose, log-uniform budget 2^16..2^24, chirp bandwidth
+1..4 GHz and N in {128, 256, 512}; reports p50/p99 latency (submit -> row on the host)
+and wall-clock paths/s through the public API.
+
 --impl reference times the CPU restatement of the reference path (the reference itself
 needs Embree/OptiX/Eigen, absent here) on the host cores with the same metric.
 Multi-GPU: replicas (each rank traces its own disjoint Halton range of the same pose;
@@ -391,6 +397,104 @@ def run_gb300(args, rank, world, local_rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args, rank, world, local_rank, dist):
+    """The serving workload (see the module docstring); replicas under torchrun: every rank
+    serves its own request stream."""
+    import torch
+
+    from hussar_gb300 import HSR_PHASE_SPLIT_FP64, PathTracer, Server, gb300, scenes
+
+    torch.cuda.set_device(local_rank)
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = 4
+    t0 = time.perf_counter()
+    backends, posegens, tris = [], [], 0
+    for i, (kind, n) in enumerate(scenes.SERVE_SCENES):
+        mesh, pg = scenes.serve_scene(kind, n, 0xC5 + i)
+        tris += mesh.triangleCount()
+        backends.append(gb300.Backend(mesh, None))
+        posegens.append(pg)
+        del mesh
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(0xC5 + 101 * rank)
+    n_req = max(1, int(round(args.rate * args.duration)))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    sid = rng.integers(0, len(backends), n_req)
+    budget = np.round(2.0 ** rng.uniform(16, 24, n_req)).astype(np.int64)
+    bw = rng.uniform(1e9, 4e9, n_req)
+    nbins = rng.choice([128, 256, 512], n_req)
+    poses = [posegens[int(s)](1, 1000 + k)[0] for k, s in enumerate(sid)]
+    srv = Server(flags=t, phase_mode=HSR_PHASE_SPLIT_FP64, max_slots=args.slots, max_samples_per_chirp=512,
+                 tick_ms=args.tick_ms)
+    ids = [srv.add_scene(be) for be in backends]
+
+    def submit(k, offset=0, scale=1):
+        rf = scenes.rf_chirp(bandwidth=float(bw[k]), samples=int(nbins[k]))
+        return srv.submit(ids[int(sid[k])], rf, int(nbins[k]), poses[k], poses[k], max(1, int(budget[k]) // scale),
+                          offset)
+
+    # warm-up: every scene once at a small budget (kernel attributes, allocator, clocks)
+    warm = [submit(int(np.nonzero(sid == s)[0][0]) if (sid == s).any() else 0, 1 << 30, 64)
+            for s in range(len(backends))]
+    for _ in range(max(args.warmup, 3) - 1):
+        warm += [submit(k, 1 << 31, 64) for k in range(min(4, n_req))]
+    for h in warm:
+        h.result()
+    srv.reset_stats()
+    clocks = ClockSampler(local_rank)
+    barrier(dist)
+    clocks.start()
+    start = time.perf_counter()
+    handles = []
+    for k in range(n_req):
+        delay = start + arrivals[k] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        handles.append(submit(k))
+    infos = [h.result()[1] for h in handles]
+    wall = time.perf_counter() - start
+    barrier(dist)
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([i["latency_ms"] for i in infos])
+    que = np.array([i["queue_ms"] for i in infos])
+    paths = int(budget.sum())
+    wall_max = max_over_ranks(dist, wall)
+    value = world * paths / wall_max  # replicas: every rank served a stream of the same law
+    offered = paths / float(arrivals[-1]) if n_req > 1 else float("nan")
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": 1,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1000.0 * wall_max, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serving: %d resident scenes (%s), %.0f req/s Poisson for %.1f s, budgets "
+                               "2^16..2^24 log-uniform, bandwidth 1..4 GHz, N in {128,256,512}, 4 bounces, "
+                               "split FP64 phase" % (len(backends), ", ".join("%s-%dk" % (k, n // 1000) for k, n in
+                                                                               scenes.SERVE_SCENES),
+                                                     args.rate, args.duration),
+                   "requests": n_req, "triangles": tris, "scene_bytes": st["scene_bytes"],
+                   "max_slots": args.slots, "tick_ms": args.tick_ms, "setup_s": setup_s,
+                   "l2": "inputs larger than L2 (%.2f GB of resident scenes)" % (st["scene_bytes"] / 1e9)},
+        "serving": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "max_ms": float(lat.max()), "queue_p50_ms": float(np.percentile(que, 50)),
+                    "queue_p99_ms": float(np.percentile(que, 99)), "offered_paths_per_s": offered,
+                    "device_paths_per_s": st["samples"] / (st["device_ms"] / 1000.0) if st["device_ms"] else None,
+                    "device_busy_frac": st["device_ms"] / (1000.0 * wall), "ticks": st["ticks"],
+                    "max_batch": st["max_batch"], "max_resident": st["max_resident"],
+                    "admitted_while_busy": st["admitted_while_busy"], "failed": st["failed"]},
+        "e2e": {"value": value, "unit": "paths/s",
+                "h2d_bytes_per_step": int(n_req * 152), "d2h_bytes_per_step": int(8 * nbins.sum()),
+                "note": "wall clock from the first arrival to the last row on the host, through hsr_server_*"},
+        "gpu_launches": int(st["ticks"]),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,17 +503,23 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
     ap.add_argument("--kernel-only", action="store_true",
                     help="timed steps only (no e2e, counting, CPU baseline): the profiling command")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (req/s)")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
+    ap.add_argument("--slots", type=int, default=256, help="serve: requests admitted at once")
+    ap.add_argument("--tick-ms", type=float, default=4.0, help="serve: target device time per tick")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     dist = init_dist(world)
     if args.impl == "reference":
         run_reference(args, rank, world, dist)
+    elif args.workload == "serve":
+        run_serve(args, rank, world, local_rank, dist)
     else:
         run_gb300(args, rank, world, local_rank, dist)
     if dist is not None:

@@ -17,6 +17,7 @@ HSR_ERR_INTERRUPTED = 4
 HSR_ERR_DEVICE = 5
 HSR_ERR_NOT_SUPPORTED = 6
 HSR_ERR_NO_DEVICE = 7
+HSR_ERR_TIMEOUT = 8
 
 HSR_PHASE_REFERENCE_FP32 = 0
 HSR_PHASE_SPLIT_FP64 = 1
@@ -26,6 +27,7 @@ HSR_SPLAT_FINE_SYNTH = 1
 STATUS_NAMES = {
     0: "HSR_OK", 1: "HSR_ERR_INVALID_ARGUMENT", 2: "HSR_ERR_CUDA", 3: "HSR_ERR_OUT_OF_MEMORY",
     4: "HSR_ERR_INTERRUPTED", 5: "HSR_ERR_DEVICE", 6: "HSR_ERR_NOT_SUPPORTED", 7: "HSR_ERR_NO_DEVICE",
+    8: "HSR_ERR_TIMEOUT",
 }
 
 
@@ -62,6 +64,30 @@ class FlagsC(ctypes.Structure):
               [(n, ctypes.c_float) for n in ("filteringMin", "filteringMax", "filteringRadius")]
 
 
+class ServerConfigC(ctypes.Structure):
+    _fields_ = [("max_slots", ctypes.c_int32), ("max_samples_per_chirp", ctypes.c_int32),
+                ("memory_bytes", ctypes.c_int64), ("tick_ms", ctypes.c_float), ("phase_mode", ctypes.c_int32),
+                ("flags", FlagsC)]
+
+
+class RequestC(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_int32), ("samples_per_chirp", ctypes.c_int32), ("rf", RFConfigC),
+                ("tx", AntennaC), ("rx", AntennaC), ("budget", ctypes.c_int64), ("index_offset", ctypes.c_int64),
+                ("out_row", ctypes.c_void_p)]
+
+
+class RequestResultC(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("ticks", ctypes.c_int32), ("queue_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double)]
+
+
+class ServerStatsC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "ticks", "samples")] + \
+               [(n, ctypes.c_double) for n in ("device_ms", "p50_ms", "p99_ms", "max_ms")] + \
+               [("max_batch", ctypes.c_int32), ("max_resident", ctypes.c_int32)] + \
+               [(n, ctypes.c_int64) for n in ("admitted_while_busy", "memory_bytes_peak", "scene_bytes")]
+
+
 # PathRecord in hsr_trace.cu / hsr_debug_records
 RECORD_DTYPE = [("depth", "<i4"), ("splatted", "<i4"), ("time", "<f4"), ("v_re", "<f4"), ("v_im", "<f4"),
                 ("dphase", "<f4"), ("bin", "<f4"), ("value_re", "<f4"), ("value_im", "<f4")]
@@ -85,6 +111,8 @@ def lib():
     L.hsr_launch_count.restype = ctypes.c_int64
     L.hsr_default_flags.argtypes = [P(FlagsC)]
     L.hsr_default_flags.restype = None
+    L.hsr_default_server_config.argtypes = [P(ServerConfigC)]
+    L.hsr_default_server_config.restype = None
     sigs = {
         "hsr_scene_create": [vp, ctypes.c_int64, vp, ctypes.c_int64, P(vp)],
         "hsr_scene_destroy": [vp],
@@ -111,6 +139,14 @@ def lib():
         "hsr_set_synth_engine": [ctypes.c_int32],
         "hsr_set_bvh_builder": [ctypes.c_int32],
         "hsr_last_kernel_ms": [vp, P(ctypes.c_float)],
+        "hsr_server_create": [P(ServerConfigC), P(vp)],
+        "hsr_server_add_scene": [vp, vp, P(ctypes.c_int32)],
+        "hsr_server_submit": [vp, P(RequestC), P(ctypes.c_uint64)],
+        "hsr_server_wait": [vp, ctypes.c_uint64, ctypes.c_int32, P(RequestResultC)],
+        "hsr_server_get_stats": [vp, P(ServerStatsC)],
+        "hsr_server_reset_stats": [vp],
+        "hsr_server_destroy": [vp],
+        "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)

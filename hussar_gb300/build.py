@@ -25,6 +25,7 @@ UNITS = {
     "hsr_guide.cu": [],
     "hsr_synth.cu": [],
     "hsr_noalloc.cu": [],
+    "hsr_serve.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
 }

@@ -250,7 +250,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
         p.flags.doGuiding = 0;
     }
     const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
-    int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N) : trace_blocks_per_sm(N, splat_mode, 0));
+    int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0));
     cudaEventRecord(sc.ev0, st);
     std::string err;
     if (wave) {

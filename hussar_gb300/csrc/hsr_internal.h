@@ -69,7 +69,19 @@ void set_last_error(const std::string &msg);
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
               std::string &err);
 
-// Launch parameters of the trace kernel (POD, passed by value).
+// Per-pose scene, chirp and accumulator row of a mixed batch (the serving loop): poses
+// of one launch may trace different resident scenes with different RF configurations
+// and range-bin counts. The tracer flags and the phase mode stay uniform.
+struct PoseJob {
+    const DNode *nodes;
+    const DTri *tris;
+    hsr_rf_config rf;
+    int32_t samples;     // N of this pose (<= TraceParams::samples, which sizes the CTA row)
+    int32_t reserved;
+    int64_t acc_offset;  // first double of the pose's 2N accumulators in TraceParams::acc
+};
+
+// Launch parameters of the trace kernels (POD, passed by value).
 struct TraceParams {
     const DNode *nodes;
     const DTri *tris;
@@ -104,6 +116,9 @@ struct TraceParams {
     // [Re h0 .. Re h3 | Im h0 .. Im h3], K = 8 N; nullptr: Dirichlet splat
     int32_t fine_bins;      // K
     float *fine;
+    // mixed batch: per-pose scene/chirp/row (nodes, tris, rf and acc rows above are then
+    // unused; samples is the largest N); nullptr: uniform batch. Wavefront kernel only.
+    const PoseJob *jobs;
 };
 
 size_t guide_bytes_per_pose();
@@ -133,7 +148,7 @@ int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, cons
                        cudaStream_t st);
 int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
 size_t wave_smem_bytes(int samples);
-int wave_blocks_per_sm(int samples);
+int wave_blocks_per_sm(int samples, bool mixed);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel
 extern int g_path_kernel;

@@ -146,7 +146,7 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
     p.work_counter = s->counters + 2;
     std::string err;
     const bool wave = flags->useGeometricalOptics != 0;
-    const int grid = sc->sm_count * (wave ? wave_blocks_per_sm(N) : trace_blocks_per_sm(N, HSR_SPLAT_DIRICHLET16, 0));
+    const int grid = sc->sm_count * (wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, HSR_SPLAT_DIRICHLET16, 0));
     const int rc = wave ? launch_wave(p, phase_mode, grid, strm, err)
                         : launch_trace(p, phase_mode, HSR_SPLAT_DIRICHLET16, grid, strm, err);
     if (rc != 0) {

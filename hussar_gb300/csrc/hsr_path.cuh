@@ -161,12 +161,14 @@ struct NeeOut {
 
 // Returns false when the estimate is occluded or skipped (no record, no splat).
 // depth == 0: direct TX->RX connection (only with onlyIndirect = false).
+// `nodes`/`tris` are the scene the pose traces, `rf`/`samples` its chirp and range bins
+// (uniform over a launch, or the pose's PoseJob in a mixed batch).
 template <int kPhase, bool kCount>
-__device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, const Ant &rx, int depth, f3 o, f3 d,
-                                         f3 tmpd, f3 hit_n, const c3 &inc_H, const c3 &H, float time, double plen,
-                                         float r, float cosTheta, float freq, float sampleWeight, NeeOut &out,
-                                         TraversalCounters *cnt, unsigned *rays) {
-    const hsr_rf_config &rf = p.rf;
+__device__ __forceinline__ bool nee_eval(const TraceParams &p, const DNode *nodes, const DTri *tris,
+                                         const hsr_rf_config &rf, int samples, const Ant &tx, const Ant &rx, int depth,
+                                         f3 o, f3 d, f3 tmpd, f3 hit_n, const c3 &inc_H, const c3 &H, float time,
+                                         double plen, float r, float cosTheta, float freq, float sampleWeight,
+                                         NeeOut &out, TraversalCounters *cnt, unsigned *rays) {
     const hsr_tracer_flags &fl = p.flags;
     // NFAntenna::nee (emitter.h:195-203)
     f3 nd = sub3(rx.pos, o);
@@ -176,7 +178,7 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
     c3 Hrx = mulcv(rx.rot, awr_eval(mulTv(rx.rot, neg3(nd))));
     if (!fl.poDiffraction) {
         if (kCount) (*rays)++;
-        if (any_hit<kCount>(p.nodes, p.tris, o, nd, kEpsilon, tMax, p.status, cnt)) return false;
+        if (any_hit<kCount>(nodes, tris, o, nd, kEpsilon, tMax, p.status, cnt)) return false;
     }
     const float nt = tMax;
     f3 no = o;
@@ -272,7 +274,7 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
             sample = 0.f;
         } else {
             float x = dt * rf.freqSlope / rf.adcRate;  // PIndex::setTime (radar.h:232-241)
-            sample = float(p.samples) * (x - floorf(x));
+            sample = float(samples) * (x - floorf(x));
         }
         // Integrator::measureRay (integrator.h:107-110)
         float angle = 2.f * kPi * (rf.startFreq - dt * rf.freqSlope / 2.f) * dt;
@@ -286,7 +288,7 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const Ant &tx, co
             sample = 0.f;
         } else {
             double x = dt * double(rf.freqSlope) / double(rf.adcRate);
-            sample = float(double(p.samples) * (x - floor(x)));
+            sample = float(double(samples) * (x - floor(x)));
         }
         double cyc = (double(rf.startFreq) - dt * double(rf.freqSlope) * 0.5) * dt;
         float frac = float(cyc - floor(cyc));

@@ -75,8 +75,8 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
         // next event estimation towards the single RX antenna (path.h:292-397)
         if (!(depth == 0 && fl.onlyIndirect)) {
             NeeOut ne;
-            if (nee_eval<kPhase, kCount>(p, tx, rx, depth, o, d, tmpd, hit_n, inc_H, H, time, plen, r, cosTheta,
-                                         freq, pc.weight, ne, cnt, rays)) {
+            if (nee_eval<kPhase, kCount>(p, p.nodes, p.tris, p.rf, p.samples, tx, rx, depth, o, d, tmpd, hit_n,
+                                         inc_H, H, time, plen, r, cosTheta, freq, pc.weight, ne, cnt, rays)) {
                 gw = cadd(gw, ne.gw_add);
                 if (kRecord && nrec < max_rec) {
                     PathRecord *rc = rec + nrec++;

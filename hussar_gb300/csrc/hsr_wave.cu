@@ -14,6 +14,11 @@
 // shared-memory addresses updated in one pass. The CTA's range row lives in shared
 // memory and is flushed to the pose's FP64 accumulators when the CTA changes pose.
 // Work items are (pose, 4096-sample tile) pairs pulled from a device counter.
+//
+// Mixed batches (kMixed, the serving loop): each pose names its own resident scene,
+// chirp, range-bin count and accumulator row (PoseJob). A CTA works on one pose at a
+// time, so these are CTA-uniform: thread 0 copies the pose's job into shared memory
+// when the CTA switches pose, and the arithmetic is the uniform kernel's.
 #include "hsr_path.cuh"
 
 namespace hsr {
@@ -35,6 +40,8 @@ struct WaveShared {
     int count;
     int pose, pending_pose, exhausted;
     long long gen, gen_end, pending_first, pending_last;
+    PoseJob job;                // mixed batches: the current pose's scene, chirp and row
+    float max_dist, bandwidth;  // mixed batches: derived from job.rf
 };
 
 struct Guided {  // the guiding part of a path's state
@@ -74,13 +81,13 @@ __device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H
 
 // Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
 // Returns true (and the new state) when the path continues with a stored hit.
-__device__ __forceinline__ bool walk(const TraceParams &p, f3 o, f3 d, const c3 &H, float &time, float &r,
-                                     double &plen, f3 &hp, f3 &n, float &cosT) {
+__device__ __forceinline__ bool walk(const TraceParams &p, const DNode *nodes, const DTri *tris, f3 o, f3 d,
+                                     const c3 &H, float &time, float &r, double &plen, f3 &hp, f3 &n, float &cosT) {
     float th;
     int primh;
-    const int slot = closest_hit<false>(p.nodes, p.tris, o, d, kEpsilon, CUDART_INF_F, th, primh, p.status, nullptr);
+    const int slot = closest_hit<false>(nodes, tris, o, d, kEpsilon, CUDART_INF_F, th, primh, p.status, nullptr);
     if (slot < 0) return false;
-    DTri T = load_tri(p.tris, slot);
+    DTri T = load_tri(tris, slot);
     n = hit_normal(T, d);
     hp = add3(o, scl3(th, d));
     cosT = fabsf(dot3(n, neg3(d)));
@@ -92,17 +99,34 @@ __device__ __forceinline__ bool walk(const TraceParams &p, f3 o, f3 d, const c3 
     return true;
 }
 
-template <int kPhase>
+// PathTracer::run's derived chirp quantities (path.h:240, radar.h:128-130).
+__device__ __forceinline__ float max_distance(const hsr_rf_config &rf) {
+    return rf.adcRate / rf.freqSlope * kSpeedOfLight;
+}
+__device__ __forceinline__ float chirp_bandwidth(const hsr_rf_config &rf) { return rf.freqSlope * rf.rampTime; }
+
+// FP64 accumulator row of a pose: pose-major rows of N, or the pose's job row.
+template <bool kMixed>
+__device__ __forceinline__ double *pose_row(const TraceParams &p, const WaveShared &S, int pose) {
+    return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
+}
+
+template <int kPhase, bool kMixed>
 __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
     float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
-    float *s_im = s_re + p.samples;
+    float *s_im = s_re + p.samples;  // the row is sized for the largest N of the launch
     const int tid = threadIdx.x;
-    const hsr_rf_config &rf = p.rf;
     const hsr_tracer_flags &fl = p.flags;
-    const float maxDist = rf.adcRate / rf.freqSlope * kSpeedOfLight;
-    const float bandwidth = rf.freqSlope * rf.rampTime;
+    // the scene, chirp and row of the current pose: launch-uniform, or the pose's job
+    const hsr_rf_config &rf = kMixed ? S.job.rf : p.rf;
+    const float maxDist0 = max_distance(p.rf), bandwidth0 = chirp_bandwidth(p.rf);
+#define HSR_NODES (kMixed ? S.job.nodes : p.nodes)
+#define HSR_TRIS (kMixed ? S.job.tris : p.tris)
+#define HSR_N (kMixed ? S.job.samples : p.samples)
+#define HSR_MAXDIST (kMixed ? S.max_dist : maxDist0)
+#define HSR_BANDWIDTH (kMixed ? S.bandwidth : bandwidth0)
     const long long total = __ldg(&p.tile_start[p.pose_count]);
 
     for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
@@ -155,7 +179,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
             SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
             if (s < gen_end) {
                 const uint64_t hindex = uint64_t(pc.offset + s);
-                const float freq = rf.startFreq + halton(hindex, 0) * bandwidth;
+                const float freq = rf.startFreq + halton(hindex, 0) * HSR_BANDWIDTH;
                 Guided g{halton(hindex, 1), halton(hindex, 2), 1.f, cf{0.f, 0.f}};
                 if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
                 f3 o = pc.tx.pos, d;
@@ -164,8 +188,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                 H = c3_scl(H, 1.f / g.pdf);
                 if (!fl.onlyIndirect) {
                     NeeOut ne;
-                    if (nee_eval<kPhase, false>(p, pc.tx, pc.rx, 0, o, d, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H,
-                                                H, 0.f, 0.0, 0.f, 1.f, freq, pc.weight, ne, nullptr, nullptr) &&
+                    if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, 0, o, d,
+                                                mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H, 0.f, 0.0, 0.f, 1.f,
+                                                freq, pc.weight, ne, nullptr, nullptr) &&
                         ne.splat) {
                         if (pc.fine_row) {
                             splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
@@ -176,18 +201,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                     }
                 }
                 bool alive = false;
-                if (!(0 >= fl.maxDepth || 0.f >= maxDist) && !c3_is_zero(H)) {
+                if (!(0 >= fl.maxDepth || 0.f >= HSR_MAXDIST) && !c3_is_zero(H)) {
                     float time = 0.f, r = 0.f, cosT;
                     double plen = 0.0;
                     f3 hp, n;
-                    if (walk(p, o, d, H, time, r, plen, hp, n, cosT)) {
+                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n, cosT)) {
                         push_path(S, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
                         alive = true;
                     }
                 }
                 if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
             }
-            if (!fl.onlyIndirect) splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
+            if (!fl.onlyIndirect) splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
             continue;
         }
@@ -227,8 +252,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                 c3 H = Hin;
                 reflect(nrm, d, H);
                 NeeOut ne;
-                if (nee_eval<kPhase, false>(p, pc.tx, pc.rx, depth, o, d, din, nrm, Hin, H, time, plen, r, cosT, freq,
-                                            pc.weight, ne, nullptr, nullptr)) {
+                if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, depth, o, d, din, nrm,
+                                            Hin, H, time, plen, r, cosT, freq, pc.weight, ne, nullptr, nullptr)) {
                     g.gw = cadd(g.gw, ne.gw_add);
                     if (ne.splat) {
                         if (pc.fine_row) {
@@ -240,28 +265,33 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                     }
                 }
                 bool alive = false;
-                if (!(depth >= fl.maxDepth || r >= maxDist) && !c3_is_zero(H)) {
+                if (!(depth >= fl.maxDepth || r >= HSR_MAXDIST) && !c3_is_zero(H)) {
                     f3 hp, n2;
                     float cosT2;
-                    if (walk(p, o, d, H, time, r, plen, hp, n2, cosT2)) {
+                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n2, cosT2)) {
                         push_path(S, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
                         alive = true;
                     }
                 }
                 if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
             }
-            splat_warp(s_re, s_im, p.samples, __ballot_sync(0xffffffffu, has_item), item);
+            splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
             continue;
         }
 
         if (pending >= 0) {
             // stack drained: finish the old pose's row and switch to the new pose
-            if (cur_pose >= 0) flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
+            if (cur_pose >= 0) flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
             cur_pose = pending;
             pc = load_pose(p, cur_pose);
-            __syncthreads();
+            __syncthreads();  // every thread is done with the old pose's job
             if (tid == 0) {
+                if (kMixed) {
+                    S.job = p.jobs[pending];
+                    S.max_dist = max_distance(S.job.rf);
+                    S.bandwidth = chirp_bandwidth(S.job.rf);
+                }
                 S.pose = pending;
                 S.gen = S.pending_first;
                 S.gen_end = S.pending_last;
@@ -274,30 +304,54 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
     }
     if (cur_pose >= 0) {
         __syncthreads();
-        flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
+        flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
     }
+#undef HSR_NODES
+#undef HSR_TRIS
+#undef HSR_N
+#undef HSR_MAXDIST
+#undef HSR_BANDWIDTH
 }
 
 }  // namespace
 
 size_t wave_smem_bytes(int samples) { return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float); }
 
-int wave_blocks_per_sm(int samples) {
+template <int kPhase, bool kMixed>
+void wave_instance(const TraceParams &p, int grid, size_t smem, cudaStream_t st) {
+    cudaFuncSetAttribute(k_wave<kPhase, kMixed>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k_wave<kPhase, kMixed><<<grid, kThreads, smem, st>>>(p);
+}
+
+int wave_blocks_per_sm(int samples, bool mixed) {
     int nb = 0;
     const size_t smem = wave_smem_bytes(samples);
-    cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_wave<HSR_PHASE_REFERENCE_FP32>, kThreads, smem);
+    if (mixed) {
+        cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_wave<HSR_PHASE_REFERENCE_FP32, true>, kThreads, smem);
+    } else {
+        cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_wave<HSR_PHASE_REFERENCE_FP32, false>, kThreads, smem);
+    }
     return nb > 0 ? nb : 1;
 }
 
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err) {
     const size_t smem = wave_smem_bytes(p.samples);
-    cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    cudaFuncSetAttribute(k_wave<HSR_PHASE_SPLIT_FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (phase_mode == HSR_PHASE_SPLIT_FP64)
-        k_wave<HSR_PHASE_SPLIT_FP64><<<grid, kThreads, smem, st>>>(p);
-    else
-        k_wave<HSR_PHASE_REFERENCE_FP32><<<grid, kThreads, smem, st>>>(p);
+    const bool split = phase_mode == HSR_PHASE_SPLIT_FP64;
+    if (p.jobs) {
+        if (split)
+            wave_instance<HSR_PHASE_SPLIT_FP64, true>(p, grid, smem, st);
+        else
+            wave_instance<HSR_PHASE_REFERENCE_FP32, true>(p, grid, smem, st);
+    } else {
+        if (split)
+            wave_instance<HSR_PHASE_SPLIT_FP64, false>(p, grid, smem, st);
+        else
+            wave_instance<HSR_PHASE_REFERENCE_FP32, false>(p, grid, smem, st);
+    }
     note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -42,6 +42,13 @@ def rf_77ghz(samples=256, adc_rate=5e6):
     return rf, FrameConfig(1, samples, 1)
 
 
+def rf_chirp(bandwidth=4e9, samples=256, ramp=51.2e-6, start=77e9):
+    """A chirp from `start` over `bandwidth` in `ramp` seconds, sampled `samples` times
+    during the ramp (adcRate = samples / ramp), with rf_77ghz's delay and idle time."""
+    return RFConfig(startFreq=start, freqSlope=bandwidth / ramp, adcRate=samples / ramp, idleTime=100e-6,
+                    rampTime=ramp, antennaDelay=0.43e-9)
+
+
 @dataclasses.dataclass
 class Workload:
     name: str
@@ -156,3 +163,106 @@ def boxes_workload(poses=4096, seed=0xC3, count=83334, min_log2=16, max_log2=22)
         tx.append(NFAntenna(np.array([x, 1.0, z], np.float32), looking(yaw)))
     budget = np.round(2.0 ** rng.uniform(min_log2, max_log2, poses)).astype(np.int64)
     return Workload("boxes-1Mtri-%dposes" % poses, mesh, rf, fc, tx, list(tx), budget, 4)
+
+
+def _grid_quads(origin, u, v, nu, nv):
+    """A parallelogram origin + [0,1]u + [0,1]v split into nu x nv quads (2 triangles
+    each, addQuad's vertex order per cell). Returns (vertices, triangles)."""
+    a = np.arange(nu + 1, dtype=np.float64) / nu
+    b = np.arange(nv + 1, dtype=np.float64) / nv
+    grid = origin[None, None, :] + a[:, None, None] * u[None, None, :] + b[None, :, None] * v[None, None, :]
+    verts = grid.reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    p00 = (i * (nv + 1) + j).reshape(-1)
+    p10 = p00 + (nv + 1)
+    p11 = p10 + 1
+    p01 = p00 + 1
+    tri = np.concatenate([np.stack([p00, p10, p11], 1), np.stack([p00, p11, p01], 1)], 1).reshape(-1, 3)
+    return verts, tri
+
+
+def urban_mesh(target_tris=5_000_000, seed=0xC4, blocks=14, pitch=42.0, street=12.0, cars=200):
+    """Synthetic urban canyon: a blocks x blocks grid of building boxes (footprint up to
+    the block, height ~U(10, 40) m) separated by `street`-wide streets, walls and roofs
+    tessellated into square cells sized so that the mesh has about `target_tris`
+    triangles, plus `cars` 4.5 x 1.8 x 1.5 m boxes on the streets and a ground quad."""
+    rng = np.random.default_rng(seed)
+    block = pitch - street
+    half = blocks * pitch / 2
+    fx = rng.uniform(0.6, 1.0, (blocks, blocks)) * block
+    fz = rng.uniform(0.6, 1.0, (blocks, blocks)) * block
+    hh = rng.uniform(10.0, 40.0, (blocks, blocks))
+    area = float(np.sum(2 * (fx + fz) * hh + fx * fz))
+    budget = max(target_tris - 12 * cars - 2, 1000)
+    cell = np.sqrt(2.0 * area / budget)
+    vs, ts, nv = [], [], 0
+    for bi in range(blocks):
+        for bj in range(blocks):
+            x0 = -half + bi * pitch + street / 2
+            z0 = -half + bj * pitch + street / 2
+            mn = np.array([x0, 0.0, z0])
+            mx = mn + np.array([fx[bi, bj], hh[bi, bj], fz[bi, bj]])
+            d = mx - mn
+            ex, ey, ez = np.array([d[0], 0, 0]), np.array([0, d[1], 0]), np.array([0, 0, d[2]])
+            n = lambda L: max(1, int(round(L / cell)))
+            faces = [(mn, ex, ey), (mn, ez, ey), (mn + ez, ex, ey), (mn + ex, ez, ey), (mn + ey, ex, ez)]
+            for o, u, v in faces:
+                gv, gt = _grid_quads(o, u, v, n(np.linalg.norm(u)), n(np.linalg.norm(v)))
+                vs.append(gv)
+                ts.append(gt + nv)
+                nv += len(gv)
+    mesh = TriangleMesh()
+    mesh.append(np.concatenate(vs).astype(np.float32), np.concatenate(ts).astype(np.int32))
+    # cars on the street lines, parallel to the street
+    for _ in range(cars):
+        along = rng.uniform(-half, half)
+        line = -half + int(rng.integers(0, blocks + 1)) * pitch
+        side = rng.choice([-3.0, 3.0])
+        if rng.random() < 0.5:
+            mn = np.array([along, 0.0, line + side - 0.9])
+            mx = mn + np.array([4.5, 1.5, 1.8])
+        else:
+            mn = np.array([line + side - 0.9, 0.0, along])
+            mx = mn + np.array([1.8, 1.5, 4.5])
+        mesh.addBox(mn.astype(np.float32), mx.astype(np.float32))
+    mesh.addQuad([-half, 0, -half], [2 * half, 0, 0], [0, 0, 2 * half])
+    return mesh
+
+
+def street_poses(count, seed, blocks=14, pitch=42.0, height=1.0):
+    """Sensors on the street centre lines of urban_mesh at `height`, random yaw."""
+    rng = np.random.default_rng(seed)
+    half = blocks * pitch / 2
+    out = []
+    for _ in range(count):
+        along = rng.uniform(-half, half)
+        line = -half + int(rng.integers(0, blocks + 1)) * pitch
+        x, z = (along, line) if rng.random() < 0.5 else (line, along)
+        out.append(NFAntenna(np.array([x, height, z], np.float32), looking(rng.uniform(0, 2 * np.pi))))
+    return out
+
+
+def plane_poses(count, seed, extent=100.0, height=1.0):
+    """Sensors uniform over the boxes ground quad at `height`, random yaw."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        x, z = rng.uniform(-extent / 2, extent / 2, 2)
+        out.append(NFAntenna(np.array([x, height, z], np.float32), looking(rng.uniform(0, 2 * np.pi))))
+    return out
+
+
+# Resident scenes of the serving workload: the boxes generator at the batched workload's
+# density (extent grows with the box count) and the urban-canyon generator, alternating,
+# at 100 k .. 5 M triangles.
+SERVE_SCENES = [("boxes", 100_000), ("urban", 250_000), ("boxes", 500_000), ("urban", 1_000_000),
+                ("boxes", 2_000_000), ("urban", 3_000_000), ("boxes", 4_000_000), ("urban", 5_000_000)]
+
+
+def serve_scene(kind, tris, seed):
+    """(mesh, pose generator) of one resident serving scene."""
+    if kind == "boxes":
+        count = max(1, (tris - 2) // 12)
+        extent = 100.0 * np.sqrt(count / 83334.0)
+        return boxes_mesh(seed, count, extent), (lambda n, s: plane_poses(n, s, extent))
+    return urban_mesh(tris, seed), (lambda n, s: street_poses(n, s))

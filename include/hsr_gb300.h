@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HSR_ABI_VERSION 1
+#define HSR_ABI_VERSION 2
 
 typedef enum hsr_status {
     HSR_OK = 0,
@@ -37,7 +37,8 @@ typedef enum hsr_status {
     HSR_ERR_INTERRUPTED = 4,       /* the caller's interrupt flag was set */
     HSR_ERR_DEVICE = 5,            /* a kernel reported an error in its device status word */
     HSR_ERR_NOT_SUPPORTED = 6,     /* a flag combination this backend does not implement */
-    HSR_ERR_NO_DEVICE = 7          /* no CUDA device is visible */
+    HSR_ERR_NO_DEVICE = 7,         /* no CUDA device is visible */
+    HSR_ERR_TIMEOUT = 8            /* a served request has not finished within the wait */
 } hsr_status;
 
 /* FMCW ramp parameters; field-for-field radar::RFConfig (libradar/include/radar/radar.h:113-136).
@@ -275,6 +276,85 @@ hsr_status hsr_set_synth_engine(int32_t engine);
 /* Timing of the most recent batch launch on this scene: device milliseconds of the
  * trace kernel alone, measured with CUDA events on the launching stream. */
 hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);
+
+/* ---- Serving: continuous batching over resident scenes ------------------------------
+ *
+ * No counterpart in the reference, whose backends run one pose per synchronous call
+ * (src/arch/gpu.cpp:499-532, examples/src/2_large_scene.cpp:149-166). A server keeps
+ * several scenes resident and traces requests (scene, pose, chirp, range bins, budget)
+ * as they arrive: a worker thread runs batching ticks, each one persistent launch over
+ * a slice of every admitted request, so requests that arrive while others run join the
+ * next tick and their work shares the device. Requests are admitted when a slot and
+ * device memory for their accumulators are free. A request's result is the row
+ * hsr_simulate_batch gives for the same scene, pose, chirp, budget and index offset
+ * (the same Halton samples; only the summation order differs). The tracer flags and the
+ * phase mode are per server; geometrical optics must be on and guiding off. */
+typedef struct hsr_server hsr_server;
+
+typedef struct hsr_server_config {
+    int32_t max_slots;             /* requests admitted at once (each holds a slot) */
+    int32_t max_samples_per_chirp; /* largest N a request may ask for */
+    int64_t memory_bytes;          /* device memory for request state (admission by footprint) */
+    float tick_ms;                 /* target device time of one batching tick */
+    int32_t phase_mode;            /* hsr_phase_mode shared by every request */
+    hsr_tracer_flags flags;        /* tracer flags shared by every request */
+} hsr_server_config;
+
+typedef struct hsr_request {
+    int32_t scene;                 /* id returned by hsr_server_add_scene */
+    int32_t samples_per_chirp;     /* N, 1 .. max_samples_per_chirp */
+    hsr_rf_config rf;
+    hsr_antenna tx, rx;
+    int64_t budget;                /* Halton indices index_offset + [0, budget) */
+    int64_t index_offset;
+    float *out_row;                /* host complex64[N]: the fetchFrame row, written before completion */
+} hsr_request;
+
+typedef struct hsr_request_result {
+    int32_t status;                /* hsr_status of the request */
+    int32_t ticks;                 /* batching ticks the request took part in */
+    double queue_ms;               /* submit -> admitted */
+    double latency_ms;             /* submit -> row written */
+} hsr_request_result;
+
+typedef struct hsr_server_stats {
+    int64_t submitted, completed, failed;
+    int64_t ticks;
+    int64_t samples;               /* paths traced by the ticks */
+    double device_ms;              /* summed device time of the ticks (CUDA events) */
+    double p50_ms, p99_ms, max_ms; /* latency of completed requests (submit -> row written) */
+    int32_t max_batch;             /* most requests in one tick */
+    int32_t max_resident;          /* most requests admitted at once */
+    int64_t admitted_while_busy;   /* requests admitted while a tick was on the device */
+    int64_t memory_bytes_peak;     /* most request-state bytes held at once */
+    int64_t scene_bytes;           /* device bytes of the registered scenes */
+} hsr_server_stats;
+
+/* max_slots 256, N <= 1024, 64 MiB of request state, 4 ms ticks, FP32 reference phase,
+ * the reference's PathTracer defaults with doGuiding = 0. */
+void hsr_default_server_config(hsr_server_config *config);
+hsr_status hsr_server_create(const hsr_server_config *config, hsr_server **out_server);
+/* Registers a resident scene (not owned: it must outlive the server). Thread-safe. */
+hsr_status hsr_server_add_scene(hsr_server *server, hsr_scene *scene, int32_t *out_id);
+/* Queues a request (copied; out_row must stay valid until the request completes).
+ * Thread-safe. */
+hsr_status hsr_server_submit(hsr_server *server, const hsr_request *request, uint64_t *out_ticket);
+/* Waits up to timeout_ms (< 0: forever) for a request. HSR_OK: finished, `out` filled
+ * and the ticket released; HSR_ERR_TIMEOUT: still running (wait again). Thread-safe. */
+hsr_status hsr_server_wait(hsr_server *server, uint64_t ticket, int32_t timeout_ms,
+                           hsr_request_result *out);
+hsr_status hsr_server_get_stats(hsr_server *server, hsr_server_stats *out);
+/* Clears the counters and the latency record (e.g. after a warm-up). */
+hsr_status hsr_server_reset_stats(hsr_server *server);
+/* Finishes the ticks on the device, fails queued and unfinished requests with
+ * HSR_ERR_INTERRUPTED, and frees the server. */
+hsr_status hsr_server_destroy(hsr_server *server);
+
+/* The tick planner (host only, no device): splits a tick's sample target over requests
+ * with `remaining` samples each, by water-filling in order of the smallest remainder;
+ * every chunk but a request's last is a multiple of `tile`. */
+hsr_status hsr_debug_plan_tick(int32_t count, const int64_t *remaining, int64_t target, int32_t tile,
+                               int64_t *out_chunk);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,170 @@
+"""The serving loop (hsr_server_*): requests over three resident scenes with different
+chirps, range-bin counts, budgets and index offsets, submitted from two threads while
+others run. Each served row must equal the same request run alone through
+hsr_simulate_batch (same Halton samples; only the FP32 shared-memory and FP64 atomic
+summation order differ: 1e-5 relative L2)."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from hussar_gb300 import HsrError, PathTracer, Server, gb300, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+def tracer(depth=3):
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = depth
+    return t
+
+
+@pytest.fixture(scope="module")
+def resident(product_lib):
+    dih = scenes.dihedral_workload(poses=16)
+    sph = scenes.sphere_ground_workload(level=4)
+    box = scenes.boxes_workload(poses=16, count=3000, min_log2=12, max_log2=12)
+    out = []
+    for w in (dih, sph, box):
+        out.append((w, gb300.Backend(w.mesh, None)))
+    return out
+
+
+def make_requests(resident, count, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        si = int(rng.integers(0, len(resident)))
+        w, _ = resident[si]
+        n = int(rng.choice([128, 256, 512]))
+        rf = scenes.rf_chirp(bandwidth=float(rng.uniform(1e9, 4e9)), samples=n)
+        pi = int(rng.integers(0, len(w.tx)))
+        budget = int(round(2.0 ** rng.uniform(10, 17)))
+        if k in (5, 20, 33):
+            budget = (1 << 21) + 12345  # spans several ticks (not a whole number of tiles)
+            si = k % 2  # on the two small scenes, to keep the test short
+            w, _ = resident[si]
+            pi = 0
+        offset = int(rng.integers(0, 1 << 20)) if k % 3 == 0 else 0
+        reqs.append(dict(scene=si, rf=rf, n=n, tx=w.tx[pi], rx=w.rx[pi], budget=budget, offset=offset))
+    return reqs
+
+
+def alone(resident, r, t):
+    _, be = resident[r["scene"]]
+    return be.simulate_batch(r["rf"], r["n"], t, [r["tx"]], [r["rx"]], [r["budget"]], index_offset=[r["offset"]])[0]
+
+
+def test_served_rows_equal_standalone_rows(resident):
+    t = tracer()
+    reqs = make_requests(resident, 48, seed=11)
+    srv = Server(flags=t, max_slots=6, tick_ms=0.05)
+    ids = [srv.add_scene(be) for _, be in resident]
+    assert ids == [0, 1, 2]
+    handles = [None] * len(reqs)
+
+    def submitter(part, seed):
+        rng = np.random.default_rng(seed)
+        for k in part:
+            r = reqs[k]
+            handles[k] = srv.submit(r["scene"], r["rf"], r["n"], r["tx"], r["rx"], r["budget"], r["offset"])
+            time.sleep(float(rng.uniform(0, 0.003)))
+
+    th = [threading.Thread(target=submitter, args=(range(i, len(reqs), 2), i)) for i in range(2)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    rows, infos = [], []
+    for h in handles:
+        row, info = h.result(timeout=120)
+        rows.append(row)
+        infos.append(info)
+    st = srv.stats()
+    srv.close()
+    print("serving stats", st)
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["max_resident"] <= 6
+    assert st["max_batch"] > 1  # requests shared ticks
+    assert st["admitted_while_busy"] > 0  # and joined while others were on the device
+    assert st["samples"] == sum(r["budget"] for r in reqs)
+    assert max(i["ticks"] for i in infos) > 1  # long requests spanned several ticks
+    worst = 0.0
+    for r, row in zip(reqs, rows):
+        ref = alone(resident, r, t)
+        e = rel_l2(row, ref)
+        worst = max(worst, e)
+        assert e <= 1e-5, (r["scene"], r["n"], r["budget"], e)
+    print("worst served vs alone", worst)
+
+
+def test_served_row_matches_oracle(resident, oracle_lib):
+    """One served request of the dihedral configuration (77-81 GHz, N = 256, 2^18
+    samples, 2 bounces) against the CPU oracle at the parity bar of 1e-4 relative L2."""
+    w, be = resident[0]
+    t = tracer(w.max_depth)
+    rf, _ = scenes.rf_77ghz(256)
+    with Server(flags=t, max_slots=2, tick_ms=0.2) as srv:
+        sid = srv.add_scene(be)
+        row, info = srv.submit(sid, rf, 256, w.tx[5], w.rx[5], 1 << 18).result(timeout=60)
+    ref = oracle_lib.Scene(w.mesh).fetch_row(rf, 256, w.tx[5], w.rx[5], t, 1 << 18)
+    assert rel_l2(row, ref) <= 1e-4
+
+
+def test_admission_by_memory_footprint(resident):
+    """With accumulator memory for two N = 512 rows, at most two requests are resident;
+    the rest wait in the queue and still complete."""
+    t = tracer()
+    w, be = resident[1]
+    mem = 2 * 16 * 512
+    with Server(flags=t, max_slots=64, memory_bytes=mem, tick_ms=0.5) as srv:
+        sid = srv.add_scene(be)
+        rf = scenes.rf_chirp(samples=512)
+        hs = [srv.submit(sid, rf, 512, w.tx[0], w.rx[0], 1 << 15, k << 15) for k in range(8)]
+        rows = [h.result(timeout=120)[0] for h in hs]
+        st = srv.stats()
+    assert st["completed"] == 8 and st["max_resident"] <= 2
+    assert st["memory_bytes_peak"] <= mem
+    # the offsets differ, so the rows are different estimates of the same signal
+    assert rel_l2(rows[0], rows[1]) > 0
+
+
+def test_zero_budget_and_rejections(resident):
+    t = tracer()
+    w, be = resident[0]
+    rf = scenes.rf_chirp(samples=128)
+    with Server(flags=t, max_samples_per_chirp=256) as srv:
+        sid = srv.add_scene(be)
+        row, _ = srv.submit(sid, rf, 128, w.tx[0], w.rx[0], 0).result(timeout=60)
+        assert np.isnan(row.view(np.float32)).all()  # 0 / 0, as fetchFrame after no samples
+        with pytest.raises(HsrError):
+            srv.submit(sid, rf, 512, w.tx[0], w.rx[0], 1 << 12)  # N above the server's maximum
+        with pytest.raises(HsrError):
+            srv.submit(7, rf, 128, w.tx[0], w.rx[0], 1 << 12)  # unknown scene
+        with pytest.raises(HsrError):
+            srv.submit(sid, rf, 128, w.tx[0], w.rx[0], -1)
+
+
+def test_close_with_work_queued_returns(resident):
+    """Destroying a server with requests queued and running finishes the ticks on the
+    device and interrupts the rest; it does not wait for the whole backlog."""
+    t = tracer()
+    w, be = resident[2]
+    srv = Server(flags=t, max_slots=1, tick_ms=0.5)
+    sid = srv.add_scene(be)
+    rf = scenes.rf_chirp(samples=256)
+    for _ in range(6):
+        srv.submit(sid, rf, 256, w.tx[0], w.rx[0], 1 << 22)
+    time.sleep(0.05)
+    t0 = time.time()
+    srv.close()
+    assert time.time() - t0 < 20
