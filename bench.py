@@ -391,10 +391,107 @@ def run_gb300(args, rank, world, local_rank, dist):
         "cpu_baseline": {"value": cpu_val, "unit": "paths/s", "cores": cpu_cores, "kind": "port",
                          "sample": "%d Halton samples of pose 0 (%.1f s wall)" % (args.cpu_samples, cpu_s)},
         "modes": modes,
+        "time_to_minus40db": time_to_error() if not args.no_tte else None,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
+
+
+TTE_TARGET = 1e-2  # -40 dB: relative L2 of the complex IF signal
+TTE_REF_LOG2 = 28   # converged reference: 2^28 samples per pose, split-FP64 phase
+
+
+def time_to_error(max_log2=26):
+    """Time to -40 dB IF-signal error against the plain GPU form, on the sphere+ground pose
+    and the 91-pose dihedral sweep. Each form's rows at budget 2^k (Halton indices
+    0 .. 2^k-1, k = 10, 11, ...) are compared with a converged run of the same estimator
+    (split-FP64 phase, 2^28 samples per pose; relative L2 over all poses' rows); the
+    smallest such budget reaching 1e-2 is then timed through the host API (wall clock,
+    synchronous calls, median of 3).
+      plain_gpu            one pose per call, one-thread-per-sample kernel, FP32 phase of
+                           the reference, Frame::splat<16> (the OptiX backend's form)
+      batched_split        all poses in one wavefront launch, split-FP64 phase, splat<16>
+      batched_split_synth  the same with the fine histogram and tensor-core synthesis of
+                           the exact spectrum (its own estimator and reference)
+      batched_split_guided[_synth]  the same with device path guiding (PathTracer::run's
+                           doubling schedule; unbiased, the same reference)
+    A form that does not reach the target by 2^max_log2 reports the budget extrapolated
+    from the slope of its last six points (log error vs log budget) and the time for it
+    at its measured throughput, marked "extrapolated"."""
+    from hussar_gb300 import (HSR_PHASE_REFERENCE_FP32, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16,
+                              HSR_SPLAT_FINE_SYNTH, PathTracer, _lib, gb300, scenes)
+    L = _lib.lib()
+    out = {"target_rel_l2": TTE_TARGET, "reference": "same estimator, split-FP64 phase, 2^%d samples per pose"
+           % TTE_REF_LOG2, "timing": "wall clock through hsr_simulate_batch, median of 3"}
+    forms = {"plain_gpu": (1, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, True, False),
+             "batched_split": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16, False, False),
+             "batched_split_synth": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, False, False),
+             "batched_split_guided": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16, False, True),
+             "batched_split_synth_guided": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, False, True)}
+    for name, w in (("sphere_ground", scenes.sphere_ground_workload()), ("dihedral_91", scenes.dihedral_workload())):
+        plain_t, guided_t = PathTracer(), PathTracer()
+        plain_t.doGuiding = False
+        guided_t.doGuiding = True
+        plain_t.maxDepth = guided_t.maxDepth = w.max_depth
+        be = gb300.Backend(w.mesh, None)
+        N, P = w.frame.samplesPerChirp, len(w.tx)
+
+        def run(form, S):
+            kernel, phase, splat, per_pose, guided = form
+            t = guided_t if guided else plain_t
+            L.hsr_set_path_kernel(kernel)
+            try:
+                if per_pose:
+                    return np.concatenate([be.simulate_batch(w.rf, N, t, [w.tx[k]], [w.rx[k]], [S], phase_mode=phase,
+                                                             splat_mode=splat) for k in range(P)])
+                return be.simulate_batch(w.rf, N, t, w.tx, w.rx, np.full(P, S, np.int64), phase_mode=phase,
+                                         splat_mode=splat)
+            finally:
+                L.hsr_set_path_kernel(0)
+
+        refs = {s: run((0, HSR_PHASE_SPLIT_FP64, s, False, False), 1 << TTE_REF_LOG2).astype(np.complex128)
+                for s in (HSR_SPLAT_DIRICHLET16, HSR_SPLAT_FINE_SYNTH)}
+        res = {}
+        for fname, form in forms.items():
+            ref = refs[form[2]]
+            curve, s40 = [], None
+            for k in range(10, max_log2 + 1):
+                rows = run(form, 1 << k).astype(np.complex128)
+                err = float(np.linalg.norm(rows - ref) / np.linalg.norm(ref))
+                curve.append([k, err])
+                if err <= TTE_TARGET:
+                    s40 = 1 << k
+                    break
+            entry = {"error_by_log2_budget": curve, "samples_per_pose": s40}
+            timed_s = s40 or (1 << max_log2)
+            run(form, timed_s)  # warm-up at this size
+            times = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                run(form, timed_s)
+                times.append(time.perf_counter() - t0)
+            sec = float(np.median(times))
+            if s40:
+                entry["seconds"] = sec
+            else:
+                k, e = np.array(curve[-6:]).T
+                slope = float(np.polyfit(k, np.log2(e), 1)[0])  # log2 error per doubling
+                if slope < -0.05:
+                    extra = np.log2(e[-1] / TTE_TARGET) / -slope
+                    entry["extrapolated"] = {"slope_per_doubling": slope, "samples_per_pose": timed_s * 2.0 ** extra,
+                                             "seconds": sec * 2.0 ** extra}
+            res[fname] = entry
+        def seconds(e):
+            return e.get("seconds") or (e.get("extrapolated") or {}).get("seconds")
+
+        plain = seconds(res["plain_gpu"])
+        for fname in forms:
+            if fname != "plain_gpu":
+                sec = seconds(res[fname])
+                res[fname]["speedup_vs_plain_gpu"] = (plain / sec) if (plain and sec) else None
+        out[name] = dict(res, poses=P, range_bins=N, triangles=w.mesh.triangleCount())
+    return out
 
 
 def run_serve(args, rank, world, local_rank, dist):
@@ -503,12 +600,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve", "tte"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
     ap.add_argument("--kernel-only", action="store_true",
                     help="timed steps only (no e2e, counting, CPU baseline): the profiling command")
+    ap.add_argument("--no-tte", action="store_true", help="skip the time-to--40 dB measurement")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests admitted at once")
@@ -520,6 +618,11 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "serve":
         run_serve(args, rank, world, local_rank, dist)
+    elif args.workload == "tte":
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local_rank)
+            print(json.dumps({"time_to_minus40db": time_to_error()}), flush=True)
     else:
         run_gb300(args, rank, world, local_rank, dist)
     if dist is not None:

@@ -147,6 +147,7 @@ def lib():
         "hsr_server_reset_stats": [vp],
         "hsr_server_destroy": [vp],
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
+        "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)

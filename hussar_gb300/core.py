@@ -173,6 +173,19 @@ class PathTracer:
         return self.frame / np.float32(self.totalWeight)
 
 
+# struct DNode (hussar_gb300/csrc/hsr_common.cuh): both child boxes of a binary node
+DNODE_DTYPE = np.dtype([("a", "<f4", 4), ("b", "<f4", 4), ("c", "<f4", 4), ("child", "<i4", 2), ("unused", "<i4", 2)])
+
+
+def child_boxes(nodes):
+    """(lo, hi) of both children of every node, shape [nodes, 2, 3]."""
+    lo = np.stack([np.stack([nodes["a"][:, 0], nodes["a"][:, 2], nodes["c"][:, 0]], 1),
+                   np.stack([nodes["b"][:, 0], nodes["b"][:, 2], nodes["c"][:, 2]], 1)], 1)
+    hi = np.stack([np.stack([nodes["a"][:, 1], nodes["a"][:, 3], nodes["c"][:, 1]], 1),
+                   np.stack([nodes["b"][:, 1], nodes["b"][:, 3], nodes["c"][:, 3]], 1)], 1)
+    return lo, hi
+
+
 class _GB300:
     """Namespace mirroring hussar::gb300 (the drop-in for hussar::cpu / hussar::gpu)."""
 
@@ -253,6 +266,15 @@ class _GB300:
                                                        ctypes.byref(lv)))
             return {"nodes": n.value, "max_depth": d.value, "leaves": lv.value}
 
+        def device_bvh(self):
+            """The device BVH (tests): (nodes, tris), nodes a DNODE_DTYPE array (root 0),
+            tris [triangles, 12] float32 records in slot order."""
+            st = self.bvh_stats()
+            nodes = np.zeros(st["nodes"], dtype=DNODE_DTYPE)
+            tris = np.zeros((st["leaves"], 12), np.float32)
+            _lib.check(_lib.lib().hsr_debug_bvh(self._scene, _lib.ptr(nodes), len(nodes), _lib.ptr(tris), len(tris)))
+            return nodes, tris
+
         def intersect(self, origins, directions, tfar=None):
             """Closest-hit queries (RT::intersect): returns t, p, n, prim."""
             o = np.ascontiguousarray(origins, np.float32).reshape(-1, 3)
@@ -297,7 +319,7 @@ class _GB300:
 
         def traversal_counts(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None):
             """Exact traversal work of one batch launch (counting instantiation):
-            dict(nodes, tris, rays, bytes) with 64 B per node and 48 B per triangle."""
+            dict(nodes, tris, rays, bytes) with 64 B per BVH node and 48 B per triangle."""
             P = len(tx)
             txa = (_lib.AntennaC * P)(*[a.to_c() for a in tx])
             rxa = (_lib.AntennaC * P)(*[a.to_c() for a in rx])

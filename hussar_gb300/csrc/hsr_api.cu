@@ -68,7 +68,7 @@ struct Scratch {
     int *train, *active, *clear;
     double *tw;
     double *acc;
-    float *fine;  // fine-histogram rows (HSR_SPLAT_FINE_SYNTH), P x kFineRowPerBin N floats
+    double *fine;  // fine-histogram rows (HSR_SPLAT_FINE_SYNTH), P x kFineRowPerBin N FP64 sums
     float *rows;
     unsigned *counters;  // [0] status word, [2..3] 64-bit work counter
     size_t bytes;
@@ -97,7 +97,7 @@ static Scratch carve(void *base, int32_t P, int32_t N, bool fine) {
     s.clear = reinterpret_cast<int *>(take(sizeof(int) * P));
     s.tw = reinterpret_cast<double *>(take(sizeof(double) * P));
     s.acc = reinterpret_cast<double *>(take(sizeof(double) * 2 * size_t(P) * N));
-    s.fine = fine ? reinterpret_cast<float *>(take(sizeof(float) * kFineRowPerBin * size_t(P) * N)) : nullptr;
+    s.fine = fine ? reinterpret_cast<double *>(take(sizeof(double) * kFineRowPerBin * size_t(P) * N)) : nullptr;
     s.rows = reinterpret_cast<float *>(take(sizeof(float) * 2 * size_t(P) * N));
     s.bytes = off;
     return s;
@@ -164,8 +164,9 @@ struct GuideMem {
     int *train_child;
     float *train_acc;
     int *train_count;
-    float *scratch_e;
-    int *scratch_i;
+    // the whole schedule of a guided call, iteration-major: per iteration budget and
+    // Halton offset (int64), sample weight (float), train, clear and active flags (int)
+    unsigned char *sched;
 };
 
 static GuideMem carve_guide(void *base, int P) {
@@ -183,8 +184,7 @@ static GuideMem carve_guide(void *base, int P) {
     g.train_child = reinterpret_cast<int *>(take(4 * M));
     g.train_acc = reinterpret_cast<float *>(take(12 * M));
     g.train_count = reinterpret_cast<int *>(take(4 * size_t(P)));
-    g.scratch_e = reinterpret_cast<float *>(take(4 * M));
-    g.scratch_i = reinterpret_cast<int *>(take(8 * M));
+    g.sched = reinterpret_cast<unsigned char *>(take(size_t(kGuideMaxIters) * 32 * size_t(P)));
     return g;
 }
 
@@ -208,13 +208,16 @@ static hsr_status ensure_guide(SceneDev &sc, int P, GuideMem &out) {
 static constexpr int32_t kTile = 4096;  // samples per work item
 
 // One trace launch over the poses' current budgets/offsets/weights in scratch.
+// `tile` (a power of two, 256 .. kTile) is the samples per work item: smaller tiles keep
+// the SMs busy when a pass has few samples (the early guided iterations).
 static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
                                const hsr_tracer_flags *fl, int32_t P, float sample_weight, bool per_pose_weights,
                                int32_t phase_mode, int32_t splat_mode, cudaStream_t st, const GuideMem *g,
-                               void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr) {
+                               void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr,
+                               int32_t tile = kTile) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(s.counters + 2, 0, 8, st)) != cudaSuccess) return cuda_fail(e, "memset counter");
-    if (launch_tile_prefix(s.budget, P, kTile, s.tile_start, st) != 0)
+    if (launch_tile_prefix(s.budget, P, tile, s.tile_start, st) != 0)
         return cuda_fail(cudaGetLastError(), "tile prefix launch");
     TraceParams p{};
     p.nodes = sc.nodes;
@@ -229,7 +232,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     p.offset = s.offset;
     p.tile_start = s.tile_start;
     p.sample_weight = sample_weight;
-    p.tile = kTile;
+    p.tile = tile;
     p.acc = s.acc;
     p.status = s.counters;
     p.work_counter = s.counters + 2;
@@ -273,7 +276,7 @@ static hsr_status run_plain(SceneDev &sc, const Scratch &s, const hsr_rf_config 
     if (fine) {
         hsr_status r = ensure_synth(sc, N, P, st);
         if (r != HSR_OK) return r;
-        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(float) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
+        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(double) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
             return cuda_fail(e, "memset fine histogram");
     } else if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess) {
         return cuda_fail(e, "memset accumulators");
@@ -346,20 +349,28 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
     if (fine) {
         r = ensure_synth(sc, N, P, st);
         if (r != HSR_OK) return r;
-        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(float) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
+        if ((e = cudaMemsetAsync(s.fine, 0, sizeof(double) * kFineRowPerBin * size_t(P) * N, st)) != cudaSuccess)
             return cuda_fail(e, "memset fine histogram");
     } else if ((e = cudaMemsetAsync(s.acc, 0, sizeof(double) * 2 * size_t(P) * N, st)) != cudaSuccess) {
         return cuda_fail(e, "memset accumulators");
     }
     if (launch_guide_reset(P, g.samp_child, g.samp_p, g.train_child, g.train_acc, g.train_count, st) != 0)
         return cuda_fail(cudaGetLastError(), "guide reset");
-    std::vector<int64_t> b(P), o(P);
-    std::vector<float> w(P);
-    std::vector<int> train(P), active(P), clear(P);
+    if (K > size_t(kGuideMaxIters)) return fail(HSR_ERR_INVALID_ARGUMENT, "guided budget needs too many iterations");
+    // every iteration's schedule, uploaded once: the iterations then run back to back
+    const size_t it_bytes = 32 * size_t(P);
+    std::vector<unsigned char> blk(K * it_bytes);
     std::vector<double> tw(P, 0.0);
+    std::vector<char> any_clear(K, 0), any_active(K, 0);
+    std::vector<int64_t> iter_samples(K, 0);
     for (size_t k = 0; k < K; ++k) {
-        if (interrupt_flag && *interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted between iterations");
-        bool any_clear = false, any_active = false;
+        unsigned char *h = blk.data() + k * it_bytes;
+        int64_t *b = reinterpret_cast<int64_t *>(h);
+        int64_t *o = b + P;
+        float *w = reinterpret_cast<float *>(o + P);
+        int *train = reinterpret_cast<int *>(w + P);
+        int *clear = train + P;
+        int *active = clear + P;
         for (int p = 0; p < P; ++p) {
             if (k < sched[p].size()) {
                 const Iter &it = sched[p][k];
@@ -372,36 +383,48 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
                 if (it.clear) tw[p] = 0.0;
                 tw[p] += double(it.budget) * double(it.weight);  // path.h:445, 466-475
                 active[p] = k + 1 < sched[p].size() ? 1 : 0;
+                iter_samples[k] += it.budget;
             } else {
                 b[p] = 0;
                 o[p] = 0;
                 w[p] = 0.f;
-                train[p] = 0;
-                clear[p] = 0;
-                active[p] = 0;
+                train[p] = clear[p] = active[p] = 0;
             }
-            any_clear |= clear[p] != 0;
-            any_active |= active[p] != 0;
+            any_clear[k] |= clear[p] != 0;
+            any_active[k] |= active[p] != 0;
         }
-        if ((e = cudaMemcpyAsync(s.budget, b.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(s.offset, o.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(s.weights, w.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(s.train, train.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(s.clear, clear.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(s.active, active.data(), 4 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
-            return cuda_fail(e, "schedule upload");
-        if (any_clear) {
-            const int rc = fine ? launch_clear_rows_f(s.fine, P, kFineRowPerBin * N, s.clear, st)
-                                : launch_clear_rows(s.acc, P, N, s.clear, st);
+    }
+    if ((e = cudaMemcpyAsync(g.sched, blk.data(), blk.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(e, "schedule upload");
+    for (size_t k = 0; k < K; ++k) {
+        if (interrupt_flag) {
+            // honour the flag between iterations (PathTracer::run, path.h:188-189): let the
+            // previous iteration finish before looking at it
+            if (k > 0 && (e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "guided iteration");
+            if (*interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted between iterations");
+        }
+        Scratch si = s;
+        unsigned char *d = g.sched + k * it_bytes;
+        si.budget = reinterpret_cast<int64_t *>(d);
+        si.offset = si.budget + P;
+        si.weights = reinterpret_cast<float *>(si.offset + P);
+        si.train = reinterpret_cast<int *>(si.weights + P);
+        si.clear = si.train + P;
+        si.active = si.clear + P;
+        if (any_clear[k]) {
+            const int rc = fine ? launch_clear_rows_f(s.fine, P, kFineRowPerBin * N, si.clear, st)
+                                : launch_clear_rows(s.acc, P, N, si.clear, st);
             if (rc != 0) return cuda_fail(cudaGetLastError(), "clear rows");
         }
-        r = enqueue_pass(sc, s, rf, N, fl, P, 1.f, true, phase_mode, splat_mode, st, &g);
+        // about four work items per resident CTA in this iteration
+        const int64_t per_item = (iter_samples[k] + 8 * int64_t(sc.sm_count) - 1) / (8 * int64_t(sc.sm_count));
+        int32_t tile = 256;
+        while (tile < kTile && tile < per_item) tile *= 2;
+        r = enqueue_pass(sc, si, rf, N, fl, P, 1.f, true, phase_mode, splat_mode, st, &g, nullptr, 0, nullptr, tile);
         if (r != HSR_OK) return r;
-        if (any_active && launch_guide_step(P, s.active, g.samp_child, g.samp_p, g.train_child, g.train_acc,
-                                            g.train_count, g.scratch_e, g.scratch_i, st) != 0)
+        if (any_active[k] &&
+            launch_guide_step(P, si.active, g.samp_child, g.samp_p, g.train_child, g.train_acc, g.train_count, st) != 0)
             return cuda_fail(cudaGetLastError(), "guide step");
-        // the host schedule arrays are rewritten next iteration: let this one's copies land
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "guided iteration");
     }
     if ((e = cudaMemcpyAsync(s.tw, tw.data(), 8 * P, cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return cuda_fail(e, "weight upload");
@@ -571,6 +594,19 @@ hsr_status hsr_scene_footprint(const hsr_scene *s, int64_t *out_bytes) {
                  int64_t(sizeof(DNode)) * s->dev.node_count + int64_t(s->dev.scratch_bytes) +
                  int64_t(guide_bytes_per_pose()) * s->dev.guide_cap;
     return HSR_OK;
+}
+
+hsr_status hsr_debug_bvh(const hsr_scene *s, void *out_nodes, int64_t node_capacity, void *out_tris,
+                         int64_t tri_capacity) {
+    if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    if ((out_nodes && node_capacity < s->dev.node_count) || (out_tris && tri_capacity < s->dev.tri_count))
+        return fail(HSR_ERR_INVALID_ARGUMENT, "output capacity below the scene's node or triangle count");
+    cudaError_t e = cudaSuccess;
+    if (out_nodes)
+        e = cudaMemcpy(out_nodes, s->dev.nodes, sizeof(DNode) * size_t(s->dev.node_count), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && out_tris && s->dev.tri_count)
+        e = cudaMemcpy(out_tris, s->dev.tris, sizeof(DTri) * size_t(s->dev.tri_count), cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "BVH copy");
 }
 
 hsr_status hsr_scene_bvh_stats(const hsr_scene *s, int64_t *out_nodes, int32_t *out_max_depth, int64_t *out_leaves) {

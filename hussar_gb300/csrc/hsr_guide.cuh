@@ -6,7 +6,8 @@
 //
 // Per pose, two trees live in device memory:
 //   sampling: child index (-1 = leaf) and the probability of the first child
-//   training: child index and per-leaf accumulators (sum w, sum w d, sum w d^2)
+//   training: child index and per-leaf accumulators [3]; the step reads the second
+//             moment sum w d^2 (slot 2), the only statistic the tree is built from
 // A step (k_guide_step) builds the training tree's energies from its accumulators,
 // copies it into the sampling tree and refines the training tree (split leaves above
 // the threshold fraction, collapse subtrees below it), as GuidingWrapper::step does
@@ -28,6 +29,9 @@ struct GuideView {  // device pointers for one batch, [pose][kGuideMaxNodes]
     float *train_acc;  // [pose][node][3]
 };
 
+// The tree helpers read through plain pointers: global memory, or a CTA's shared-memory
+// copy of the pose's trees (the wavefront kernel stages them when it switches pose).
+
 // Tree density of the sampling tree at x (relative to uniform); descends by position.
 __device__ __forceinline__ float guide_tree_pdf(const int *child, const float *pfirst, float x0, float x1) {
     float pdf = 1.f;
@@ -35,9 +39,9 @@ __device__ __forceinline__ float guide_tree_pdf(const int *child, const float *p
     float lo0 = 0.f, lo1 = 0.f, s0 = 1.f, s1 = 1.f;
     int depth = 0;
     while (depth < kGuideMaxDepth) {
-        const int c = __ldg(&child[node]);
+        const int c = child[node];
         if (c < 0) break;
-        const float p0 = __ldg(&pfirst[node]);
+        const float p0 = pfirst[node];
         if ((depth & 1) == 0) {
             s0 *= 0.5f;
             if (x0 < lo0 + s0) {
@@ -72,9 +76,9 @@ __device__ __forceinline__ float guide_tree_sample(const int *child, const float
     float lo0 = 0.f, lo1 = 0.f, s0 = 1.f, s1 = 1.f;
     int depth = 0;
     while (depth < kGuideMaxDepth) {
-        const int c = __ldg(&child[node]);
+        const int c = child[node];
         if (c < 0) break;
-        const float p0 = __ldg(&pfirst[node]);
+        const float p0 = pfirst[node];
         float &x = (depth & 1) == 0 ? x0 : x1;
         if (x < p0) {
             x = p0 > 0.f ? x / p0 : 0.f;
@@ -120,9 +124,8 @@ __device__ __forceinline__ float guide_sample(const int *child, const float *pfi
     return pdf + u;
 }
 
-// GuidingWrapper::splat (path.h:96-111) into the training tree's leaf at x.
-__device__ __forceinline__ void guide_splat(const int *child, float *acc, float density, float weight, float x0,
-                                            float x1) {
+// The training tree's leaf at x (GuidingWrapper::splat's lookup, path.h:96-111).
+__device__ __forceinline__ int guide_leaf(const int *child, float x0, float x1) {
     int node = 0;
     float lo0 = 0.f, lo1 = 0.f, s0 = 1.f, s1 = 1.f;
     int depth = 0;
@@ -148,9 +151,7 @@ __device__ __forceinline__ void guide_splat(const int *child, float *acc, float 
         }
         ++depth;
     }
-    atomicAdd(&acc[3 * node + 0], weight);
-    atomicAdd(&acc[3 * node + 1], weight * density);
-    atomicAdd(&acc[3 * node + 2], weight * density * density);
+    return node;
 }
 
 }  // namespace hsr

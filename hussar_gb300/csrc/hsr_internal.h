@@ -112,10 +112,10 @@ struct TraceParams {
     const float *g_samp_p;
     const int *g_train_child;
     float *g_train_acc;
-    // fine-histogram mode (HSR_SPLAT_FINE_SYNTH): per pose a row of 8K floats,
+    // fine-histogram mode (HSR_SPLAT_FINE_SYNTH): per pose a row of 8K FP64 sums,
     // [Re h0 .. Re h3 | Im h0 .. Im h3], K = 8 N; nullptr: Dirichlet splat
     int32_t fine_bins;      // K
-    float *fine;
+    double *fine;
     // mixed batch: per-pose scene/chirp/row (nodes, tris, rf and acc rows above are then
     // unused; samples is the largest N); nullptr: uniform batch. Wavefront kernel only.
     const PoseJob *jobs;
@@ -125,15 +125,17 @@ size_t guide_bytes_per_pose();
 int launch_guide_reset(int P, int *samp_child, float *samp_p, int *train_child, float *train_acc, int *train_count,
                        cudaStream_t st);
 int launch_guide_step(int P, const int *active, int *samp_child, float *samp_p, int *train_child, float *train_acc,
-                      int *train_count, float *scratch_e, int *scratch_i, cudaStream_t st);
+                      int *train_count, cudaStream_t st);
+// longest guided schedule (PathTracer::run iterations) a call may have
+constexpr int kGuideMaxIters = 50;
 
 int synth_build_operand(SynthOperand &op, int N, cudaStream_t st, std::string &err);
 void synth_free_operand(SynthOperand &op);
 size_t synth_scratch_bytes(const SynthOperand &op, int P);
-int synth_run(const SynthOperand &op, const float *fine, int P, void *scratch, int engine, const int64_t *budget,
+int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, int engine, const int64_t *budget,
               float sample_weight, const double *tw, int normalise, float *out_rows, unsigned *status, cudaStream_t st,
               std::string &err);
-int launch_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st);
+int launch_clear_rows_f(double *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st);
 // 0: tensor cores (tcgen05, split BF16); 1: CUDA cores (FP32)
 extern int g_synth_engine;
 
@@ -147,7 +149,7 @@ int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, cons
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st);
 int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
-size_t wave_smem_bytes(int samples);
+size_t wave_smem_bytes(int samples, bool guided);
 int wave_blocks_per_sm(int samples, bool mixed);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel

@@ -353,48 +353,67 @@ __device__ __forceinline__ void splat_serial(float *s_re, float *s_im, int n, co
 
 // A full warp adds the items of the lanes in `mask` cooperatively: lane l owns window
 // offset l - 16 (lane 0 also owns +16), so one item's 33 bins are distinct addresses
-// updated by distinct lanes. Must be called by all 32 lanes.
+// updated by distinct lanes. Items are taken in lane order; each lane sums its bin over
+// a run of items with the same center in registers and adds the sum once when the
+// center changes (coherent returns put most of a warp's items on one center, and the
+// shared-memory atomics on those few bins are what limits the splat). A delta item
+// (shift 0) adds its value at offset 0 only. Must be called by all 32 lanes.
 __device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, unsigned mask, const SplatItem &mine) {
     const int lane = threadIdx.x & 31;
+    const int s = lane - 16;
+    int center = 0;
+    bool open = false;
+    float ar = 0.f, ai = 0.f, er = 0.f, ei = 0.f;  // this lane's bin, and lane 0's bin +16
+    auto flush = [&]() {
+        const bool inside = (center - 16 >= 0) && (center + 16 < n);
+        if (ar != 0.f || ai != 0.f) {
+            const int bin = inside ? center + s : ref_mod(center + s, n);
+            atomicAdd(&s_re[bin], ar);
+            atomicAdd(&s_im[bin], ai);
+        }
+        if (lane == 0 && (er != 0.f || ei != 0.f)) {
+            const int bin = inside ? center + 16 : ref_mod(center + 16, n);
+            atomicAdd(&s_re[bin], er);
+            atomicAdd(&s_im[bin], ei);
+        }
+        ar = ai = er = ei = 0.f;
+    };
     while (mask) {
         const int j = __ffs(mask) - 1;
         mask &= mask - 1;
-        const int center = __shfl_sync(0xffffffffu, mine.center, j);
+        const int c = __shfl_sync(0xffffffffu, mine.center, j);
         const float shift = __shfl_sync(0xffffffffu, mine.shift, j);
         const float vr = __shfl_sync(0xffffffffu, mine.value.re, j);
         const float vi = __shfl_sync(0xffffffffu, mine.value.im, j);
         const float w = __shfl_sync(0xffffffffu, mine.w, j);
+        if (open && c != center) flush();
+        center = c;
+        open = true;
         if (shift == 0.f) {
-            if (lane == 0) {
-                int bin = ref_mod(center, n);
-                atomicAdd(&s_re[bin], vr);
-                atomicAdd(&s_im[bin], vi);
+            if (s == 0) {
+                ar += vr;
+                ai += vi;
             }
             continue;
         }
-        const bool inside = (center - 16 >= 0) && (center + 16 < n);
-        {
-            const int s = lane - 16;
-            int bin = inside ? center + s : ref_mod(center + s, n);
-            float ws = w / (shift - float(s));
-            atomicAdd(&s_re[bin], ws * vr);
-            atomicAdd(&s_im[bin], ws * vi);
-        }
+        const float ws = w / (shift - float(s));
+        ar += ws * vr;
+        ai += ws * vi;
         if (lane == 0) {
-            const int s = 16;
-            int bin = inside ? center + s : ref_mod(center + s, n);
-            float ws = w / (shift - float(s));
-            atomicAdd(&s_re[bin], ws * vr);
-            atomicAdd(&s_im[bin], ws * vi);
+            const float w16 = w / (shift - 16.f);
+            er += w16 * vr;
+            ei += w16 * vi;
         }
     }
+    if (open) flush();
 }
 
 // Fine range histogram (HSR_SPLAT_FINE_SYNTH): 8 sub-bins per range bin with moments
 // h_d += c eps^d / d! (d = 0..3) of the sub-bin offset eps (in bins); the spectrum is
 // synthesised from it afterwards (hsr_synth.cu). `row` is the pose's
-// [Re h0..h3 | Im h0..h3] row, K = 8 N.
-__device__ __forceinline__ void splat_fine(float *row, int K, float sample, cf value) {
+// [Re h0..h3 | Im h0..h3] row, K = 8 N. The terms are FP32; the sums are FP64, since a
+// coherent return adds millions of nearly equal terms to one sub-bin.
+__device__ __forceinline__ void splat_fine(double *row, int K, float sample, cf value) {
     const float bs = sample * float(kFineOS);
     const float kk = rintf(bs);
     const float eps = (bs - kk) * (1.f / float(kFineOS));
@@ -405,8 +424,8 @@ __device__ __forceinline__ void splat_fine(float *row, int K, float sample, cf v
     float m = 1.f;
 #pragma unroll
     for (int d = 0; d < kFineMoments; ++d) {
-        atomicAdd(row + d * K + k, value.re * m);
-        atomicAdd(row + (kFineMoments + d) * K + k, value.im * m);
+        atomicAdd(row + d * K + k, double(value.re * m));
+        atomicAdd(row + (kFineMoments + d) * K + k, double(value.im * m));
         m = m * eps / float(d + 1);
     }
 }
@@ -422,6 +441,10 @@ __device__ __forceinline__ int find_pose(const int64_t *__restrict__ tile_start,
     }
     return lo;
 }
+
+// A CTA's shared-memory row holds FP32 partial sums of at most this many samples of one
+// pose before it is flushed to the FP64 accumulators.
+constexpr long long kFlushSamples = 65536;
 
 // Flushes a CTA's shared-memory row into the pose's FP64 accumulators and clears it.
 __device__ __forceinline__ void flush_row(double *acc, float *s_re, float *s_im, int n) {
@@ -442,7 +465,7 @@ namespace hsr {
 struct PoseCtx {
     Ant tx, rx;
     int64_t offset;
-    float *fine_row;  // fine-histogram row of the pose (nullptr: Dirichlet splat)
+    double *fine_row;  // fine-histogram row of the pose (nullptr: Dirichlet splat)
     float weight;
     int train;
     const int *samp_child;
@@ -468,8 +491,12 @@ __device__ __forceinline__ PoseCtx load_pose(const TraceParams &p, int pose) {
 }
 
 // guiding.splat(|guidingWeight| * primaryPdf, {}, 1 / primaryPdf, primary) (path.h:448-450).
-// Only the second moment drives the tree, so zero-density samples add nothing.
-__device__ __forceinline__ void guide_train(const PoseCtx &c, cf gw, float pdf, float x0, float x1) {
+// Only the second moment drives the tree, so zero-density samples add nothing. The sum
+// goes to `acc2[stride * leaf]`: the pose's training accumulators in global memory
+// (stride 3, slot 2), or a CTA's shared-memory copy (stride 1) flushed by flush_guide;
+// `train_child` is the training topology (global, or the CTA's staged copy).
+__device__ __forceinline__ void guide_train(const PoseCtx &c, const int *train_child, float *acc2, int stride, cf gw,
+                                            float pdf, float x0, float x1) {
     if (!c.train || !(pdf > 0.f)) return;
     // std::abs(radar::complex) (complex.h:225-237)
     float ax = fabsf(gw.re), ay = fabsf(gw.im);
@@ -482,7 +509,20 @@ __device__ __forceinline__ void guide_train(const PoseCtx &c, cf gw, float pdf, 
     }
     const float density = mag * pdf;
     if (density == 0.f) return;
-    guide_splat(c.train_child, c.train_acc, density, 1.f / pdf, x0, x1);
+    const float weight = 1.f / pdf;
+    const int leaf = guide_leaf(train_child, x0, x1);
+    atomicAdd(&acc2[stride * leaf], weight * density * density);
+}
+
+// Adds a CTA's shared-memory training sums to the pose's accumulators and clears them.
+__device__ __forceinline__ void flush_guide(const PoseCtx &c, float *s_g) {
+    for (int i = threadIdx.x; i < kGuideMaxNodes; i += blockDim.x) {
+        const float v = s_g[i];
+        if (v != 0.f) {
+            if (c.train) atomicAdd(&c.train_acc[3 * i + 2], v);
+            s_g[i] = 0.f;
+        }
+    }
 }
 
 }  // namespace hsr

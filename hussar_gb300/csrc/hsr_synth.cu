@@ -66,14 +66,15 @@ __global__ void k_build_bt(const double2 *__restrict__ g, int N, int K, int KK, 
     bt[idx] = v;
 }
 
-// x = x1 + x2 + x3 in BF16 (row-major, padded copies)
-__global__ void k_split3(const float *__restrict__ x, int rows, int cols, int ld_in, int rows_pad, int cols_pad,
+// x = x1 + x2 + x3 in BF16 (row-major, padded copies) of the FP32 value of x
+template <typename T>
+__global__ void k_split3(const T *__restrict__ x, int rows, int cols, int ld_in, int rows_pad, int cols_pad,
                          __nv_bfloat16 *__restrict__ o1, __nv_bfloat16 *__restrict__ o2,
                          __nv_bfloat16 *__restrict__ o3) {
     const int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (idx >= int64_t(rows_pad) * cols_pad) return;
     const int r = int(idx / cols_pad), c = int(idx % cols_pad);
-    const float v = (r < rows && c < cols) ? x[size_t(r) * ld_in + c] : 0.f;
+    const float v = (r < rows && c < cols) ? float(x[size_t(r) * ld_in + c]) : 0.f;
     const __nv_bfloat16 a = __float2bfloat16_rn(v);
     const float r1 = v - __bfloat162float(a);
     const __nv_bfloat16 b = __float2bfloat16_rn(r1);
@@ -88,7 +89,7 @@ __global__ void k_split3(const float *__restrict__ x, int rows, int cols, int ld
 // CUDA-core FP32 GEMM (cross-check and small batches): C[M x NC] = A[M x KK] * B,
 // with B given transposed (bt[NC x KK]).
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_sgemm_nt(const float *__restrict__ a, const float *__restrict__ bt, int M,
+__global__ void __launch_bounds__(256) k_sgemm_nt(const double *__restrict__ a, const float *__restrict__ bt, int M,
                                                   int NC, int KK, int lda, int ldb, float *__restrict__ c, int ldc) {
     __shared__ float As[16][65];
     __shared__ float Bs[16][65];
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(256) k_sgemm_nt(const float *__restrict__ a, c
         for (int t = threadIdx.x; t < 64 * 16; t += 256) {
             const int rr = t / 16, kk = t % 16;
             const int m = m0 + rr, n = n0 + rr, k = k0 + kk;
-            As[kk][rr] = (m < M && k < KK) ? a[size_t(m) * lda + k] : 0.f;
+            As[kk][rr] = (m < M && k < KK) ? float(a[size_t(m) * lda + k]) : 0.f;
             Bs[kk][rr] = (n < NC && k < KK) ? bt[size_t(n) * ldb + k] : 0.f;
         }
         __syncthreads();
@@ -419,8 +420,8 @@ size_t synth_scratch_bytes(const SynthOperand &op, int P) {
     return size_t(Mpad) * op.KKpad * 2 * 3 + size_t(P) * op.NCpad * 4 + 3 * 256;
 }
 
-// fine histograms (P x KK floats, row stride KK) -> frame rows (P x N complex64)
-int synth_run(const SynthOperand &op, const float *fine, int P, void *scratch, int engine, const int64_t *budget,
+// fine histograms (P x KK FP64 sums, row stride KK) -> frame rows (P x N complex64)
+int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, int engine, const int64_t *budget,
               float sample_weight, const double *tw, int normalise, float *out_rows, unsigned *status, cudaStream_t st,
               std::string &err) {
     const int Mpad = (P + kBM - 1) / kBM * kBM;

@@ -128,7 +128,7 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
         o = hp;
         depth++;
     }
-    guide_train(pc, gw, primaryPdf, px, py);
+    if (pc.train) guide_train(pc, pc.train_child, pc.train_acc + 2, 3, gw, primaryPdf, px, py);
 }
 
 template <int kPhase, bool kRecord, bool kCount>
@@ -142,6 +142,7 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
     float *s_re = smem, *s_im = smem + p.samples;
     for (int k = threadIdx.x; k < 2 * p.samples; k += blockDim.x) smem[k] = 0.f;
     int cur_pose = -1;
+    long long since_flush = 0;  // samples of cur_pose in the row since its last flush (CTA-uniform)
     PoseCtx pc;
     while (true) {
         __syncthreads();
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
             }
             cur_pose = pose;
             pc = load_pose(p, pose);
+            since_flush = 0;
         }
         const int64_t budget = __ldg(&p.budget[pose]);
         const int64_t first = (item - __ldg(&p.tile_start[pose])) * p.tile;
@@ -164,6 +166,13 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
         for (int64_t s = first + threadIdx.x; s < last; s += blockDim.x) {
             trace_sample<kPhase, kRecord, kCount>(p, pc, uint64_t(pc.offset + s), s_re, s_im,
                                                   kRecord ? records + s * max_rec : nullptr, max_rec, &cnt, &rays);
+        }
+        since_flush += last - first;
+        if (since_flush >= kFlushSamples) {
+            // bound the FP32 partial sums: move the row to the FP64 accumulators
+            __syncthreads();
+            flush_row(p.acc + 2 * int64_t(cur_pose) * p.samples, s_re, s_im, p.samples);
+            since_flush = 0;
         }
     }
     if (cur_pose >= 0) {
@@ -318,13 +327,13 @@ __global__ void k_clear_rows(double *acc, int32_t pose_count, int32_t samples, c
 }
 
 // Zeroes the fine-histogram rows (len floats each) of the poses with clear[pose] != 0.
-__global__ void k_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *__restrict__ clear) {
+__global__ void k_clear_rows_f(double *rows, int32_t pose_count, int32_t len, const int *__restrict__ clear) {
     int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= int64_t(pose_count) * len) return;
-    if (clear[i / len]) rows[i] = 0.f;
+    if (clear[i / len]) rows[i] = 0.0;
 }
 
-int launch_clear_rows_f(float *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st) {
+int launch_clear_rows_f(double *rows, int32_t pose_count, int32_t len, const int *clear, cudaStream_t st) {
     int64_t n = int64_t(pose_count) * len;
     k_clear_rows_f<<<unsigned((n + 255) / 256), 256, 0, st>>>(rows, pose_count, len, clear);
     note_launches(1);

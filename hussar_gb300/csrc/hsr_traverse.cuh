@@ -7,7 +7,7 @@
 // restatement; a hit needs tnear < t <= tfar; equal-t ties go to the lower original
 // primitive id, so the answer does not depend on the BVH shape or traversal order.
 // Box test: slab test with fused multiply-adds on boxes padded at build time (the
-// padding absorbs the rounding), NaN slabs (0 * inf) left unbounded: conservative.
+// padding absorbs the rounding); 1/d is kept finite (see safe_inv).
 #pragma once
 #include "hsr_common.cuh"
 
@@ -21,14 +21,23 @@ struct RayPre {
     float oix, oiy, oiz;   // o / d products for the FMA slab test
 };
 
+// Direction components below 1e-30 in magnitude are replaced by +-1e-30 before the
+// division, so 1/d stays finite: an exact zero would make the FMA slab form evaluate
+// inf - inf = NaN on one plane and reject a box the (axis-parallel) ray lies in. The
+// planes' distances are then about +-|x - o| * 1e30, far below FLT_MAX for any scene
+// coordinate, and the FMA cancellation error (~6e-8 |o|) stays below the boxes' padding.
+__device__ __forceinline__ float safe_inv(float d) {
+    return 1.f / (fabsf(d) >= 1e-30f ? d : copysignf(1e-30f, d));
+}
+
 __device__ __forceinline__ RayPre ray_pre(f3 o, f3 d) {
     RayPre r;
     r.ox = o.x;
     r.oy = o.y;
     r.oz = o.z;
-    r.ix = 1.f / d.x;
-    r.iy = 1.f / d.y;
-    r.iz = 1.f / d.z;
+    r.ix = safe_inv(d.x);
+    r.iy = safe_inv(d.y);
+    r.iz = safe_inv(d.z);
     r.oix = o.x * r.ix;
     r.oiy = o.y * r.iy;
     r.oiz = o.z * r.iz;

@@ -2,9 +2,10 @@
 // default, path.h:156): the same per-path arithmetic as the one-thread-per-sample
 // kernel, reorganised so that warps stay converged.
 //
-// A persistent CTA of 256 threads keeps a stack of up to 512 live path states in
-// shared memory and alternates two stages:
-//   GENERATE  (stack below 256): 256 new samples, one per thread: Halton point,
+// A persistent CTA of 256 threads keeps a stack of up to 384 live path states in
+// shared memory (four CTAs per SM: 64 registers, ~46 KB of shared memory each) and
+// alternates two stages:
+//   GENERATE  (at most 128 live paths): 256 new samples, one per thread: Halton point,
 //             antenna ray, closest hit; paths that hit something are pushed.
 //   EXTEND    (otherwise): 256 paths popped, one per thread: specular reflection,
 //             next-event estimate towards RX (shadow ray, PO re-radiation, filtering,
@@ -26,7 +27,7 @@ namespace hsr {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStack = 2 * kThreads;
+constexpr int kStack = 3 * kThreads / 2;  // live path states per CTA
 
 struct WaveShared {
     float ox[kStack], oy[kStack], oz[kStack];  // hit point (origin of the next segment)
@@ -40,6 +41,7 @@ struct WaveShared {
     int count;
     int pose, pending_pose, exhausted;
     long long gen, gen_end, pending_first, pending_last;
+    long long since_flush;      // samples generated since the row was last flushed
     PoseJob job;                // mixed batches: the current pose's scene, chirp and row
     float max_dist, bandwidth;  // mixed batches: derived from job.rf
 };
@@ -111,12 +113,16 @@ __device__ __forceinline__ double *pose_row(const TraceParams &p, const WaveShar
     return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
 }
 
+// Four CTAs per SM for the uniform form (64 registers; the few spills cost less than the
+// latency the extra warps hide); the mixed form keeps two (it spills heavily below ~120).
 template <int kPhase, bool kMixed>
-__global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
+__global__ void __launch_bounds__(kThreads, kMixed ? 2 : 4) k_wave(TraceParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
     float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
     float *s_im = s_re + p.samples;  // the row is sized for the largest N of the launch
+    // guided launches: the CTA's training sums (second moment per training-tree node)
+    float *s_g = s_re + 2 * p.samples;
     const int tid = threadIdx.x;
     const hsr_tracer_flags &fl = p.flags;
     // the scene, chirp and row of the current pose: launch-uniform, or the pose's job
@@ -130,12 +136,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
     const long long total = __ldg(&p.tile_start[p.pose_count]);
 
     for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
+    if (p.do_guide)
+        for (int k = tid; k < kGuideMaxNodes; k += kThreads) s_g[k] = 0.f;
     if (tid == 0) {
         S.count = 0;
         S.pose = -1;
         S.pending_pose = -1;
         S.exhausted = 0;
         S.gen = S.gen_end = 0;
+        S.since_flush = 0;
     }
     __syncthreads();
 
@@ -169,11 +178,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
         const long long gen = S.gen, gen_end = S.gen_end;
         const int pending = S.pending_pose;
         const int exhausted = S.exhausted;
+        const long long since_flush = S.since_flush;
         __syncthreads();  // every thread has read the shared control words
 
-        if (gen < gen_end && count < kThreads) {
+        if (since_flush >= kFlushSamples && cur_pose >= 0) {
+            // bound the FP32 partial sums: move the row to the FP64 accumulators
+            flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
+            if (p.do_guide) flush_guide(pc, s_g);
+            if (tid == 0) S.since_flush = 0;
+            __syncthreads();
+            continue;
+        }
+
+        if (gen < gen_end && count <= kStack - kThreads) {
             // ---------------- GENERATE ----------------
-            if (tid == 0) S.gen = min(gen + (long long)kThreads, gen_end);
+            if (tid == 0) {
+                S.gen = min(gen + (long long)kThreads, gen_end);
+                S.since_flush += S.gen - gen;
+            }
             const long long s = gen + tid;
             bool has_item = false;
             SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
@@ -210,7 +232,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                         alive = true;
                     }
                 }
-                if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
+                if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
             }
             if (!fl.onlyIndirect) splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
@@ -273,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                         alive = true;
                     }
                 }
-                if (!alive) guide_train(pc, g.gw, g.pdf, g.x0, g.x1);
+                if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
             }
             splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
             __syncthreads();
@@ -282,7 +304,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
 
         if (pending >= 0) {
             // stack drained: finish the old pose's row and switch to the new pose
-            if (cur_pose >= 0) flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
+            if (cur_pose >= 0) {
+                flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
+                if (p.do_guide) flush_guide(pc, s_g);
+            }
             cur_pose = pending;
             pc = load_pose(p, cur_pose);
             __syncthreads();  // every thread is done with the old pose's job
@@ -293,6 +318,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
                     S.bandwidth = chirp_bandwidth(S.job.rf);
                 }
                 S.pose = pending;
+                S.since_flush = 0;
                 S.gen = S.pending_first;
                 S.gen_end = S.pending_last;
                 S.pending_pose = -1;
@@ -305,6 +331,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
     if (cur_pose >= 0) {
         __syncthreads();
         flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
+        if (p.do_guide) flush_guide(pc, s_g);
     }
 #undef HSR_NODES
 #undef HSR_TRIS
@@ -315,7 +342,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_wave(TraceParams p) {
 
 }  // namespace
 
-size_t wave_smem_bytes(int samples) { return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float); }
+size_t wave_smem_bytes(int samples, bool guided) {
+    // guided: the CTA's training sums
+    return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float) + (guided ? kGuideMaxNodes * sizeof(float) : 0);
+}
 
 template <int kPhase, bool kMixed>
 void wave_instance(const TraceParams &p, int grid, size_t smem, cudaStream_t st) {
@@ -325,7 +355,7 @@ void wave_instance(const TraceParams &p, int grid, size_t smem, cudaStream_t st)
 
 int wave_blocks_per_sm(int samples, bool mixed) {
     int nb = 0;
-    const size_t smem = wave_smem_bytes(samples);
+    const size_t smem = wave_smem_bytes(samples, false);
     if (mixed) {
         cudaFuncSetAttribute(k_wave<HSR_PHASE_REFERENCE_FP32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(smem));
@@ -339,7 +369,7 @@ int wave_blocks_per_sm(int samples, bool mixed) {
 }
 
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err) {
-    const size_t smem = wave_smem_bytes(p.samples);
+    const size_t smem = wave_smem_bytes(p.samples, p.do_guide != 0);
     const bool split = phase_mode == HSR_PHASE_SPLIT_FP64;
     if (p.jobs) {
         if (split)

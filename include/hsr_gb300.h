@@ -258,6 +258,14 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
                                       const hsr_antenna *rx, const int64_t *budget,
                                       const int64_t *index_offset, int64_t *out_counts);
 
+/* Copies the scene's device BVH to the host (tests): out_nodes receives node_count binary
+ * nodes of 64 bytes each, both child boxes and child references (layout in
+ * hussar_gb300/csrc/hsr_common.cuh, struct DNode; a negative reference c is triangle slot
+ * ~c), out_tris triangle_count 48-byte records {v0.xyz, original id bits, v1-v0, 0,
+ * v2-v0, 0} in slot order. Either pointer may be null; capacities are in records. */
+hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_capacity, void *out_tris,
+                         int64_t tri_capacity);
+
 /* Which trace kernel the simulate calls use (process-wide): 0 (default) = the wavefront
  * kernel whenever geometrical optics is on, 1 = always the one-thread-per-sample kernel.
  * Both compute the same per-path values; tests use this to check each one. */

@@ -1,0 +1,85 @@
+"""The device BVH as built on the GPU (PLOC and LBVH topologies).
+
+Structure: a binary tree over all triangles, root 0, every internal node but the root and
+every triangle slot referenced exactly once. Conservativeness: each stored child box
+contains the padded bounding box of every triangle beneath it, with the padding the build
+applies (max|x| * 4e-6 + 1e-6 per axis), so the FP32 slab test cannot reject a box that a
+hit lies in."""
+import numpy as np
+import pytest
+
+from hussar_gb300 import TriangleMesh, gb300, scenes
+from hussar_gb300.core import child_boxes
+
+pytestmark = pytest.mark.gpu
+
+
+def padded_boxes(mesh, tris):
+    """Padded boxes of the triangles in slot order, from the mesh's own vertices (the
+    records carry the original primitive id in v0.w)."""
+    prim = tris[:, 3].copy().view(np.int32)
+    v = np.asarray(mesh.vertexBuffer, np.float32)[np.asarray(mesh.indexBuffer)[prim]]  # [n, 3, 3]
+    v0, v1, v2 = v[:, 0], v[:, 1], v[:, 2]
+    mn = np.minimum(v0, np.minimum(v1, v2))
+    mx = np.maximum(v0, np.maximum(v1, v2))
+    # the build may round m * 4e-6 + 1e-6 once (fused) or twice: check against the smaller pad
+    m = np.maximum(np.abs(mn), np.abs(mx))
+    pad2 = (m * np.float32(4e-6)).astype(np.float32) + np.float32(1e-6)
+    pad1 = (m.astype(np.float64) * np.float64(np.float32(4e-6)) + np.float64(np.float32(1e-6))).astype(np.float32)
+    pad = np.minimum(pad1, pad2).astype(np.float32)
+    return mn - pad, mx + pad
+
+
+def check_tree(be, mesh):
+    nt = mesh.triangleCount()
+    nodes, tris = be.device_bvh()
+    assert len(tris) == nt and len(nodes) == nt - 1
+    child = nodes["child"]
+    internal = child[child >= 0]
+    leaves = ~child[child < 0]
+    assert np.array_equal(np.sort(internal), np.arange(1, nt - 1))
+    assert np.array_equal(np.sort(leaves), np.arange(nt))
+    lo, hi = child_boxes(nodes)
+    tlo, thi = padded_boxes(mesh, tris)
+    # post-order over the tree (explicit stack), subtree boxes bottom-up
+    order, stack = [], [0]
+    while stack:
+        i = stack.pop()
+        order.append(i)
+        stack.extend(int(c) for c in child[i] if c >= 0)
+    sub_lo = np.zeros((nt - 1, 3), np.float32)
+    sub_hi = np.zeros((nt - 1, 3), np.float32)
+    for i in reversed(order):
+        blo, bhi = [], []
+        for k in range(2):
+            c = int(child[i, k])
+            cl, ch = (sub_lo[c], sub_hi[c]) if c >= 0 else (tlo[~c], thi[~c])
+            assert (lo[i, k] <= cl).all() and (hi[i, k] >= ch).all(), (i, k)
+            blo.append(cl)
+            bhi.append(ch)
+        sub_lo[i] = np.minimum(blo[0], blo[1])
+        sub_hi[i] = np.maximum(bhi[0], bhi[1])
+    return nodes
+
+
+@pytest.mark.parametrize("builder", [0, 1], ids=["ploc", "lbvh"])
+def test_device_bvh_contains_padded_triangles(product_lib, builder):
+    product_lib.hsr_set_bvh_builder(builder)
+    try:
+        for mesh in (scenes.dihedral_mesh(), scenes.sphere_ground_workload(level=3).mesh,
+                     scenes.boxes_mesh(seed=3, count=2000)):
+            be = gb300.Backend(mesh, None)
+            check_tree(be, mesh)
+            print(mesh.triangleCount(), "triangles, depth", be.bvh_stats()["max_depth"])
+    finally:
+        product_lib.hsr_set_bvh_builder(0)
+
+
+def test_single_triangle_scene(product_lib):
+    m = TriangleMesh()
+    m.append(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32), np.array([[0, 1, 2]], np.int32))
+    be = gb300.Backend(m, None)
+    st = be.bvh_stats()
+    assert st["leaves"] == 1 and st["nodes"] == 1
+    t, p, n, prim = be.intersect(np.array([[0.2, 0.2, 1.0]], np.float32), np.array([[0, 0, -1.0]], np.float32))
+    assert prim[0] == 0 and t[0] == np.float32(1.0)

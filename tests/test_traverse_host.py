@@ -1,0 +1,64 @@
+"""The device traversal code on the CPU: hussar_gb300/csrc/hsr_traverse.cuh compiled with
+g++ through host definitions of the CUDA intrinsics (tests/native/host_shim.h), over a
+binary tree in the kernels' node layout; every closest-hit and any-hit answer is compared
+with brute force over all triangles (same triangle test and tie rule). Catches traversal
+logic errors without a GPU."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from hussar_gb300 import scenes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CUDA_INC = "/usr/local/cuda/include"
+
+
+@pytest.fixture(scope="module")
+def checker(tmp_path_factory):
+    if not os.path.exists(os.path.join(CUDA_INC, "cuda_runtime.h")) or shutil.which("g++") is None:
+        pytest.skip("needs g++ and the CUDA headers")
+    exe = str(tmp_path_factory.mktemp("trav") / "bvh_traverse_check")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "tests", "native"),
+                    "-I", os.path.join(ROOT, "hussar_gb300", "csrc"), "-I", CUDA_INC, "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "native", "bvh_traverse_check.cpp"),
+                    "-o", exe], check=True)
+    return exe
+
+
+def run(checker, tmp_path, mesh, rays, seed):
+    rng = np.random.default_rng(seed)
+    v = np.asarray(mesh.vertexBuffer, np.float32)
+    f = np.asarray(mesh.indexBuffer, np.int32)
+    lo, hi = v.min(0), v.max(0)
+    span = hi - lo
+    o = rng.uniform(lo - 0.1 * span, hi + 0.1 * span, (rays, 3)).astype(np.float32)
+    d = rng.normal(size=(rays, 3))
+    # a third of the rays are parallel to one or two axes (exact zero components)
+    third = rays // 3
+    d[:third, 0] = 0.0
+    d[third // 2:third, 2] = 0.0
+    d[third:third + third // 4] = [[0, -1, 0]]
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tf = rng.uniform(0, 2 * np.linalg.norm(span), rays).astype(np.float32)
+    path = tmp_path / ("in%d.bin" % seed)
+    with open(path, "wb") as fh:
+        fh.write(np.array([len(v), len(f), rays], np.int64).tobytes())
+        for a in (v, f, o, d, tf):
+            fh.write(np.ascontiguousarray(a).tobytes())
+    out = subprocess.run([checker, str(path)], check=True, capture_output=True, text=True).stdout.split()
+    res = {out[i]: float(out[i + 1]) for i in range(0, len(out), 2)}
+    print(res)
+    return res
+
+
+@pytest.mark.parametrize("name", ["dihedral", "sphere", "boxes"])
+def test_traversal_matches_brute_force(checker, tmp_path, name):
+    mesh = {"dihedral": lambda: scenes.dihedral_mesh(),
+            "sphere": lambda: scenes.sphere_ground_workload(level=3).mesh,
+            "boxes": lambda: scenes.boxes_mesh(seed=5, count=400, extent=30.0)}[name]()
+    res = run(checker, tmp_path, mesh, 3000, seed=len(name))
+    assert res["closest_mismatch"] == 0 and res["any_mismatch"] == 0
+    assert res["stack_status"] == 0
