@@ -46,7 +46,7 @@ if ROOT not in sys.path:
 METRIC = "paths/s"
 # DRAM bytes (read + write) of one trace launch, from the ncu capture summarised in
 # profiles/k_wave_sphere_ground_2p22.md (dram__bytes_read.sum + dram__bytes_write.sum)
-NCU_TRAFFIC = {"sphere": 3.899904e6 + 1.024e3}
+NCU_TRAFFIC = {"sphere": 6.085376e6 + 35.84e3}
 WORKLOAD = "icosphere-L6 (81,920 tris) + 20x20 m ground, sensor 10 m / 0.5 m, 3 bounces, 2^22 samples, N=512"
 
 
