@@ -89,11 +89,34 @@ class Frame:
         return self
 
     def argmax(self):
-        """radar.h:534-546: grid index (chirp, sample, channel) of the largest magnitude."""
-        i = int(np.argmax(np.abs(self.data.reshape(-1))))
+        """radar.h:534-546: grid index (chirp, sample, channel) of the first element with
+        the largest magnitude, the magnitude evaluated as std::abs(radar::complex) does
+        in single precision (complex.h:225-237: s * sqrt((x/s)^2 + (y/s)^2), s = max|.|)."""
+        i = int(np.argmax(complex_abs(self.data.reshape(-1))))
         return np.unravel_index(i, self.data.shape)
+
+    def fft(self):
+        """radar.h:412-435: in-place forward 3-D DFT of the cube (FFTW_FORWARD, unnormalised,
+        over chirps, samples and channels). Evaluated in FP64 and rounded to complex64
+        (the reference uses FFTW in single precision)."""
+        self.data = np.fft.fftn(self.data.astype(np.complex128), axes=(0, 1, 2)).astype(np.complex64)
 
     def tobytes(self):
         """Raw complex64 in [chirp][sample][channel] order, as writeFrameToFile writes it
         (examples/src/utils.h:29-35)."""
         return self.data.astype(np.complex64).tobytes()
+
+
+def complex_abs(z):
+    """std::abs(radar::complex<float>) (libradar/include/radar/complex.h:225-237),
+    elementwise in float32: the larger component scales both before the square root."""
+    z = np.asarray(z, np.complex64)
+    x = np.abs(z.real).astype(np.float32)
+    y = np.abs(z.imag).astype(np.float32)
+    s = np.maximum(x, y)
+    out = np.zeros(z.shape, np.float32)
+    nz = s != 0
+    xs = x[nz] / s[nz]
+    ys = y[nz] / s[nz]
+    out[nz] = s[nz] * np.sqrt(xs * xs + ys * ys)
+    return out
