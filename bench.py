@@ -392,10 +392,62 @@ def run_gb300(args, rank, world, local_rank, dist):
                          "sample": "%d Halton samples of pose 0 (%.1f s wall)" % (args.cpu_samples, cpu_s)},
         "modes": modes,
         "time_to_minus40db": time_to_error() if not args.no_tte else None,
+        "batch_graph": graph_overhead(torch, dev),
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
+
+
+def graph_overhead(torch, dev, reps=50):
+    """Per-batch device time of a small batch (the dihedral sweep, 91 poses x 2^12
+    samples) through hsr_simulate_batch_device and through its captured CUDA graph
+    (hsr_batch_graph_launch), CUDA events over `reps` back-to-back calls."""
+    import ctypes
+
+    from hussar_gb300 import PathTracer, _lib, gb300, scenes
+    L = _lib.lib()
+    w = scenes.dihedral_workload()
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    be = gb300.Backend(w.mesh, None)
+    P, N = len(w.tx), w.frame.samplesPerChirp
+    tx = (_lib.AntennaC * P)(*[a.to_c() for a in w.tx])
+    rx = (_lib.AntennaC * P)(*[a.to_c() for a in w.rx])
+    d_tx = torch.frombuffer(bytearray(bytes(tx)), dtype=torch.uint8).to(dev)
+    d_rx = torch.frombuffer(bytearray(bytes(rx)), dtype=torch.uint8).to(dev)
+    d_b = torch.full((P,), 1 << 12, dtype=torch.int64, device=dev)
+    d_o = torch.zeros(P, dtype=torch.int64, device=dev)
+    d_out = torch.zeros(2 * P * N, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    vp = ctypes.c_void_p
+    rf_c, fl_c = w.rf.to_c(), t.flags_c()
+
+    def direct():
+        _lib.check(L.hsr_simulate_batch_device(be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), P,
+                                               vp(d_tx.data_ptr()), vp(d_rx.data_ptr()), vp(d_b.data_ptr()),
+                                               vp(d_o.data_ptr()), _lib.HSR_PHASE_REFERENCE_FP32,
+                                               _lib.HSR_SPLAT_DIRICHLET16, vp(d_out.data_ptr()),
+                                               vp(stream.cuda_stream)))
+
+    g = be.batch_graph(w.rf, N, t, P, d_tx.data_ptr(), d_rx.data_ptr(), d_b.data_ptr(), d_o.data_ptr(),
+                       d_out.data_ptr())
+    out = {"workload": "dihedral, 91 poses x 2^12 samples", "reps": reps}
+    for name, fn in (("direct_us", direct), ("graph_us", lambda: g.launch(stream.cuda_stream))):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = 1000.0 * e0.elapsed_time(e1) / reps
+    g.status()
+    g.close()
+    return out
 
 
 TTE_TARGET = 1e-2  # -40 dB: relative L2 of the complex IF signal

@@ -186,6 +186,31 @@ def child_boxes(nodes):
     return lo, hi
 
 
+class BatchGraph:
+    """A captured plain batch (hsr_batch_graph_*); keeps its backend alive."""
+
+    def __init__(self, handle, backend):
+        self._h = handle
+        self._backend = backend
+
+    def launch(self, stream=None):
+        _lib.check(_lib.lib().hsr_batch_graph_launch(self._h, ctypes.c_void_p(stream)))
+
+    def status(self):
+        _lib.check(_lib.lib().hsr_batch_graph_status(self._h))
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            _lib.lib().hsr_batch_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _GB300:
     """Namespace mirroring hussar::gb300 (the drop-in for hussar::cpu / hussar::gpu)."""
 
@@ -316,6 +341,18 @@ class _GB300:
                 P, ctypes.cast(txa, ctypes.c_void_p), ctypes.cast(rxa, ctypes.c_void_p), _lib.ptr(b), _lib.ptr(off),
                 int(phase_mode), int(splat_mode), _lib.ptr(out), ctypes.c_void_p(stream)))
             return out
+
+        def batch_graph(self, rf, samples_per_chirp, integrator, pose_count, d_tx, d_rx, d_budget, d_offset,
+                        d_out_rows, phase_mode=_lib.HSR_PHASE_REFERENCE_FP32):
+            """The plain batch over device buffers (addresses as integers) captured into a
+            CUDA graph (hsr_batch_graph_create); BatchGraph.launch(stream) replays it."""
+            h = ctypes.c_void_p()
+            vp = ctypes.c_void_p
+            _lib.check(_lib.lib().hsr_batch_graph_create(
+                self._scene, ctypes.byref(rf.to_c()), int(samples_per_chirp), ctypes.byref(integrator.flags_c()),
+                int(pose_count), vp(d_tx), vp(d_rx), vp(d_budget), vp(d_offset), int(phase_mode), vp(d_out_rows),
+                ctypes.byref(h)))
+            return BatchGraph(h, self)
 
         def traversal_counts(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None):
             """Exact traversal work of one batch launch (counting instantiation):

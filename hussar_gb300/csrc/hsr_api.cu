@@ -4,6 +4,7 @@
 // crosses the ABI.
 #include <atomic>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -254,15 +255,22 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     }
     const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
     int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0));
-    cudaEventRecord(sc.ev0, st);
+    // timing events only outside stream capture (a captured graph must not record the
+    // scene's events: it may outlive them)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cap);
+    const bool timing = cap == cudaStreamCaptureStatusNone;
+    if (timing) cudaEventRecord(sc.ev0, st);
     std::string err;
     if (wave) {
         if (launch_wave(p, phase_mode, grid, st, err) != 0) return fail(HSR_ERR_CUDA, err);
     } else if (launch_trace(p, phase_mode, splat_mode, grid, st, err) != 0) {
         return fail(HSR_ERR_CUDA, err);
     }
-    cudaEventRecord(sc.ev1, st);
-    sc.timing_valid = true;
+    if (timing) {
+        cudaEventRecord(sc.ev1, st);
+        sc.timing_valid = true;
+    }
     return HSR_OK;
 }
 
@@ -911,6 +919,103 @@ hsr_status hsr_last_kernel_ms(const hsr_scene *s, float *out_ms) {
     if (e != cudaSuccess) return cuda_fail(e, "event sync");
     e = cudaEventElapsedTime(out_ms, s->dev.ev0, s->dev.ev1);
     if (e != cudaSuccess) return cuda_fail(e, "event elapsed");
+    return HSR_OK;
+}
+
+// ---- a plain batch captured into a CUDA graph ------------------------------------
+struct hsr_batch_graph {
+    hsr_scene *scene = nullptr;
+    void *scratch = nullptr;
+    unsigned *status = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+hsr_status hsr_batch_graph_create(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,
+                                  int32_t P, const hsr_antenna *d_tx, const hsr_antenna *d_rx,
+                                  const int64_t *d_budget, const int64_t *d_offset, int32_t phase_mode,
+                                  float *d_out_rows, hsr_batch_graph **out) {
+    if (!out) return fail(HSR_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    if (!s || !d_tx || !d_rx || !d_budget || !d_offset || !d_out_rows || P <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no poses");
+    hsr_status st = validate_common(rf, N, fl);
+    if (st != HSR_OK) return st;
+    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
+    if (fl->doGuiding)
+        return fail(HSR_ERR_NOT_SUPPORTED, "a batch graph runs the plain method (doGuiding must be 0)");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::unique_ptr<hsr_batch_graph> g(new hsr_batch_graph());
+    g->scene = s;
+    const Scratch need = carve(nullptr, P, N, false);
+    cudaError_t e = cudaMalloc(&g->scratch, need.bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "graph scratch allocation");
+    auto cleanup = [&]() {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        cudaFree(g->scratch);
+    };
+    if ((e = cudaMemset(g->scratch, 0, 256)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "graph scratch clear");
+    }
+    const Scratch sc = carve(g->scratch, P, N, false);
+    g->status = sc.counters;
+    cudaStream_t cs = nullptr;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "capture stream");
+    }
+    hsr_status rst = HSR_OK;
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        rst = cuda_fail(e, "begin capture");
+    } else {
+        rst = upload_poses(sc, P, d_tx, d_rx, d_budget, d_offset, cudaMemcpyDeviceToDevice, cs);
+        if (rst == HSR_OK)
+            rst = run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, HSR_SPLAT_DIRICHLET16, 1, d_out_rows, cs);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(cs, &graph);
+        g->graph = graph;
+        if (rst == HSR_OK && e != cudaSuccess) rst = cuda_fail(e, "end capture");
+        if (rst == HSR_OK && (e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+            rst = cuda_fail(e, "graph instantiation");
+    }
+    cudaStreamDestroy(cs);
+    if (rst != HSR_OK) {
+        cudaGetLastError();
+        cleanup();
+        return rst;
+    }
+    *out = g.release();
+    return HSR_OK;
+}
+
+hsr_status hsr_batch_graph_launch(hsr_batch_graph *g, void *stream) {
+    if (!g || !g->exec) return fail(HSR_ERR_INVALID_ARGUMENT, "null graph");
+    cudaError_t e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+    note_launches(1);
+    return HSR_OK;
+}
+
+hsr_status hsr_batch_graph_status(hsr_batch_graph *g) {
+    if (!g) return fail(HSR_ERR_INVALID_ARGUMENT, "null graph");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "graph synchronisation");
+    unsigned bits = 0;
+    if ((e = cudaMemcpy(&bits, g->status, sizeof(bits), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "graph status read");
+    if (bits) return fail(HSR_ERR_DEVICE, "a graph launch reported device status " + std::to_string(bits));
+    return HSR_OK;
+}
+
+hsr_status hsr_batch_graph_destroy(hsr_batch_graph *g) {
+    if (!g) return HSR_OK;
+    cudaDeviceSynchronize();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->scratch);
+    delete g;
     return HSR_OK;
 }
 

@@ -285,6 +285,29 @@ hsr_status hsr_set_synth_engine(int32_t engine);
  * trace kernel alone, measured with CUDA events on the launching stream. */
 hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);
 
+/* ---- A plain batch captured into a CUDA graph --------------------------------------
+ *
+ * No counterpart in the reference (its GPU backend launches one pose per call). Captures
+ * hsr_simulate_batch_device's plain method (doGuiding = 0, HSR_SPLAT_DIRICHLET16) for
+ * fixed device buffers once; every launch replays the whole batch (pose upload, work-item
+ * prefix, the persistent trace launch, fetchFrame rows) as one graph launch and reads the
+ * buffers' current contents, so poses, budgets and offsets may change between launches
+ * (the pose count, N, chirp and flags may not). The graph owns its scratch; it uses the
+ * scene's BVH, so destroy it before the scene. hsr_launch_count counts a graph launch as
+ * one launch. */
+typedef struct hsr_batch_graph hsr_batch_graph;
+
+hsr_status hsr_batch_graph_create(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
+                                  const hsr_tracer_flags *flags, int32_t pose_count, const hsr_antenna *d_tx,
+                                  const hsr_antenna *d_rx, const int64_t *d_budget,
+                                  const int64_t *d_index_offset, int32_t phase_mode, float *d_out_rows,
+                                  hsr_batch_graph **out_graph);
+/* Asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream). */
+hsr_status hsr_batch_graph_launch(hsr_batch_graph *graph, void *stream);
+/* Synchronises the device; HSR_ERR_DEVICE if any launch so far set the status word. */
+hsr_status hsr_batch_graph_status(hsr_batch_graph *graph);
+hsr_status hsr_batch_graph_destroy(hsr_batch_graph *graph);
+
 /* ---- Serving: continuous batching over resident scenes ------------------------------
  *
  * No counterpart in the reference, whose backends run one pose per synchronous call

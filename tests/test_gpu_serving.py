@@ -50,7 +50,7 @@ def make_requests(resident, count, seed):
         pi = int(rng.integers(0, len(w.tx)))
         budget = int(round(2.0 ** rng.uniform(10, 17)))
         if k in (5, 20, 33):
-            budget = (1 << 21) + 12345  # spans several ticks (not a whole number of tiles)
+            budget = (1 << 23) + 12345  # above the tick floor: spans several ticks (not whole tiles)
             si = k % 2  # on the two small scenes, to keep the test short
             w, _ = resident[si]
             pi = 0
