@@ -546,6 +546,69 @@ def time_to_error(max_log2=26):
     return out
 
 
+def run_urban_mimo(args, rank, world, local_rank, dist):
+    """The guided urban MIMO configuration (scenes.urban_mimo_workload): 12 virtual
+    channels of one pose traced as one guided batch (PathTracer::run's doubling schedule,
+    2^22 samples per channel: 8 iterations), split-FP64 phase, up to 5 bounces; each step
+    also assembles the 128 x 256 x 12 frame on the device (zero velocity: every chirp row
+    is the first) and reads it back. Replicas under torchrun."""
+    import torch
+
+    from hussar_gb300 import HSR_PHASE_SPLIT_FP64, PathTracer, _lib, gb300, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    L = _lib.lib()
+    w = scenes.urban_mimo_workload()
+    be = gb300.Backend(w.mesh, None)
+    P, N, C = len(w.tx), w.frame.samplesPerChirp, w.frame.chirpCount
+    off = np.array([replica_range(rank, int(b))[0] for b in w.budget], np.int64)
+    res = {}
+    for name, guided in (("guided", True), ("plain", False)):
+        t = PathTracer()
+        t.doGuiding = guided
+        t.maxDepth = w.max_depth
+
+        def step():
+            rows = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, index_offset=off,
+                                     phase_mode=HSR_PHASE_SPLIT_FP64)
+            d = torch.from_numpy(rows.view(np.float32)).to(dev).view(P, N, 2)
+            frame = d.permute(1, 0, 2).unsqueeze(0).expand(C, N, P, 2).contiguous()  # [chirp][sample][channel]
+            return frame.cpu()
+
+        for _ in range(max(args.warmup, 3) if guided else 1):
+            step()
+        barrier(dist)
+        times = []
+        n0 = L.hsr_launch_count()
+        steps = args.steps if guided else 2
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            frame = step()
+            times.append(time.perf_counter() - t0)
+        ms = max_over_ranks(dist, 1000.0 * float(np.median(times)))
+        res[name] = {"ms_per_step": ms, "paths_per_s": world * float(w.budget.sum()) / (ms / 1000.0),
+                     "library_launches_per_step": (L.hsr_launch_count() - n0) / steps}
+    if rank != 0:
+        return
+    g = res["guided"]
+    line = {
+        "metric": METRIC, "value": g["paths_per_s"], "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": g["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "urban canyon %d triangles, 3 TX x 4 RX at lambda/2 (12 channels), %d chirps x %d "
+                               "samples, guided (8 doubling iterations, 2^22 samples per channel), 5 bounces, "
+                               "split FP64 phase" % (w.mesh.triangleCount(), C, N),
+                   "frame_shape": [C, N, P], "l2": "inputs larger than L2 (%.0f MB scene)" % (be.footprint() / 1e6)},
+        "e2e": {"value": g["paths_per_s"], "unit": "paths/s", "h2d_bytes_per_step": int(P * (96 + 16)),
+                "d2h_bytes_per_step": int(C * N * P * 8),
+                "note": "wall clock through hsr_simulate_batch plus the frame assembly and read-back"},
+        "modes": {"plain_same_budget": res["plain"]},
+        "gpu_launches": int(round(g["library_launches_per_step"] * args.steps)),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args, rank, world, local_rank, dist):
     """The serving workload (see the module docstring); replicas under torchrun: every rank
     serves its own request stream."""
@@ -652,7 +715,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve", "tte"])
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve", "tte", "urban_mimo"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
@@ -670,6 +733,8 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "serve":
         run_serve(args, rank, world, local_rank, dist)
+    elif args.workload == "urban_mimo":
+        run_urban_mimo(args, rank, world, local_rank, dist)
     elif args.workload == "tte":
         if rank == 0:
             import torch

@@ -7,7 +7,7 @@
 //   4. triangle records written in sorted order (k_write_tris)
 //   5. topology, one of:
 //      PLOC (default): parallel locally-ordered clustering over the Morton order
-//        (Meister and Bittner 2018): every cluster finds, within +-16 positions, the
+//        (Meister and Bittner 2018): every cluster finds, within +-256 positions, the
 //        neighbour whose merged box has the smallest surface area; mutual nearest pairs
 //        merge; survivors are compacted in order; repeat until one cluster is left.
 //        Surface-area-driven like an SAH build, robust to large overlapping triangles.
@@ -225,7 +225,7 @@ __global__ void k_leaf_depth(int64_t n, const int32_t *__restrict__ parent_inter
 }
 
 // ---------------- PLOC ----------------
-constexpr int kPlocRadius = 16;
+constexpr int kPlocRadius = 256;
 
 struct Cluster {
     int id;       // node encoding: >= 0 internal node, < 0 leaf slot (~slot)

@@ -266,3 +266,35 @@ def serve_scene(kind, tris, seed):
         extent = 100.0 * np.sqrt(count / 83334.0)
         return boxes_mesh(seed, count, extent), (lambda n, s: plane_poses(n, s, extent))
     return urban_mesh(tris, seed), (lambda n, s: street_poses(n, s))
+
+
+def mimo_array(position, yaw, n_tx=3, n_rx=4, start_freq=77e9):
+    """TX and RX antennas of a MIMO radar at `position` looking along `yaw`: RX elements
+    half a wavelength (at `start_freq`) apart along the array's horizontal axis, TX
+    elements n_rx half-wavelengths apart, so the n_tx x n_rx (TX, RX) pairs form a
+    uniform virtual array of half-wavelength spacing. Returns (tx list, rx list)."""
+    half = 299792458.0 / start_freq / 2.0
+    R = looking(yaw).astype(np.float64)
+    axis = R[:, 0]  # horizontal, perpendicular to the boresight R[:, 2]
+    p = np.asarray(position, np.float64)
+    tx = [NFAntenna((p + axis * (i * n_rx * half)).astype(np.float32), R.astype(np.float32)) for i in range(n_tx)]
+    rx = [NFAntenna((p + axis * (j * half)).astype(np.float32), R.astype(np.float32)) for j in range(n_rx)]
+    return tx, rx
+
+
+def urban_mimo_workload(tris=5_000_000, seed=0xC4, samples=1 << 22, chirps=128):
+    """The guided urban MIMO configuration: the urban canyon (about `tris` triangles),
+    one sensor on a street at 1 m with a 3 TX x 4 RX array at half-wavelength spacing
+    (12 virtual channels, each a (TX, RX) pose of one batch), 77-81 GHz, 256 samples per
+    chirp, `chirps` chirps per frame, up to 5 bounces; `samples` per channel."""
+    mesh = urban_mesh(tris, seed)
+    rng = np.random.default_rng(seed + 7)
+    pose = street_poses(1, seed + 9)[0]
+    yaw = float(rng.uniform(0, 2 * np.pi))
+    txs, rxs = mimo_array(pose.position(), yaw)
+    tx = [t for t in txs for _ in rxs]
+    rx = [r for _ in txs for r in rxs]
+    rf, _ = rf_77ghz(256)
+    fc = FrameConfig(chirps, 256, len(tx))
+    return Workload("urban-%dk-mimo3x4" % (tris // 1000), mesh, rf, fc, tx, rx,
+                    np.full(len(tx), samples, np.int64), 5)
