@@ -147,6 +147,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def l2_read_gbs(mib=32, sweeps=64):
+    """Read bandwidth of an L2-resident `mib` MiB buffer (hsr_measure_l2_read: one launch
+    of `sweeps` L2-cached passes, best of five): the L2 denominator for traversal, whose
+    working set mostly stays in L2 (MEASURED_PEAKS.json holds HBM and tensor peaks)."""
+    import ctypes
+
+    from hussar_gb300 import _lib
+    out = ctypes.c_double()
+    _lib.check(_lib.lib().hsr_measure_l2_read(mib << 20, sweeps, ctypes.byref(out)))
+    return out.value
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -372,6 +384,7 @@ def run_gb300(args, rank, world, local_rank, dist):
     alg_bytes = counts["bytes"] * scale
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (trace_ms / 1000.0) / 1e9
+    l2_gbs = l2_read_gbs()
     cpu_val, cpu_cores, cpu_s = cpu_baseline(w, t, args.cpu_samples)
     line = {
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
@@ -387,7 +400,8 @@ def run_gb300(args, rank, world, local_rank, dist):
                      "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get(args.workload),
                      "kernel": "k_wave",
                      "kernel_ms": trace_ms, "algorithmic_bytes": alg_bytes, "rays": counts["rays"] * scale,
-                     "nodes": counts["nodes"] * scale, "tris": counts["tris"] * scale, "peak_source": peak_kind},
+                     "nodes": counts["nodes"] * scale, "tris": counts["tris"] * scale, "peak_source": peak_kind,
+                     "l2_read_gbs": l2_gbs, "frac_of_l2_read": achieved / l2_gbs},
         "cpu_baseline": {"value": cpu_val, "unit": "paths/s", "cores": cpu_cores, "kind": "port",
                          "sample": "%d Halton samples of pose 0 (%.1f s wall)" % (args.cpu_samples, cpu_s)},
         "modes": modes,
@@ -609,6 +623,87 @@ def run_urban_mimo(args, rank, world, local_rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_synth(args, rank, world, local_rank, dist):
+    """The synthesis GEMM at batch scale: the 91 dihedral poses repeated to --poses (2048
+    by default), 2^12 samples each, N = 256, HSR_SPLAT_FINE_SYNTH through
+    hsr_simulate_batch_device; the step time minus the trace kernel's time is the
+    synthesis (split of the histogram, tcgen05 GEMM, rows). Replicas under torchrun."""
+    import ctypes
+
+    import torch
+
+    from hussar_gb300 import PathTracer, _lib, gb300, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    L = _lib.lib()
+    P = args.poses or 2048
+    w = scenes.dihedral_workload()
+    idx = np.arange(P) % len(w.tx)
+    w.tx, w.rx = [w.tx[i] for i in idx], [w.rx[i] for i in idx]
+    w.budget = np.full(P, 1 << 12, np.int64)
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    be = gb300.Backend(w.mesh, None)
+    B = DeviceBatch(w, dev, rank, torch, _lib)
+    N = B.N
+    stream = torch.cuda.current_stream(dev)
+    rf_c, fl_c = w.rf.to_c(), t.flags_c()
+    vp = ctypes.c_void_p
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def step(splat):
+        _lib.check(L.hsr_simulate_batch_device(
+            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), P, vp(B.d_tx.data_ptr()), vp(B.d_rx.data_ptr()),
+            vp(B.d_budget.data_ptr()), vp(B.d_offset.data_ptr()), _lib.HSR_PHASE_REFERENCE_FP32, splat,
+            vp(B.d_rows.data_ptr()), vp(stream.cuda_stream)))
+
+    res = {}
+    for name, splat in (("fine_synth", _lib.HSR_SPLAT_FINE_SYNTH), ("dirichlet16", _lib.HSR_SPLAT_DIRICHLET16)):
+        for _ in range(max(args.warmup, 3)):
+            step(splat)
+        ms, trace = [], []
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(splat)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            kms = ctypes.c_float()
+            _lib.check(L.hsr_last_kernel_ms(be.handle, ctypes.byref(kms)))
+            trace.append(kms.value)
+        res[name] = {"ms_per_step": max_over_ranks(dist, float(np.median(ms))), "trace_ms": float(np.median(trace))}
+    if rank != 0:
+        return
+    f = res["fine_synth"]
+    synth_ms = max(f["ms_per_step"] - f["trace_ms"], 1e-6)
+    useful = 8.0 * P * (32 * N) * N  # complex [P x 32N] x [32N x N] in real flops
+    executed = 6 * 2.0 * P * (64 * N) * (2 * N)  # six BF16 products of the real [P x 64N] x [64N x 2N]
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tc = peaks.get("bf16_tflops", 1900.0)
+    line = {
+        "metric": METRIC, "value": world * float(B.paths) / (f["ms_per_step"] / 1000.0), "unit": "paths/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": f["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "dihedral poses repeated to %d, 2^12 samples each, N=%d, fine-histogram synthesis"
+                               % (P, N), "l2": "flushed between steps (512 MiB write)"},
+        "roofline": {"bound": "tensor", "kernel": "synthesis (k_split3 + k_umma_gemm + rows)",
+                     "achieved": useful / (synth_ms / 1000.0) / 1e12, "peak": tc, "unit": "TFLOP/s",
+                     "frac": useful / (synth_ms / 1000.0) / 1e12 / tc, "traffic": None,
+                     "executed_bf16_tflops": executed / (synth_ms / 1000.0) / 1e12, "synthesis_ms": synth_ms,
+                     "note": "useful = the complex product's flops; the six BF16 split products execute 6x "
+                             "the real product"},
+        "modes": res,
+        "e2e": None,
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args, rank, world, local_rank, dist):
     """The serving workload (see the module docstring); replicas under torchrun: every rank
     serves its own request stream."""
@@ -715,7 +810,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--workload", default="sphere", choices=["sphere", "boxes", "serve", "tte", "urban_mimo"])
+    ap.add_argument("--workload", default="sphere",
+                    choices=["sphere", "boxes", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
@@ -733,6 +829,8 @@ def main():
         run_reference(args, rank, world, dist)
     elif args.workload == "serve":
         run_serve(args, rank, world, local_rank, dist)
+    elif args.workload == "synth":
+        run_synth(args, rank, world, local_rank, dist)
     elif args.workload == "urban_mimo":
         run_urban_mimo(args, rank, world, local_rank, dist)
     elif args.workload == "tte":

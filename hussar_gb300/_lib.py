@@ -148,6 +148,7 @@ def lib():
         "hsr_server_destroy": [vp],
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
+        "hsr_measure_l2_read": [ctypes.c_int64, ctypes.c_int32, P(ctypes.c_double)],
         "hsr_batch_graph_create": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                    ctypes.c_int32, vp, P(vp)],
         "hsr_batch_graph_launch": [vp, vp],

@@ -922,6 +922,62 @@ hsr_status hsr_last_kernel_ms(const hsr_scene *s, float *out_ms) {
     return HSR_OK;
 }
 
+// ---- measurement support: L2 read bandwidth ----------------------------------------
+namespace {
+// Every thread sweeps its share of an L2-resident buffer `sweeps` times with L2-cached
+// (not L1) loads; the checksum keeps the loads.
+__global__ void k_l2_read(const float4 *__restrict__ buf, int64_t n4, int sweeps, float *sink) {
+    float acc = 0.f;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int s = 0; s < sweeps; ++s)
+        for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += stride) {
+            const float4 v = __ldcg(buf + i);
+            acc += (v.x + v.y) + (v.z + v.w);
+        }
+    if (acc == 1234567.f) sink[0] = acc;
+}
+}  // namespace
+
+hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs) {
+    if (!out_gbs || bytes < (1 << 20) || sweeps < 1) return fail(HSR_ERR_INVALID_ARGUMENT, "bad L2 measurement size");
+    hsr_status st = check_device();
+    if (st != HSR_OK) return st;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t n4 = bytes / 16;
+    float4 *buf = nullptr;
+    float *sink = nullptr;
+    std::string err;
+    if (!dev_alloc(&buf, size_t(n4) * 16, err) || !dev_alloc(&sink, 16, err)) {
+        cudaFree(buf);
+        return fail(HSR_ERR_OUT_OF_MEMORY, err);
+    }
+    cudaMemset(buf, 0, size_t(n4) * 16);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int r = 0; r < 6; ++r) {  // the first run warms L2 and is not counted
+        cudaEventRecord(e0);
+        k_l2_read<<<sms * 8, 256>>>(buf, n4, sweeps, sink);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    note_launches(6);
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(e, "L2 read kernel");
+    *out_gbs = double(n4) * 16.0 * sweeps / (double(best) / 1000.0) / 1e9;
+    return HSR_OK;
+}
+
 // ---- a plain batch captured into a CUDA graph ------------------------------------
 struct hsr_batch_graph {
     hsr_scene *scene = nullptr;

@@ -258,6 +258,11 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *scene, const hsr_rf_config *rf,
                                       const hsr_antenna *rx, const int64_t *budget,
                                       const int64_t *index_offset, int64_t *out_counts);
 
+/* Measurement support: read bandwidth of an L2-resident buffer of `bytes` (L2-cached
+ * loads, `sweeps` passes in one launch, best of five launches, CUDA events), the L2
+ * denominator of the traversal roofline. Synchronous. */
+hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs);
+
 /* Copies the scene's device BVH to the host (tests): out_nodes receives node_count binary
  * nodes of 64 bytes each, both child boxes and child references (layout in
  * hussar_gb300/csrc/hsr_common.cuh, struct DNode; a negative reference c is triangle slot
