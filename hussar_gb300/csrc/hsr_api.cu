@@ -461,7 +461,6 @@ static hsr_status read_status(const Scratch &s, cudaStream_t st) {
         if (bits & kStatusBadBin) m += " bin-out-of-range";
         if (bits & kStatusBadWorkItem) m += " bad-work-item";
         if (bits & (1u << 3)) m += " synthesis-wait-timeout";
-        if (bits & kStatusSyncTimeout) m += " wavefront-sync-timeout";
         return fail(HSR_ERR_DEVICE, m);
     }
     return HSR_OK;

@@ -21,7 +21,6 @@ enum StatusBits : unsigned {
     kStatusBadBin = 1u << 1,          // a splat bin was outside the frame (guarded, skipped)
     kStatusBadWorkItem = 1u << 2,     // work item index out of range (guarded)
     // bit 3: a synthesis GEMM wait gave up (hsr_synth.cu)
-    kStatusSyncTimeout = 1u << 4,     // a wavefront CTA sync point gave up waiting (kernel returned)
 };
 
 struct f3 {
