@@ -88,6 +88,11 @@ class ServerStatsC(ctypes.Structure):
                [(n, ctypes.c_int64) for n in ("admitted_while_busy", "memory_bytes_peak", "scene_bytes")]
 
 
+class LaunchConfigC(ctypes.Structure):
+    _fields_ = [("tile", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("queue_threshold", ctypes.c_int32),
+                ("trace_ms", ctypes.c_float), ("default_trace_ms", ctypes.c_float)]
+
+
 # PathRecord in hsr_trace.cu / hsr_debug_records
 RECORD_DTYPE = [("depth", "<i4"), ("splatted", "<i4"), ("time", "<f4"), ("v_re", "<f4"), ("v_im", "<f4"),
                 ("dphase", "<f4"), ("bin", "<f4"), ("value_re", "<f4"), ("value_im", "<f4")]
@@ -148,6 +153,10 @@ def lib():
         "hsr_server_destroy": [vp],
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
+        "hsr_autotune_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
+                               ctypes.c_int32, ctypes.c_int32, P(LaunchConfigC)],
+        "hsr_set_launch_config": [vp, P(LaunchConfigC)],
+        "hsr_get_launch_config": [vp, P(LaunchConfigC)],
         "hsr_measure_l2_read": [ctypes.c_int64, ctypes.c_int32, P(ctypes.c_double)],
         "hsr_batch_graph_create": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                    ctypes.c_int32, vp, P(vp)],

@@ -354,6 +354,27 @@ class _GB300:
                 ctypes.byref(h)))
             return BatchGraph(h, self)
 
+        def autotune(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None,
+                     phase_mode=_lib.HSR_PHASE_REFERENCE_FP32, splat_mode=_lib.HSR_SPLAT_DIRICHLET16):
+            """hsr_autotune_batch: times this batch under candidate launch shapes, keeps the
+            fastest for later plain runs on this scene and returns it as a dict."""
+            P = len(tx)
+            txa = (_lib.AntennaC * P)(*[a.to_c() for a in tx])
+            rxa = (_lib.AntennaC * P)(*[a.to_c() for a in rx])
+            b = np.ascontiguousarray(budget, np.int64)
+            off = np.zeros(P, np.int64) if index_offset is None else np.ascontiguousarray(index_offset, np.int64)
+            out = _lib.LaunchConfigC()
+            _lib.check(_lib.lib().hsr_autotune_batch(
+                self._scene, ctypes.byref(rf.to_c()), int(samples_per_chirp), ctypes.byref(integrator.flags_c()), P,
+                ctypes.cast(txa, ctypes.c_void_p), ctypes.cast(rxa, ctypes.c_void_p), _lib.ptr(b), _lib.ptr(off),
+                int(phase_mode), int(splat_mode), ctypes.byref(out)))
+            return {name: getattr(out, name) for name, _ in _lib.LaunchConfigC._fields_}
+
+        def set_launch_config(self, tile=0, ctas_per_sm=0, queue_threshold=0, default=False):
+            """Sets the scene's launch shape (default=True: back to the default shape)."""
+            c = _lib.LaunchConfigC(int(tile), int(ctas_per_sm), int(queue_threshold), 0.0, 0.0)
+            _lib.check(_lib.lib().hsr_set_launch_config(self._scene, None if default else ctypes.byref(c)))
+
         def traversal_counts(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None):
             """Exact traversal work of one batch launch (counting instantiation):
             dict(nodes, tris, rays, bytes) with 64 B per BVH node and 48 B per triangle."""

@@ -209,13 +209,16 @@ static hsr_status ensure_guide(SceneDev &sc, int P, GuideMem &out) {
 static constexpr int32_t kTile = 4096;  // samples per work item
 
 // One trace launch over the poses' current budgets/offsets/weights in scratch.
-// `tile` (a power of two, 256 .. kTile) is the samples per work item: smaller tiles keep
-// the SMs busy when a pass has few samples (the early guided iterations).
+// `tile` is the samples per work item: 0 takes the scene's autotuned tile (or kTile);
+// the guided iterations pass their own (smaller tiles keep the SMs busy when a pass has
+// few samples). The autotuned CTAs per SM and queue threshold apply to plain passes.
 static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_config *rf, int32_t N,
                                const hsr_tracer_flags *fl, int32_t P, float sample_weight, bool per_pose_weights,
                                int32_t phase_mode, int32_t splat_mode, cudaStream_t st, const GuideMem *g,
                                void *records = nullptr, int max_rec = 0, unsigned long long *counters = nullptr,
-                               int32_t tile = kTile) {
+                               int32_t tile = 0) {
+    const bool tuned = tile == 0 && !fl->doGuiding;
+    if (tile == 0) tile = (tuned && sc.tuned.tile > 0) ? sc.tuned.tile : kTile;
     cudaError_t e;
     if ((e = cudaMemsetAsync(s.counters + 2, 0, 8, st)) != cudaSuccess) return cuda_fail(e, "memset counter");
     if (launch_tile_prefix(s.budget, P, tile, s.tile_start, st) != 0)
@@ -254,7 +257,12 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
         p.flags.doGuiding = 0;
     }
     const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
-    int grid = sc.sm_count * (wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0));
+    int per_sm = wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0);
+    if (wave && tuned) {
+        if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);
+        p.queue_threshold = sc.tuned.queue_threshold;
+    }
+    int grid = sc.sm_count * per_sm;
     // timing events only outside stream capture (a captured graph must not record the
     // scene's events: it may outlive them)
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -860,6 +868,112 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         return cuda_fail(e, "row download");
     if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "batch run");
     return read_status(sc, strm);
+}
+
+// ---- autotuning of the plain wavefront launch --------------------------------------
+// Times the trace kernel (CUDA events) of the caller's batch under each candidate
+// launch shape and keeps the fastest on the scene. Coordinate search: the work-item tile,
+// then CTAs per SM, then the queue threshold; every trial runs twice, the faster counts.
+// The candidates change only the grouping of sums, not the samples: rows agree with the
+// default shape up to FP32/FP64 summation order.
+hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl, int32_t P,
+                              const hsr_antenna *tx, const hsr_antenna *rx, const int64_t *budget,
+                              const int64_t *offset, int32_t phase_mode, int32_t splat_mode,
+                              hsr_launch_config *out_best) {
+    if (!s || !tx || !rx || !budget || !offset || !out_best || P <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no poses");
+    hsr_status st = validate_common(rf, N, fl);
+    if (st != HSR_OK) return st;
+    if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
+    if (fl->doGuiding || !fl->useGeometricalOptics)
+        return fail(HSR_ERR_NOT_SUPPORTED, "the autotuner tunes the plain wavefront launch (GO mode, no guiding)");
+    for (int32_t i = 0; i < P; ++i)
+        if (budget[i] < 0 || offset[i] < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
+    std::lock_guard<std::mutex> lk(s->mu);
+    SceneDev &d = s->dev;
+    Scratch sc;
+    if ((st = ensure_scratch(d, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
+    if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, nullptr)) != HSR_OK) return st;
+    const LaunchConfig saved = d.tuned;
+    auto trial = [&](const LaunchConfig &c, float &ms) -> hsr_status {
+        d.tuned = c;
+        ms = 1e30f;
+        for (int r = 0; r < 2; ++r) {
+            hsr_status rs = run_plain(d, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, sc.rows, nullptr);
+            if (rs != HSR_OK) return rs;
+            cudaError_t e = cudaEventSynchronize(d.ev1);
+            if (e != cudaSuccess) return cuda_fail(e, "autotune trial");
+            float t = 0.f;
+            cudaEventElapsedTime(&t, d.ev0, d.ev1);
+            ms = std::min(ms, t);
+        }
+        return read_status(sc, nullptr);
+    };
+    LaunchConfig best;  // the default shape
+    float best_ms = 0.f, ms = 0.f;
+    if ((st = trial(best, best_ms)) != HSR_OK) {
+        d.tuned = saved;
+        return st;
+    }
+    const float default_ms = best_ms;
+    const int32_t tiles[] = {1024, 2048, 4096, 8192, 16384};
+    const int32_t ctas[] = {2, 3, 4};
+    const int32_t thresholds[] = {32, 64, kWaveMaxQueueThreshold};
+    for (int32_t t : tiles) {
+        LaunchConfig c = best;
+        c.tile = t;
+        if ((st = trial(c, ms)) != HSR_OK) break;
+        if (ms < best_ms) best_ms = ms, best = c;
+    }
+    for (int32_t k = 0; st == HSR_OK && k < 3; ++k) {
+        LaunchConfig c = best;
+        c.ctas_per_sm = ctas[k];
+        if ((st = trial(c, ms)) != HSR_OK) break;
+        if (ms < best_ms) best_ms = ms, best = c;
+    }
+    for (int32_t k = 0; st == HSR_OK && k < 3; ++k) {
+        LaunchConfig c = best;
+        c.queue_threshold = thresholds[k];
+        if ((st = trial(c, ms)) != HSR_OK) break;
+        if (ms < best_ms) best_ms = ms, best = c;
+    }
+    if (st != HSR_OK) {
+        d.tuned = saved;
+        return st;
+    }
+    d.tuned = best;
+    out_best->tile = best.tile > 0 ? best.tile : kTile;
+    out_best->ctas_per_sm = best.ctas_per_sm;
+    out_best->queue_threshold = best.queue_threshold > 0 ? best.queue_threshold : kWaveMaxQueueThreshold;
+    out_best->trace_ms = best_ms;
+    out_best->default_trace_ms = default_ms;
+    return HSR_OK;
+}
+
+hsr_status hsr_set_launch_config(hsr_scene *s, const hsr_launch_config *c) {
+    if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    LaunchConfig l;
+    if (c) {
+        if (c->tile < 0 || (c->tile > 0 && (c->tile < 32 || c->tile > (1 << 20))) || c->ctas_per_sm < 0 ||
+            c->ctas_per_sm > 32 || c->queue_threshold < 0 || c->queue_threshold > kWaveMaxQueueThreshold)
+            return fail(HSR_ERR_INVALID_ARGUMENT, "launch config out of range");
+        l.tile = c->tile;
+        l.ctas_per_sm = c->ctas_per_sm;
+        l.queue_threshold = c->queue_threshold;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->dev.tuned = l;  // null: back to the default shape
+    return HSR_OK;
+}
+
+hsr_status hsr_get_launch_config(const hsr_scene *s, hsr_launch_config *out) {
+    if (!s || !out) return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    out->tile = s->dev.tuned.tile;
+    out->ctas_per_sm = s->dev.tuned.ctas_per_sm;
+    out->queue_threshold = s->dev.tuned.queue_threshold;
+    out->trace_ms = 0.f;
+    out->default_trace_ms = 0.f;
+    return HSR_OK;
 }
 
 hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,

@@ -26,6 +26,14 @@ struct SynthOperand {
     void *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;  // its three BF16 terms
 };
 
+// Launch shape of the plain wavefront pass chosen by the autotuner (0 fields: default).
+struct LaunchConfig {
+    int32_t tile = 0;             // samples per work item
+    int32_t ctas_per_sm = 0;      // persistent grid: SMs x this (<= the occupancy limit)
+    int32_t queue_threshold = 0;  // see TraceParams::queue_threshold
+};
+constexpr int kWaveMaxQueueThreshold = 128;  // the wavefront CTA's 384-entry stack minus 256
+
 // A resident scene: triangles + BVH on the device, plus per-scene scratch reused by
 // every simulate call on this scene (calls on one scene must not overlap).
 struct SceneDev {
@@ -46,6 +54,7 @@ struct SceneDev {
     void *synth_scratch = nullptr;
     size_t synth_scratch_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    LaunchConfig tuned;  // set by hsr_autotune_batch / hsr_set_launch_config
     float last_kernel_ms = 0.f;
     bool timing_valid = false;
     int sm_count = 0;
@@ -119,7 +128,11 @@ struct TraceParams {
     // mixed batch: per-pose scene/chirp/row (nodes, tris, rf and acc rows above are then
     // unused; samples is the largest N); nullptr: uniform batch. Wavefront kernel only.
     const PoseJob *jobs;
+    // wavefront kernel: GENERATE runs while a CTA holds at most this many live paths
+    // (<= kWaveStack - 256; 0: that maximum)
+    int32_t queue_threshold;
 };
+
 
 size_t guide_bytes_per_pose();
 int launch_guide_reset(int P, int *samp_child, float *samp_p, int *train_child, float *train_acc, int *train_count,

@@ -5,7 +5,8 @@
 // A persistent CTA of 256 threads keeps a stack of up to 384 live path states in
 // shared memory (four CTAs per SM: 64 registers, ~46 KB of shared memory each) and
 // alternates two stages:
-//   GENERATE  (at most 128 live paths): 256 new samples, one per thread: Halton point,
+//   GENERATE  (at most 128 live paths, or the autotuned queue threshold): 256 new
+//             samples, one per thread: Halton point,
 //             antenna ray, closest hit; paths that hit something are pushed.
 //   EXTEND    (otherwise): 256 paths popped, one per thread: specular reflection,
 //             next-event estimate towards RX (shadow ray, PO re-radiation, filtering,
@@ -134,6 +135,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
 #define HSR_MAXDIST (kMixed ? S.max_dist : maxDist0)
 #define HSR_BANDWIDTH (kMixed ? S.bandwidth : bandwidth0)
     const long long total = __ldg(&p.tile_start[p.pose_count]);
+    static_assert(kStack - kThreads == kWaveMaxQueueThreshold, "queue threshold bound");
+    const int queue_threshold = (p.queue_threshold > 0 && p.queue_threshold < kStack - kThreads)
+                                    ? p.queue_threshold : kStack - kThreads;
 
     for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
     if (p.do_guide)
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             continue;
         }
 
-        if (gen < gen_end && count <= kStack - kThreads) {
+        if (gen < gen_end && count <= queue_threshold) {
             // ---------------- GENERATE ----------------
             if (tid == 0) {
                 S.gen = min(gen + (long long)kThreads, gen_end);

@@ -271,6 +271,29 @@ hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs);
 hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_capacity, void *out_tris,
                          int64_t tri_capacity);
 
+/* ---- Autotuning of the plain wavefront launch ---------------------------------------
+ * No counterpart in the reference. The launch shape of a plain batch: samples per work
+ * item (tile), persistent CTAs per SM, and the queue threshold (GENERATE runs while a CTA
+ * holds at most this many live paths; at most 128). Zero fields mean the default shape.
+ * The shape changes the grouping of sums, not the samples traced. */
+typedef struct hsr_launch_config {
+    int32_t tile;
+    int32_t ctas_per_sm;
+    int32_t queue_threshold;
+    float trace_ms;          /* hsr_autotune_batch: the chosen shape's trace-kernel time */
+    float default_trace_ms;  /* and the default shape's, on the same batch */
+} hsr_launch_config;
+
+/* Runs the given batch (host arrays, as hsr_simulate_batch; plain GO mode) under
+ * candidate shapes, keeps the fastest for later plain runs on this scene and returns it. */
+hsr_status hsr_autotune_batch(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
+                              const hsr_tracer_flags *flags, int32_t pose_count, const hsr_antenna *tx,
+                              const hsr_antenna *rx, const int64_t *budget, const int64_t *index_offset,
+                              int32_t phase_mode, int32_t splat_mode, hsr_launch_config *out_best);
+/* Sets the scene's launch shape (NULL: the default). */
+hsr_status hsr_set_launch_config(hsr_scene *scene, const hsr_launch_config *config);
+hsr_status hsr_get_launch_config(const hsr_scene *scene, hsr_launch_config *out);
+
 /* Which trace kernel the simulate calls use (process-wide): 0 (default) = the wavefront
  * kernel whenever geometrical optics is on, 1 = always the one-thread-per-sample kernel.
  * Both compute the same per-path values; tests use this to check each one. */

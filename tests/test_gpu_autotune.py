@@ -1,0 +1,38 @@
+"""The launch-shape autotuner (hsr_autotune_batch): it times the caller's batch under
+candidate shapes (work-item tile, CTAs per SM, queue threshold) and keeps the fastest.
+A shape changes only the grouping of sums, so rows agree with the default shape up to
+summation order (1e-5 relative L2)."""
+import numpy as np
+import pytest
+
+from hussar_gb300 import PathTracer, gb300, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_autotune_picks_a_valid_shape_and_keeps_results(product_lib):
+    w = scenes.sphere_ground_workload(samples=1 << 20, level=5)
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    be = gb300.Backend(w.mesh, None)
+    N = w.frame.samplesPerChirp
+    ref = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
+    best = be.autotune(w.rf, N, t, w.tx, w.rx, w.budget)
+    print("autotuned", best)
+    assert best["tile"] in (1024, 2048, 4096, 8192, 16384)
+    assert best["ctas_per_sm"] in (0, 2, 3, 4) and 1 <= best["queue_threshold"] <= 128
+    assert 0 < best["trace_ms"] <= best["default_trace_ms"]
+    tuned = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
+    assert rel_l2(tuned, ref) <= 1e-5
+    # an explicit odd shape gives the same rows too, and the default can be restored
+    be.set_launch_config(tile=1024, ctas_per_sm=2, queue_threshold=32)
+    assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5
+    be.set_launch_config(default=True)
+    assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5

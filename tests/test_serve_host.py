@@ -67,6 +67,7 @@ int main(void) {
     S(hsr_server_stats); F(hsr_server_stats, device_ms); F(hsr_server_stats, max_batch);
     F(hsr_server_stats, admitted_while_busy); F(hsr_server_stats, scene_bytes);
     S(hsr_tracer_flags); S(hsr_antenna); S(hsr_rf_config);
+    S(hsr_launch_config); F(hsr_launch_config, queue_threshold); F(hsr_launch_config, default_trace_ms);
     return 0;
 }
 """
@@ -83,7 +84,8 @@ def test_ctypes_mirrors_match_c_layout(tmp_path):
     c = dict(line.rsplit(" ", 1) for line in out if line)
     mirrors = {"hsr_server_config": _lib.ServerConfigC, "hsr_request": _lib.RequestC,
                "hsr_request_result": _lib.RequestResultC, "hsr_server_stats": _lib.ServerStatsC,
-               "hsr_tracer_flags": _lib.FlagsC, "hsr_antenna": _lib.AntennaC, "hsr_rf_config": _lib.RFConfigC}
+               "hsr_tracer_flags": _lib.FlagsC, "hsr_antenna": _lib.AntennaC, "hsr_rf_config": _lib.RFConfigC,
+               "hsr_launch_config": _lib.LaunchConfigC}
     for key, val in c.items():
         if "." in key:
             t, m = key.split(".")
