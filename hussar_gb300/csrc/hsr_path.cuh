@@ -283,11 +283,12 @@ __device__ __forceinline__ bool nee_eval(const TraceParams &p, const DNode *node
         ph = cf{c, s};
     } else {
         // path length reduced to phase in FP64: cycles = f0 dt - S dt^2 / 2 (mod 1)
-        double dt = nlen / 299792458.0 + double(rf.antennaDelay);
+        // FP64 divides are long sequences on this part: multiply by reciprocals (<= 1 ulp)
+        double dt = nlen * (1.0 / 299792458.0) + double(rf.antennaDelay);
         if (rf.freqSlope == 0.f) {
             sample = 0.f;
         } else {
-            double x = dt * double(rf.freqSlope) / double(rf.adcRate);
+            double x = dt * (double(rf.freqSlope) / double(rf.adcRate));
             sample = float(double(samples) * (x - floor(x)));
         }
         double cyc = (double(rf.startFreq) - dt * double(rf.freqSlope) * 0.5) * dt;
@@ -351,18 +352,37 @@ __device__ __forceinline__ void splat_serial(float *s_re, float *s_im, int n, co
     }
 }
 
-// A full warp adds the items of the lanes in `mask` cooperatively: lane l owns window
-// offset l - 16 (lane 0 also owns +16), so one item's 33 bins are distinct addresses
-// updated by distinct lanes. Items are taken in lane order; each lane sums its bin over
-// a run of items with the same center in registers and adds the sum once when the
-// center changes (coherent returns put most of a warp's items on one center, and the
-// shared-memory atomics on those few bins are what limits the splat). A delta item
-// (shift 0) adds its value at offset 0 only. Must be called by all 32 lanes.
-__device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, unsigned mask, const SplatItem &mine) {
+// 1 / x by the hardware approximation (rcp.approx.ftz.f32, within 1 ulp for normal x).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// An item of a warp's cooperative splat: the fractional shift (0 => delta peak), the
+// value times the sinc weight (weight 1 for a delta peak), and the center bin. The
+// owning lane forms it once; every lane then needs only its own bin's 1 / (shift - s).
+__device__ __forceinline__ float4 splat_item(float sample, cf value) {
+    const SplatItem it = splat_prepare(sample, value);
+    return make_float4(it.shift, it.w * it.value.re, it.w * it.value.im, __int_as_float(it.center));
+}
+
+// A full warp adds the items of the lanes with `has` set cooperatively: lane l owns
+// window offset l - 16 (lane 0 also owns +16), so one item's 33 bins are distinct
+// addresses updated by distinct lanes. Items are broadcast by shuffles in lane order;
+// each lane sums its bin over a run of items with the same center in registers and adds
+// the sum once when the center changes (coherent returns put most of a warp's items on
+// one center, and the shared-memory atomics on those few bins are what limits the
+// splat). The per-bin factor 1 / (shift - s) is the hardware reciprocal (within 1 ulp;
+// the reference divides, radar.h:612-618; |shift - s| >= 1e-4, so it is never
+// subnormal). Must be called by all 32 lanes.
+__device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, bool has, float4 mine) {
+    unsigned mask = __ballot_sync(0xffffffffu, has);
+    if (mask == 0u) return;
     const int lane = threadIdx.x & 31;
     const int s = lane - 16;
-    int center = 0;
-    bool open = false;
+    const float fs = float(s);
+    int center = INT_MIN;  // no run open
     float ar = 0.f, ai = 0.f, er = 0.f, ei = 0.f;  // this lane's bin, and lane 0's bin +16
     auto flush = [&]() {
         const bool inside = (center - 16 >= 0) && (center + 16 < n);
@@ -381,31 +401,31 @@ __device__ __forceinline__ void splat_warp(float *s_re, float *s_im, int n, unsi
     while (mask) {
         const int j = __ffs(mask) - 1;
         mask &= mask - 1;
-        const int c = __shfl_sync(0xffffffffu, mine.center, j);
-        const float shift = __shfl_sync(0xffffffffu, mine.shift, j);
-        const float vr = __shfl_sync(0xffffffffu, mine.value.re, j);
-        const float vi = __shfl_sync(0xffffffffu, mine.value.im, j);
-        const float w = __shfl_sync(0xffffffffu, mine.w, j);
-        if (open && c != center) flush();
-        center = c;
-        open = true;
+        const float shift = __shfl_sync(0xffffffffu, mine.x, j);
+        const float wr = __shfl_sync(0xffffffffu, mine.y, j);
+        const float wi = __shfl_sync(0xffffffffu, mine.z, j);
+        const int c = __shfl_sync(0xffffffffu, __float_as_int(mine.w), j);
+        if (c != center) {
+            if (center != INT_MIN) flush();
+            center = c;
+        }
         if (shift == 0.f) {
             if (s == 0) {
-                ar += vr;
-                ai += vi;
+                ar += wr;
+                ai += wi;
             }
             continue;
         }
-        const float ws = w / (shift - float(s));
-        ar += ws * vr;
-        ai += ws * vi;
+        const float rcp = rcp_approx(shift - fs);
+        ar = __fmaf_rn(wr, rcp, ar);
+        ai = __fmaf_rn(wi, rcp, ai);
         if (lane == 0) {
-            const float w16 = w / (shift - 16.f);
-            er += w16 * vr;
-            ei += w16 * vi;
+            const float r16 = rcp_approx(shift - 16.f);
+            er = __fmaf_rn(wr, r16, er);
+            ei = __fmaf_rn(wi, r16, ei);
         }
     }
-    if (open) flush();
+    flush();
 }
 
 // Fine range histogram (HSR_SPLAT_FINE_SYNTH): 8 sub-bins per range bin with moments

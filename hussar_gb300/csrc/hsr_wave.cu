@@ -3,7 +3,8 @@
 // kernel, reorganised so that warps stay converged.
 //
 // A persistent CTA of 256 threads keeps a stack of up to 384 live path states in
-// shared memory (four CTAs per SM: 64 registers, ~46 KB of shared memory each) and
+// shared memory (four CTAs per SM: 64 registers; ~32 KB of shared memory each plus the
+// range row, so that four CTAs leave about 90 KB of the SM's L1 to the BVH) and
 // alternates two stages:
 //   GENERATE  (at most 128 live paths, or the autotuned queue threshold): 256 new
 //             samples, one per thread: Halton point,
@@ -35,10 +36,11 @@ struct WaveShared {
     float dx[kStack], dy[kStack], dz[kStack];  // incoming direction
     float h[6][kStack];                        // incoming H field (re, im) x 3
     float nx[kStack], ny[kStack], nz[kStack];  // faceforwarded normal at the hit
-    float time[kStack], r[kStack], cosT[kStack], freq[kStack];
-    float px[kStack], py[kStack], pdf[kStack], gwr[kStack], gwi[kStack];  // guiding: primary, pdf, weight
+    float r[kStack], cosT[kStack], freq[kStack];
     int depth[kStack];
-    double plen[kStack];  // FP64 path length (split-phase mode)
+    // the phase input: time of flight (FP32 reference phase, as float) or the FP64 path
+    // length (split phase); each mode carries only its own
+    double tlen[kStack];
     int count;
     int pose, pending_pose, exhausted;
     long long gen, gen_end, pending_first, pending_last;
@@ -52,8 +54,13 @@ struct Guided {  // the guiding part of a path's state
     cf gw;
 };
 
-__device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H, f3 n, float time, float r,
-                                          float cosT, float freq, int depth, double plen, const Guided &g) {
+// Guided launches keep the guiding part of each stacked path (primary sample, pdf,
+// weight) in five more [kStack] arrays after the training sums (`gst`, null otherwise).
+constexpr int kGuideStackFields = 5;
+
+template <int kPhase>
+__device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d, const c3 &H, f3 n, float time,
+                                          float r, float cosT, float freq, int depth, double plen, const Guided &g) {
     const int slot = atomicAdd(&S.count, 1);  // < kStack by construction (see k_wave)
     S.ox[slot] = o.x;
     S.oy[slot] = o.y;
@@ -69,17 +76,21 @@ __device__ __forceinline__ void push_path(WaveShared &S, f3 o, f3 d, const c3 &H
     S.nx[slot] = n.x;
     S.ny[slot] = n.y;
     S.nz[slot] = n.z;
-    S.time[slot] = time;
     S.r[slot] = r;
     S.cosT[slot] = cosT;
     S.freq[slot] = freq;
     S.depth[slot] = depth;
-    S.plen[slot] = plen;
-    S.px[slot] = g.x0;
-    S.py[slot] = g.x1;
-    S.pdf[slot] = g.pdf;
-    S.gwr[slot] = g.gw.re;
-    S.gwi[slot] = g.gw.im;
+    if (kPhase == HSR_PHASE_REFERENCE_FP32)
+        reinterpret_cast<float *>(S.tlen)[slot] = time;
+    else
+        S.tlen[slot] = plen;
+    if (gst) {
+        gst[slot] = g.x0;
+        gst[kStack + slot] = g.x1;
+        gst[2 * kStack + slot] = g.pdf;
+        gst[3 * kStack + slot] = g.gw.re;
+        gst[4 * kStack + slot] = g.gw.im;
+    }
 }
 
 // Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
@@ -124,6 +135,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
     float *s_im = s_re + p.samples;  // the row is sized for the largest N of the launch
     // guided launches: the CTA's training sums (second moment per training-tree node)
     float *s_g = s_re + 2 * p.samples;
+    float *gst = p.do_guide ? s_g + kGuideMaxNodes : nullptr;
     const int tid = threadIdx.x;
     const hsr_tracer_flags &fl = p.flags;
     // the scene, chirp and row of the current pose: launch-uniform, or the pose's job
@@ -202,7 +214,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             }
             const long long s = gen + tid;
             bool has_item = false;
-            SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
+            float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
             if (s < gen_end) {
                 const uint64_t hindex = uint64_t(pc.offset + s);
                 const float freq = rf.startFreq + halton(hindex, 0) * HSR_BANDWIDTH;
@@ -221,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                         if (pc.fine_row) {
                             splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
                         } else {
-                            item = splat_prepare(ne.sample, ne.value);
+                            item = splat_item(ne.sample, ne.value);
                             has_item = true;
                         }
                     }
@@ -232,13 +244,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     double plen = 0.0;
                     f3 hp, n;
                     if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n, cosT)) {
-                        push_path(S, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
+                        push_path<kPhase>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
                         alive = true;
                     }
                 }
                 if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
             }
-            if (!fl.onlyIndirect) splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
+            if (!fl.onlyIndirect) splat_warp(s_re, s_im, HSR_N, has_item, item);
             __syncthreads();
             continue;
         }
@@ -255,24 +267,28 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             Guided g{0.f, 0.f, 1.f, cf{0.f, 0.f}};
             if (mine) {
                 const int slot = count - 1 - tid;
-                g = Guided{S.px[slot], S.py[slot], S.pdf[slot], cf{S.gwr[slot], S.gwi[slot]}};
+                if (gst)
+                    g = Guided{gst[slot], gst[kStack + slot], gst[2 * kStack + slot],
+                               cf{gst[3 * kStack + slot], gst[4 * kStack + slot]}};
                 o = mk3(S.ox[slot], S.oy[slot], S.oz[slot]);
                 din = mk3(S.dx[slot], S.dy[slot], S.dz[slot]);
 #pragma unroll
                 for (int i = 0; i < 3; ++i) Hin.v[i] = cf{S.h[2 * i][slot], S.h[2 * i + 1][slot]};
                 nrm = mk3(S.nx[slot], S.ny[slot], S.nz[slot]);
-                time = S.time[slot];
+                if (kPhase == HSR_PHASE_REFERENCE_FP32)
+                    time = reinterpret_cast<const float *>(S.tlen)[slot];
+                else
+                    plen = S.tlen[slot];
                 r = S.r[slot];
                 cosT = S.cosT[slot];
                 freq = S.freq[slot];
                 depth = S.depth[slot];
-                plen = S.plen[slot];
             }
             __syncthreads();  // all pops read before the stack shrinks
             if (tid == 0) S.count = count - n;
             __syncthreads();
             bool has_item = false;
-            SplatItem item{0, 0.f, cf{0.f, 0.f}, 0.f};
+            float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
             if (mine) {
                 f3 d = din;
                 c3 H = Hin;
@@ -285,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                         if (pc.fine_row) {
                             splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
                         } else {
-                            item = splat_prepare(ne.sample, ne.value);
+                            item = splat_item(ne.sample, ne.value);
                             has_item = true;
                         }
                     }
@@ -295,13 +311,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     f3 hp, n2;
                     float cosT2;
                     if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n2, cosT2)) {
-                        push_path(S, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
+                        push_path<kPhase>(S, gst, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
                         alive = true;
                     }
                 }
                 if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
             }
-            splat_warp(s_re, s_im, HSR_N, __ballot_sync(0xffffffffu, has_item), item);
+            splat_warp(s_re, s_im, HSR_N, has_item, item);
             __syncthreads();
             continue;
         }
@@ -347,8 +363,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
 }  // namespace
 
 size_t wave_smem_bytes(int samples, bool guided) {
-    // guided: the CTA's training sums
-    return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float) + (guided ? kGuideMaxNodes * sizeof(float) : 0);
+    // guided: the CTA's training sums and the guiding part of the stacked paths
+    return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float) +
+           (guided ? (kGuideMaxNodes + kGuideStackFields * kStack) * sizeof(float) : 0);
 }
 
 template <int kPhase, bool kMixed>

@@ -152,6 +152,85 @@ private:
     std::function<void(const SceneView &, long, bool *)> m_run;
 };
 
+/* A serving loop over resident scenes (hsr_server_*): requests from any thread, traced
+ * in shared batching ticks. No counterpart in the reference, whose backends trace one
+ * pose per synchronous run() (src/arch/gpu.cpp:499-532). The tracer flags come from an
+ * integrator (its public flags of path.h:153-169; guiding must be off). A request's row
+ * is the fetchFrame() row of a plain run of `budget` samples at index offset `offset`. */
+class Server {
+public:
+    explicit Server(const hsr_server_config &config) { check(hsr_server_create(&config, &m_server)); }
+
+    template <typename Integrator>
+    explicit Server(const Integrator &integrator, int32_t phase_mode = HSR_PHASE_REFERENCE_FP32,
+                    int32_t max_slots = 0, int64_t memory_bytes = 0) {
+        hsr_server_config c;
+        hsr_default_server_config(&c);
+        c.flags = to_hsr_flags(integrator);
+        c.phase_mode = phase_mode;
+        if (max_slots > 0) c.max_slots = max_slots;
+        if (memory_bytes > 0) c.memory_bytes = memory_bytes;
+        check(hsr_server_create(&c, &m_server));
+    }
+
+    Server(const Server &) = delete;
+    Server &operator=(const Server &) = delete;
+    /* Finishes the device work; requests still queued fail with HSR_ERR_INTERRUPTED. */
+    ~Server() { hsr_server_destroy(m_server); }
+
+    /* The backend's scene stays resident; it must outlive the server. */
+    int32_t addScene(const Backend &backend) {
+        int32_t id = -1;
+        check(hsr_server_add_scene(m_server, backend.handle(), &id));
+        return id;
+    }
+
+    /* Queues one pose; `out_row` (complex64[samples_per_chirp], as float re/im pairs) must
+     * stay valid until wait() reports the ticket finished. */
+    template <typename Scene>
+    uint64_t submit(int32_t scene_id, const Scene &scene, int32_t samples_per_chirp, long budget, float *out_row,
+                    long index_offset = 0) {
+        hsr_request r;
+        r.scene = scene_id;
+        r.samples_per_chirp = samples_per_chirp;
+        r.rf = to_hsr_rf(scene.rfConfig);
+        r.tx = to_hsr(scene.tx);
+        r.rx = to_hsr(scene.rx);
+        r.budget = int64_t(budget);
+        r.index_offset = int64_t(index_offset);
+        r.out_row = out_row;
+        uint64_t ticket = 0;
+        check(hsr_server_submit(m_server, &r, &ticket));
+        return ticket;
+    }
+
+    /* Blocks until the request finishes (timeout_ms < 0) or the timeout passes; returns
+     * false on a timeout. A request that failed throws. */
+    bool wait(uint64_t ticket, hsr_request_result *result = nullptr, int32_t timeout_ms = -1) {
+        hsr_request_result r;
+        hsr_status s = hsr_server_wait(m_server, ticket, timeout_ms, &r);
+        if (s == HSR_ERR_TIMEOUT) return false;
+        check(s);
+        if (r.status != HSR_OK)
+            throw std::runtime_error("gb300: request failed with status " + std::to_string(r.status));
+        if (result) *result = r;
+        return true;
+    }
+
+    hsr_server_stats stats() const {
+        hsr_server_stats s;
+        check(hsr_server_get_stats(m_server, &s));
+        return s;
+    }
+
+    void resetStats() { check(hsr_server_reset_stats(m_server)); }
+
+    hsr_server *handle() const { return m_server; }
+
+private:
+    hsr_server *m_server = nullptr;
+};
+
 }  // namespace gb300
 }  // namespace hussar
 

@@ -1,6 +1,7 @@
 """The C++ drop-in (include/hussar/gb300.h + gb300_types.h): the reference's example
 flow compiled with g++ against libhsr_gb300.so gives the same frames as the Python
-binding and the oracle."""
+binding and the oracle, and so does the C++ serving wrapper with several client
+threads submitting at once."""
 import os
 import subprocess
 
@@ -13,14 +14,23 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.fixture(scope="module")
-def example_bin(product_lib, tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("cpp") / "dihedral_example")
+def compile_example(name, out_dir):
+    out = str(out_dir / name)
     libdir = os.path.join(ROOT, "hussar_gb300")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
-                           os.path.join(ROOT, "tests", "cpp", "dihedral_example.cpp"), "-L", libdir, "-lhsr_gb300",
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-pthread", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-L", libdir, "-lhsr_gb300",
                            "-Wl,-rpath," + libdir, "-o", out])
     return out
+
+
+@pytest.fixture(scope="module")
+def example_bin(product_lib, tmp_path_factory):
+    return compile_example("dihedral_example", tmp_path_factory.mktemp("cpp"))
+
+
+@pytest.fixture(scope="module")
+def serve_bin(product_lib, tmp_path_factory):
+    return compile_example("serve_example", tmp_path_factory.mktemp("cpp"))
 
 
 def test_cpp_example_matches_python_and_oracle(example_bin, tmp_path, oracle_lib):
@@ -46,3 +56,31 @@ def test_cpp_example_matches_python_and_oracle(example_bin, tmp_path, oracle_lib
             continue
         assert np.linalg.norm(frames[k] - ref) / np.linalg.norm(ref) <= 1e-4
         assert np.linalg.norm(frames[k] - rows[k]) / np.linalg.norm(rows[k]) <= 1e-5
+
+
+def test_cpp_server_matches_batch_and_oracle(serve_bin, tmp_path, oracle_lib):
+    poses, samples, threads = 24, 1 << 16, 4
+    sim = str(tmp_path / "served.SIM")
+    out = subprocess.check_output([serve_bin, sim, str(poses), str(samples), str(threads)], text=True)
+    print(out)
+    rows = np.fromfile(sim, np.complex64).reshape(poses, 256)
+    pose = np.fromfile(sim + ".poses", np.float32).reshape(poses, 12)
+    w = scenes.dihedral_workload(poses=poses, samples_per_pose=samples)
+    w.tx = [NFAntenna(p[:3], p[3:].reshape(3, 3)) for p in pose]
+    w.rx = w.tx
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = 2
+    be = gb300.Backend(w.mesh, None)
+    batch = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, w.budget)
+    ora = oracle_lib.Scene(w.mesh)
+    for k in range(0, poses, 5):
+        ref = ora.fetch_row(w.rf, 256, w.tx[k], w.rx[k], t, samples)
+        if np.linalg.norm(ref) > 0:
+            assert np.linalg.norm(rows[k] - ref) / np.linalg.norm(ref) <= 1e-4, k
+    for k in range(poses):
+        if np.linalg.norm(batch[k]) == 0:
+            assert np.linalg.norm(rows[k]) == 0, k
+        else:
+            # the same Halton samples; only the FP64 summation order differs
+            assert np.linalg.norm(rows[k] - batch[k]) / np.linalg.norm(batch[k]) <= 1e-5, k
