@@ -1,8 +1,10 @@
 """Builds libhsr_gb300.so in-tree with nvcc for sm_103a (no torch involved).
 
-The trace kernel is compiled with -fmad=false so that its float expressions round
-exactly like the CPU restatement used by the tests; the other translation units use
-the default contraction.
+The trace kernels are compiled with -fmad=false so that their float expressions round
+exactly like the CPU restatement used by the tests, except the wavefront kernel's
+split-phase instantiations (hsr_wave_split.cu): that form is bounded against the FP64
+oracle rather than matched to the reference's FP32 rounding, and gains from fused
+multiply-adds. The other translation units use the default contraction.
 """
 import concurrent.futures
 import os
@@ -28,6 +30,7 @@ UNITS = {
     "hsr_serve.cu": [],
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
+    "hsr_wave_split.cu": [],
 }
 
 

@@ -163,6 +163,8 @@ int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, cons
                        cudaStream_t st);
 int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
 size_t wave_smem_bytes(int samples, bool guided);
+// The split-phase instantiations of the wavefront kernel (hsr_wave_split.cu).
+void launch_wave_split(const TraceParams &p, bool mixed, int grid, size_t smem, cudaStream_t st);
 int wave_blocks_per_sm(int samples, bool mixed);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel

@@ -1,377 +1,13 @@
-// Wavefront form of the radar path tracer (geometrical-optics mode, the reference's
-// default, path.h:156): the same per-path arithmetic as the one-thread-per-sample
-// kernel, reorganised so that warps stay converged.
-//
-// A persistent CTA of 256 threads keeps a stack of up to 384 live path states in
-// shared memory (four CTAs per SM: 64 registers; ~32 KB of shared memory each plus the
-// range row, so that four CTAs leave about 90 KB of the SM's L1 to the BVH) and
-// alternates two stages:
-//   GENERATE  (at most 128 live paths, or the autotuned queue threshold): 256 new
-//             samples, one per thread: Halton point,
-//             antenna ray, closest hit; paths that hit something are pushed.
-//   EXTEND    (otherwise): 256 paths popped, one per thread: specular reflection,
-//             next-event estimate towards RX (shadow ray, PO re-radiation, filtering,
-//             phase), and the next closest hit; survivors are pushed back.
-// Every next-event contribution is splatted by its warp cooperatively: lane l owns
-// window offset l-16 of Frame::splat<16>, so one contribution's 33 bins are 33 distinct
-// shared-memory addresses updated in one pass. The CTA's range row lives in shared
-// memory and is flushed to the pose's FP64 accumulators when the CTA changes pose.
-// Work items are (pose, 4096-sample tile) pairs pulled from a device counter.
-//
-// Mixed batches (kMixed, the serving loop): each pose names its own resident scene,
-// chirp, range-bin count and accumulator row (PoseJob). A CTA works on one pose at a
-// time, so these are CTA-uniform: thread 0 copies the pose's job into shared memory
-// when the CTA switches pose, and the arithmetic is the uniform kernel's.
-#include "hsr_path.cuh"
+// The wavefront kernel's FP32 reference-phase instantiations (compiled without
+// multiply-add contraction) and its host entry points; the kernel is in hsr_wave.cuh.
+#include "hsr_wave.cuh"
 
 namespace hsr {
-
-namespace {
-
-constexpr int kThreads = 256;
-constexpr int kStack = 3 * kThreads / 2;  // live path states per CTA
-
-struct WaveShared {
-    float ox[kStack], oy[kStack], oz[kStack];  // hit point (origin of the next segment)
-    float dx[kStack], dy[kStack], dz[kStack];  // incoming direction
-    float h[6][kStack];                        // incoming H field (re, im) x 3
-    float nx[kStack], ny[kStack], nz[kStack];  // faceforwarded normal at the hit
-    float r[kStack], cosT[kStack], freq[kStack];
-    int depth[kStack];
-    // the phase input: time of flight (FP32 reference phase, as float) or the FP64 path
-    // length (split phase); each mode carries only its own
-    double tlen[kStack];
-    int count;
-    int pose, pending_pose, exhausted;
-    long long gen, gen_end, pending_first, pending_last;
-    long long since_flush;      // samples generated since the row was last flushed
-    PoseJob job;                // mixed batches: the current pose's scene, chirp and row
-    float max_dist, bandwidth;  // mixed batches: derived from job.rf
-};
-
-struct Guided {  // the guiding part of a path's state
-    float x0, x1, pdf;
-    cf gw;
-};
-
-// Guided launches keep the guiding part of each stacked path (primary sample, pdf,
-// weight) in five more [kStack] arrays after the training sums (`gst`, null otherwise).
-constexpr int kGuideStackFields = 5;
-
-template <int kPhase>
-__device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d, const c3 &H, f3 n, float time,
-                                          float r, float cosT, float freq, int depth, double plen, const Guided &g) {
-    const int slot = atomicAdd(&S.count, 1);  // < kStack by construction (see k_wave)
-    S.ox[slot] = o.x;
-    S.oy[slot] = o.y;
-    S.oz[slot] = o.z;
-    S.dx[slot] = d.x;
-    S.dy[slot] = d.y;
-    S.dz[slot] = d.z;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        S.h[2 * i][slot] = H.v[i].re;
-        S.h[2 * i + 1][slot] = H.v[i].im;
-    }
-    S.nx[slot] = n.x;
-    S.ny[slot] = n.y;
-    S.nz[slot] = n.z;
-    S.r[slot] = r;
-    S.cosT[slot] = cosT;
-    S.freq[slot] = freq;
-    S.depth[slot] = depth;
-    if (kPhase == HSR_PHASE_REFERENCE_FP32)
-        reinterpret_cast<float *>(S.tlen)[slot] = time;
-    else
-        S.tlen[slot] = plen;
-    if (gst) {
-        gst[slot] = g.x0;
-        gst[kStack + slot] = g.x1;
-        gst[2 * kStack + slot] = g.pdf;
-        gst[3 * kStack + slot] = g.gw.re;
-        gst[4 * kStack + slot] = g.gw.im;
-    }
-}
-
-// Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
-// Returns true (and the new state) when the path continues with a stored hit.
-__device__ __forceinline__ bool walk(const TraceParams &p, const DNode *nodes, const DTri *tris, f3 o, f3 d,
-                                     const c3 &H, float &time, float &r, double &plen, f3 &hp, f3 &n, float &cosT) {
-    float th;
-    int primh;
-    const int slot = closest_hit<false>(nodes, tris, o, d, kEpsilon, CUDART_INF_F, th, primh, p.status, nullptr);
-    if (slot < 0) return false;
-    DTri T = load_tri(tris, slot);
-    n = hit_normal(T, d);
-    hp = add3(o, scl3(th, d));
-    cosT = fabsf(dot3(n, neg3(d)));
-    if (cosT < 0.001f) return false;
-    r += th;
-    time += th / kSpeedOfLight;
-    plen += double(th);
-    if (c3_is_zero(H)) return false;
-    return true;
-}
-
-// PathTracer::run's derived chirp quantities (path.h:240, radar.h:128-130).
-__device__ __forceinline__ float max_distance(const hsr_rf_config &rf) {
-    return rf.adcRate / rf.freqSlope * kSpeedOfLight;
-}
-__device__ __forceinline__ float chirp_bandwidth(const hsr_rf_config &rf) { return rf.freqSlope * rf.rampTime; }
-
-// FP64 accumulator row of a pose: pose-major rows of N, or the pose's job row.
-template <bool kMixed>
-__device__ __forceinline__ double *pose_row(const TraceParams &p, const WaveShared &S, int pose) {
-    return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
-}
-
-// Four CTAs per SM (64 registers): the spills cost less than the latency the extra
-// warps hide (measured: 1.2x on the sphere bench, 1.13x on the serving mix over two).
-template <int kPhase, bool kMixed>
-__global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
-    float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
-    float *s_im = s_re + p.samples;  // the row is sized for the largest N of the launch
-    // guided launches: the CTA's training sums (second moment per training-tree node)
-    float *s_g = s_re + 2 * p.samples;
-    float *gst = p.do_guide ? s_g + kGuideMaxNodes : nullptr;
-    const int tid = threadIdx.x;
-    const hsr_tracer_flags &fl = p.flags;
-    // the scene, chirp and row of the current pose: launch-uniform, or the pose's job
-    const hsr_rf_config &rf = kMixed ? S.job.rf : p.rf;
-    const float maxDist0 = max_distance(p.rf), bandwidth0 = chirp_bandwidth(p.rf);
-#define HSR_NODES (kMixed ? S.job.nodes : p.nodes)
-#define HSR_TRIS (kMixed ? S.job.tris : p.tris)
-#define HSR_N (kMixed ? S.job.samples : p.samples)
-#define HSR_MAXDIST (kMixed ? S.max_dist : maxDist0)
-#define HSR_BANDWIDTH (kMixed ? S.bandwidth : bandwidth0)
-    const long long total = __ldg(&p.tile_start[p.pose_count]);
-    static_assert(kStack - kThreads == kWaveMaxQueueThreshold, "queue threshold bound");
-    const int queue_threshold = (p.queue_threshold > 0 && p.queue_threshold < kStack - kThreads)
-                                    ? p.queue_threshold : kStack - kThreads;
-
-    for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
-    if (p.do_guide)
-        for (int k = tid; k < kGuideMaxNodes; k += kThreads) s_g[k] = 0.f;
-    if (tid == 0) {
-        S.count = 0;
-        S.pose = -1;
-        S.pending_pose = -1;
-        S.exhausted = 0;
-        S.gen = S.gen_end = 0;
-        S.since_flush = 0;
-    }
-    __syncthreads();
-
-    PoseCtx pc;
-    int cur_pose = -1;
-
-    while (true) {
-        // thread 0 pulls work items while the generation range is used up
-        if (tid == 0) {
-            while (S.gen >= S.gen_end && !S.exhausted && S.pending_pose < 0) {
-                const long long item = (long long)atomicAdd((unsigned long long *)p.work_counter, 1ull);
-                if (item >= total) {
-                    S.exhausted = 1;
-                    break;
-                }
-                const int pose = find_pose(p.tile_start, p.pose_count, item);
-                const long long first = (item - __ldg(&p.tile_start[pose])) * p.tile;
-                const long long last = min(first + (long long)p.tile, (long long)__ldg(&p.budget[pose]));
-                if (pose == S.pose) {
-                    S.gen = first;
-                    S.gen_end = last;
-                } else {
-                    S.pending_pose = pose;
-                    S.pending_first = first;
-                    S.pending_last = last;
-                }
-            }
-        }
-        __syncthreads();
-        const int count = S.count;
-        const long long gen = S.gen, gen_end = S.gen_end;
-        const int pending = S.pending_pose;
-        const int exhausted = S.exhausted;
-        const long long since_flush = S.since_flush;
-        __syncthreads();  // every thread has read the shared control words
-
-        if (since_flush >= kFlushSamples && cur_pose >= 0) {
-            // bound the FP32 partial sums: move the row to the FP64 accumulators
-            flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
-            if (p.do_guide) flush_guide(pc, s_g);
-            if (tid == 0) S.since_flush = 0;
-            __syncthreads();
-            continue;
-        }
-
-        if (gen < gen_end && count <= queue_threshold) {
-            // ---------------- GENERATE ----------------
-            if (tid == 0) {
-                S.gen = min(gen + (long long)kThreads, gen_end);
-                S.since_flush += S.gen - gen;
-            }
-            const long long s = gen + tid;
-            bool has_item = false;
-            float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (s < gen_end) {
-                const uint64_t hindex = uint64_t(pc.offset + s);
-                const float freq = rf.startFreq + halton(hindex, 0) * HSR_BANDWIDTH;
-                Guided g{halton(hindex, 1), halton(hindex, 2), 1.f, cf{0.f, 0.f}};
-                if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
-                f3 o = pc.tx.pos, d;
-                c3 H;
-                antenna_sample(pc.tx, g.x0, g.x1, d, H);
-                H = c3_scl(H, 1.f / g.pdf);
-                if (!fl.onlyIndirect) {
-                    NeeOut ne;
-                    if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, 0, o, d,
-                                                mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H, 0.f, 0.0, 0.f, 1.f,
-                                                freq, pc.weight, ne, nullptr, nullptr) &&
-                        ne.splat) {
-                        if (pc.fine_row) {
-                            splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
-                        } else {
-                            item = splat_item(ne.sample, ne.value);
-                            has_item = true;
-                        }
-                    }
-                }
-                bool alive = false;
-                if (!(0 >= fl.maxDepth || 0.f >= HSR_MAXDIST) && !c3_is_zero(H)) {
-                    float time = 0.f, r = 0.f, cosT;
-                    double plen = 0.0;
-                    f3 hp, n;
-                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n, cosT)) {
-                        push_path<kPhase>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
-                        alive = true;
-                    }
-                }
-                if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
-            }
-            if (!fl.onlyIndirect) splat_warp(s_re, s_im, HSR_N, has_item, item);
-            __syncthreads();
-            continue;
-        }
-
-        if (count > 0) {
-            // ---------------- EXTEND ----------------
-            const int n = min(count, kThreads);
-            const bool mine = tid < n;
-            f3 o, din, nrm;
-            c3 Hin;
-            float time = 0.f, r = 0.f, cosT = 1.f, freq = 0.f;
-            int depth = 0;
-            double plen = 0.0;
-            Guided g{0.f, 0.f, 1.f, cf{0.f, 0.f}};
-            if (mine) {
-                const int slot = count - 1 - tid;
-                if (gst)
-                    g = Guided{gst[slot], gst[kStack + slot], gst[2 * kStack + slot],
-                               cf{gst[3 * kStack + slot], gst[4 * kStack + slot]}};
-                o = mk3(S.ox[slot], S.oy[slot], S.oz[slot]);
-                din = mk3(S.dx[slot], S.dy[slot], S.dz[slot]);
-#pragma unroll
-                for (int i = 0; i < 3; ++i) Hin.v[i] = cf{S.h[2 * i][slot], S.h[2 * i + 1][slot]};
-                nrm = mk3(S.nx[slot], S.ny[slot], S.nz[slot]);
-                if (kPhase == HSR_PHASE_REFERENCE_FP32)
-                    time = reinterpret_cast<const float *>(S.tlen)[slot];
-                else
-                    plen = S.tlen[slot];
-                r = S.r[slot];
-                cosT = S.cosT[slot];
-                freq = S.freq[slot];
-                depth = S.depth[slot];
-            }
-            __syncthreads();  // all pops read before the stack shrinks
-            if (tid == 0) S.count = count - n;
-            __syncthreads();
-            bool has_item = false;
-            float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (mine) {
-                f3 d = din;
-                c3 H = Hin;
-                reflect(nrm, d, H);
-                NeeOut ne;
-                if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, depth, o, d, din, nrm,
-                                            Hin, H, time, plen, r, cosT, freq, pc.weight, ne, nullptr, nullptr)) {
-                    g.gw = cadd(g.gw, ne.gw_add);
-                    if (ne.splat) {
-                        if (pc.fine_row) {
-                            splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
-                        } else {
-                            item = splat_item(ne.sample, ne.value);
-                            has_item = true;
-                        }
-                    }
-                }
-                bool alive = false;
-                if (!(depth >= fl.maxDepth || r >= HSR_MAXDIST) && !c3_is_zero(H)) {
-                    f3 hp, n2;
-                    float cosT2;
-                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n2, cosT2)) {
-                        push_path<kPhase>(S, gst, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
-                        alive = true;
-                    }
-                }
-                if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
-            }
-            splat_warp(s_re, s_im, HSR_N, has_item, item);
-            __syncthreads();
-            continue;
-        }
-
-        if (pending >= 0) {
-            // stack drained: finish the old pose's row and switch to the new pose
-            if (cur_pose >= 0) {
-                flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
-                if (p.do_guide) flush_guide(pc, s_g);
-            }
-            cur_pose = pending;
-            pc = load_pose(p, cur_pose);
-            __syncthreads();  // every thread is done with the old pose's job
-            if (tid == 0) {
-                if (kMixed) {
-                    S.job = p.jobs[pending];
-                    S.max_dist = max_distance(S.job.rf);
-                    S.bandwidth = chirp_bandwidth(S.job.rf);
-                }
-                S.pose = pending;
-                S.since_flush = 0;
-                S.gen = S.pending_first;
-                S.gen_end = S.pending_last;
-                S.pending_pose = -1;
-            }
-            __syncthreads();
-            continue;
-        }
-        if (exhausted) break;
-    }
-    if (cur_pose >= 0) {
-        __syncthreads();
-        flush_row(pose_row<kMixed>(p, S, cur_pose), s_re, s_im, HSR_N);
-        if (p.do_guide) flush_guide(pc, s_g);
-    }
-#undef HSR_NODES
-#undef HSR_TRIS
-#undef HSR_N
-#undef HSR_MAXDIST
-#undef HSR_BANDWIDTH
-}
-
-}  // namespace
 
 size_t wave_smem_bytes(int samples, bool guided) {
     // guided: the CTA's training sums and the guiding part of the stacked paths
     return sizeof(WaveShared) + 2 * size_t(samples) * sizeof(float) +
            (guided ? (kGuideMaxNodes + kGuideStackFields * kStack) * sizeof(float) : 0);
-}
-
-template <int kPhase, bool kMixed>
-void wave_instance(const TraceParams &p, int grid, size_t smem, cudaStream_t st) {
-    cudaFuncSetAttribute(k_wave<kPhase, kMixed>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k_wave<kPhase, kMixed><<<grid, kThreads, smem, st>>>(p);
 }
 
 int wave_blocks_per_sm(int samples, bool mixed) {
@@ -394,12 +30,12 @@ int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st,
     const bool split = phase_mode == HSR_PHASE_SPLIT_FP64;
     if (p.jobs) {
         if (split)
-            wave_instance<HSR_PHASE_SPLIT_FP64, true>(p, grid, smem, st);
+            launch_wave_split(p, true, grid, smem, st);
         else
             wave_instance<HSR_PHASE_REFERENCE_FP32, true>(p, grid, smem, st);
     } else {
         if (split)
-            wave_instance<HSR_PHASE_SPLIT_FP64, false>(p, grid, smem, st);
+            launch_wave_split(p, false, grid, smem, st);
         else
             wave_instance<HSR_PHASE_REFERENCE_FP32, false>(p, grid, smem, st);
     }
