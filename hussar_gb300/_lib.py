@@ -153,6 +153,7 @@ def lib():
         "hsr_server_destroy": [vp],
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
+        "hsr_debug_halton": [vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_autotune_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                ctypes.c_int32, ctypes.c_int32, P(LaunchConfigC)],
         "hsr_set_launch_config": [vp, P(LaunchConfigC)],

@@ -625,6 +625,22 @@ hsr_status hsr_debug_bvh(const hsr_scene *s, void *out_nodes, int64_t node_capac
     return e == cudaSuccess ? HSR_OK : cuda_fail(e, "BVH copy");
 }
 
+hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, float *out) {
+    if (count < 0 || dim < 0 || (count > 0 && (!index || !out))) return fail(HSR_ERR_INVALID_ARGUMENT, "bad arguments");
+    hsr_status r = check_device();
+    if (r != HSR_OK || count == 0) return r;
+    uint64_t *d_index = nullptr;
+    std::string err;
+    if (!dev_alloc(&d_index, (sizeof(uint64_t) + sizeof(float)) * size_t(count), err))
+        return fail(HSR_ERR_OUT_OF_MEMORY, err);
+    float *d_out = reinterpret_cast<float *>(d_index + count);
+    cudaError_t e = cudaMemcpy(d_index, index, sizeof(uint64_t) * size_t(count), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && launch_debug_halton(d_index, count, dim, d_out) != 0) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d_out, sizeof(float) * size_t(count), cudaMemcpyDeviceToHost);
+    cudaFree(d_index);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "halton");
+}
+
 hsr_status hsr_scene_bvh_stats(const hsr_scene *s, int64_t *out_nodes, int32_t *out_max_depth, int64_t *out_leaves) {
     if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
     if (out_nodes) *out_nodes = s->dev.node_count;

@@ -158,6 +158,8 @@ int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, 
 int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, const int64_t *budget, float sample_weight,
                     const double *total_weight, int normalise, float *out_rows, cudaStream_t st);
 int launch_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *clear, cudaStream_t st);
+// The device Halton sampler at host-chosen indices (hsr_debug_halton).
+int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out);
 int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st);

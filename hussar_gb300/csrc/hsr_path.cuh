@@ -15,6 +15,12 @@ namespace hsr {
 
 // radicalInverse<base> (libhussar/include/hussar/samplers/halton.h:38-54)
 template <int kBase> __device__ __forceinline__ float radical_inverse(uint64_t v) {
+    if (kBase == 2) {
+        // base 2: the reversed digits are the bit reversal of v's d significant bits, and
+        // the reference's float(reversed) * 2^-d equals float(brev64(v)) * 2^-64 exactly
+        // (brev64(v) = reversed * 2^(64-d); rounding commutes with the power-of-two scale)
+        return fminf(__ull2float_rn(__brevll(v)) * 0x1p-64f, 0.99999994f);
+    }
     const float invBase = 1.f / float(kBase);
     float invBaseN = 1.f;
     uint64_t reversed;

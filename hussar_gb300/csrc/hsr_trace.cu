@@ -362,6 +362,20 @@ int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, cons
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+namespace {
+__global__ void k_debug_halton(const uint64_t *index, int64_t count, int dim, float *out) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = halton(index[i], dim);
+}
+}  // namespace
+
+int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out) {
+    if (count <= 0) return 0;
+    k_debug_halton<<<unsigned((count + 255) / 256), 256>>>(d_index, count, dim, d_out);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st) {

@@ -66,7 +66,14 @@ constexpr int kGuideStackFields = 5;
 template <int kPhase>
 __device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d, const c3 &H, f3 n, float time,
                                           float r, float cosT, float freq, int depth, double plen, const Guided &g) {
-    const int slot = atomicAdd(&S.count, 1);  // < kStack by construction (see k_wave)
+    // one shared atomic per warp: the lanes pushing here take consecutive slots
+    const unsigned active = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(active) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&S.count, __popc(active));
+    base = __shfl_sync(active, base, leader);
+    const int slot = base + __popc(active & ((1u << lane) - 1u));  // < kStack by construction (see k_wave)
     S.ox[slot] = o.x;
     S.oy[slot] = o.y;
     S.oz[slot] = o.z;

@@ -271,6 +271,11 @@ hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs);
 hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_capacity, void *out_tris,
                          int64_t tri_capacity);
 
+/* The device Halton sampler (HaltonSampler::get1D, halton.h:56-67, 1082-1084) at `count`
+ * host indices in dimension `dim` (0..9; larger dimensions give 0 as in the reference),
+ * into out[count] (host). For tests: the trace kernels call the same device function. */
+hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, float *out);
+
 /* ---- Autotuning of the plain wavefront launch ---------------------------------------
  * No counterpart in the reference. The launch shape of a plain batch: samples per work
  * item (tile), persistent CTAs per SM, and the queue threshold (GENERATE runs while a CTA
