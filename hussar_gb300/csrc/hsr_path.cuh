@@ -13,6 +13,45 @@
 
 namespace hsr {
 
+// Tables of the chunked radical inverse (bases 3 and 5): rev[c] is c's kDigits base-kBase
+// digits in reverse order (leading zeros included); inv_pow[n] is (1/kBase)^n formed by n
+// sequential float multiplications, the value the reference's loop leaves in invBaseN
+// after n digits. Built at compile time.
+template <int kBase, int kDigits> struct RadicalTable {
+    static constexpr int size() {
+        int s = 1;
+        for (int i = 0; i < kDigits; ++i) s *= kBase;
+        return s;
+    }
+    unsigned short rev[size()];
+    float inv_pow[48];
+    constexpr RadicalTable() : rev(), inv_pow() {
+        for (int c = 0; c < size(); ++c) {
+            int w = c, r = 0;
+            for (int i = 0; i < kDigits; ++i) {
+                r = r * kBase + w % kBase;
+                w /= kBase;
+            }
+            rev[c] = static_cast<unsigned short>(r);
+        }
+        const float inv = 1.f / float(kBase);
+        float x = 1.f;
+        for (int n = 0; n < 48; ++n) {
+            inv_pow[n] = x;
+            x *= inv;
+        }
+    }
+};
+__device__ constexpr RadicalTable<3, 6> kRadical3{};
+__device__ constexpr RadicalTable<5, 4> kRadical5{};
+
+template <int kBase> __device__ __forceinline__ const auto &radical_table() {
+    if constexpr (kBase == 3)
+        return kRadical3;
+    else
+        return kRadical5;
+}
+
 // radicalInverse<base> (libhussar/include/hussar/samplers/halton.h:38-54)
 template <int kBase> __device__ __forceinline__ float radical_inverse(uint64_t v) {
     if (kBase == 2) {
@@ -20,6 +59,31 @@ template <int kBase> __device__ __forceinline__ float radical_inverse(uint64_t v
         // the reference's float(reversed) * 2^-d equals float(brev64(v)) * 2^-64 exactly
         // (brev64(v) = reversed * 2^(64-d); rounding commutes with the power-of-two scale)
         return fminf(__ull2float_rn(__brevll(v)) * 0x1p-64f, 0.99999994f);
+    }
+    if constexpr (kBase == 3 || kBase == 5) {
+        if (v < (1ull << 26)) {
+            // the reference's digit loop, several digits per step: while a whole chunk of
+            // kDigits digits remains, reversed = reversed * B^kDigits + rev[chunk] (the
+            // integer the digit-by-digit loop forms), then the last digits one by one
+            const auto &T = radical_table<kBase>();
+            constexpr unsigned kChunk = sizeof(T.rev) / sizeof(T.rev[0]);
+            constexpr int kDigits = kBase == 3 ? 6 : 4;
+            unsigned w = unsigned(v), rev = 0;
+            int n = 0;
+            while (w >= kChunk) {
+                const unsigned next = w / kChunk;
+                rev = rev * kChunk + __ldg(&T.rev[w - next * kChunk]);
+                n += kDigits;
+                w = next;
+            }
+            while (w) {
+                const unsigned next = w / kBase;
+                rev = rev * kBase + (w - next * kBase);
+                ++n;
+                w = next;
+            }
+            return fminf(__uint2float_rn(rev) * __ldg(&T.inv_pow[n]), 0.99999994f);
+        }
     }
     const float invBase = 1.f / float(kBase);
     float invBaseN = 1.f;

@@ -1,7 +1,8 @@
 // The wavefront kernel's split-phase instantiations, compiled with multiply-add
-// contraction: the split form is the accuracy-first one (FP64 path length and phase),
-// bounded against the FP64 oracle rather than reproducing the reference's FP32
-// rounding, and the fused forms are both faster and at least as accurate.
+// contraction and the approximate single-precision divide and square root (within 2
+// ulp): the split form is the accuracy-first one (FP64 path length and phase), bounded
+// against the FP64 oracle rather than reproducing the reference's FP32 rounding, and
+// its error is set by the FP32 geometry (~1e-7 relative), which these leave unchanged.
 #include "hsr_wave.cuh"
 
 namespace hsr {
