@@ -44,10 +44,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "paths/s"
-# DRAM bytes (read + write) of one trace launch, from the ncu capture summarised in
-# profiles/k_wave_sphere_ground_2p22.md (dram__bytes_read.sum + dram__bytes_write.sum)
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_wave launch of the sphere bench
-# (ncu --set full capture of the first timed step; profiles/k_wave_sphere_ground_2p22.md)
+# DRAM bytes of one k_wave launch of the sphere bench (dram__bytes_read.sum +
+# dram__bytes_write.sum from an ncu --set full capture of the first timed step of
+# `bench.py --kernel-only`)
 NCU_TRAFFIC = {"sphere": 4.081408e6 + 36.096e3}
 WORKLOAD = "icosphere-L6 (81,920 tris) + 20x20 m ground, sensor 10 m / 0.5 m, 3 bounces, 2^22 samples, N=512"
 

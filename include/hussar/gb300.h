@@ -10,7 +10,8 @@
  *
  * It is duck-typed like the reference's backends, so it works with
  *  - libhussar's own types (Eigen vectors, radar::Frame, hussar::PathTracer) once
- *    PathTracer befriends hussar::gb300::BackendAccess, and
+ *    PathTracer befriends hussar::gb300::BackendAccess (one friend declaration in
+ *    path.h), and
  *  - the self-contained mirror types in hussar/gb300_types.h.
  * Requirements on the types:
  *   mesh.vertexBuffer[i].x()/.y()/.z(), mesh.indexBuffer[i].v0/.v1/.v2
