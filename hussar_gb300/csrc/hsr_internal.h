@@ -33,6 +33,7 @@ struct LaunchConfig {
     int32_t queue_threshold = 0;  // see TraceParams::queue_threshold
 };
 constexpr int kWaveMaxQueueThreshold = 128;  // the wavefront CTA's 384-entry stack minus 256
+constexpr int kWaveSmallQueue = 64;          // thresholds up to this run with a 320-entry stack
 
 // A resident scene: triangles + BVH on the device, plus per-scene scratch reused by
 // every simulate call on this scene (calls on one scene must not overlap).
@@ -166,7 +167,7 @@ int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, cons
 int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
 size_t wave_smem_bytes(int samples, bool guided);
 // The split-phase instantiations of the wavefront kernel (hsr_wave_split.cu).
-void launch_wave_split(const TraceParams &p, bool mixed, int grid, size_t smem, cudaStream_t st);
+void launch_wave_split(const TraceParams &p, int grid, cudaStream_t st);
 int wave_blocks_per_sm(int samples, bool mixed);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel

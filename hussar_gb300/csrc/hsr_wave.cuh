@@ -34,18 +34,22 @@ namespace hsr {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStack = 3 * kThreads / 2;  // live path states per CTA
 
-struct WaveShared {
-    float ox[kStack], oy[kStack], oz[kStack];  // hit point (origin of the next segment)
-    float dx[kStack], dy[kStack], dz[kStack];  // incoming direction
-    float h[6][kStack];                        // incoming H field (re, im) x 3
-    float nx[kStack], ny[kStack], nz[kStack];  // faceforwarded normal at the hit
-    float r[kStack], cosT[kStack], freq[kStack];
-    int depth[kStack];
+// A CTA's live path states: a stack of kThreads + kQueue entries, where kQueue bounds the
+// paths left when GENERATE runs (the queue threshold). Two capacities are built: 384
+// entries (threshold up to 128) and 320 (up to 64), whose 5 KB less shared memory per
+// CTA leaves more of the SM's L1 to the BVH (4 % on the dense boxes scenes, which the
+// autotuner runs at threshold 64).
+template <int kCap> struct WaveShared {
+    float ox[kCap], oy[kCap], oz[kCap];  // hit point (origin of the next segment)
+    float dx[kCap], dy[kCap], dz[kCap];  // incoming direction
+    float h[6][kCap];                    // incoming H field (re, im) x 3
+    float nx[kCap], ny[kCap], nz[kCap];  // faceforwarded normal at the hit
+    float r[kCap], cosT[kCap], freq[kCap];
+    int depth[kCap];
     // the phase input: time of flight (FP32 reference phase, as float) or the FP64 path
     // length (split phase); each mode carries only its own
-    double tlen[kStack];
+    double tlen[kCap];
     int count;
     int pose, pending_pose, exhausted;
     long long gen, gen_end, pending_first, pending_last;
@@ -60,11 +64,11 @@ struct Guided {  // the guiding part of a path's state
 };
 
 // Guided launches keep the guiding part of each stacked path (primary sample, pdf,
-// weight) in five more [kStack] arrays after the training sums (`gst`, null otherwise).
+// weight) in five more [kCap] arrays after the training sums (`gst`, null otherwise).
 constexpr int kGuideStackFields = 5;
 
-template <int kPhase>
-__device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d, const c3 &H, f3 n, float time,
+template <int kPhase, int kCap>
+__device__ __forceinline__ void push_path(WaveShared<kCap> &S, float *gst, f3 o, f3 d, const c3 &H, f3 n, float time,
                                           float r, float cosT, float freq, int depth, double plen, const Guided &g) {
     // one shared atomic per warp: the lanes pushing here take consecutive slots
     const unsigned active = __activemask();
@@ -73,7 +77,7 @@ __device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d,
     int base = 0;
     if (lane == leader) base = atomicAdd(&S.count, __popc(active));
     base = __shfl_sync(active, base, leader);
-    const int slot = base + __popc(active & ((1u << lane) - 1u));  // < kStack by construction (see k_wave)
+    const int slot = base + __popc(active & ((1u << lane) - 1u));  // < kCap by construction (see k_wave)
     S.ox[slot] = o.x;
     S.oy[slot] = o.y;
     S.oz[slot] = o.z;
@@ -98,10 +102,10 @@ __device__ __forceinline__ void push_path(WaveShared &S, float *gst, f3 o, f3 d,
         S.tlen[slot] = plen;
     if (gst) {
         gst[slot] = g.x0;
-        gst[kStack + slot] = g.x1;
-        gst[2 * kStack + slot] = g.pdf;
-        gst[3 * kStack + slot] = g.gw.re;
-        gst[4 * kStack + slot] = g.gw.im;
+        gst[kCap + slot] = g.x1;
+        gst[2 * kCap + slot] = g.pdf;
+        gst[3 * kCap + slot] = g.gw.re;
+        gst[4 * kCap + slot] = g.gw.im;
     }
 }
 
@@ -132,18 +136,19 @@ __device__ __forceinline__ float max_distance(const hsr_rf_config &rf) {
 __device__ __forceinline__ float chirp_bandwidth(const hsr_rf_config &rf) { return rf.freqSlope * rf.rampTime; }
 
 // FP64 accumulator row of a pose: pose-major rows of N, or the pose's job row.
-template <bool kMixed>
-__device__ __forceinline__ double *pose_row(const TraceParams &p, const WaveShared &S, int pose) {
+template <bool kMixed, class Shared>
+__device__ __forceinline__ double *pose_row(const TraceParams &p, const Shared &S, int pose) {
     return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
 }
 
 // Four CTAs per SM (64 registers): the spills cost less than the latency the extra
 // warps hide (measured: 1.2x on the sphere bench, 1.13x on the serving mix over two).
-template <int kPhase, bool kMixed>
+template <int kPhase, bool kMixed, int kQueue>
 __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
+    constexpr int kCap = kThreads + kQueue;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    WaveShared &S = *reinterpret_cast<WaveShared *>(smem_raw);
-    float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared));
+    WaveShared<kCap> &S = *reinterpret_cast<WaveShared<kCap> *>(smem_raw);
+    float *s_re = reinterpret_cast<float *>(smem_raw + sizeof(WaveShared<kCap>));
     float *s_im = s_re + p.samples;  // the row is sized for the largest N of the launch
     // guided launches: the CTA's training sums (second moment per training-tree node)
     float *s_g = s_re + 2 * p.samples;
@@ -159,9 +164,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
 #define HSR_MAXDIST (kMixed ? S.max_dist : maxDist0)
 #define HSR_BANDWIDTH (kMixed ? S.bandwidth : bandwidth0)
     const long long total = __ldg(&p.tile_start[p.pose_count]);
-    static_assert(kStack - kThreads == kWaveMaxQueueThreshold, "queue threshold bound");
-    const int queue_threshold = (p.queue_threshold > 0 && p.queue_threshold < kStack - kThreads)
-                                    ? p.queue_threshold : kStack - kThreads;
+    static_assert(kQueue <= kWaveMaxQueueThreshold, "queue threshold bound");
+    const int queue_threshold = (p.queue_threshold > 0 && p.queue_threshold < kQueue) ? p.queue_threshold : kQueue;
 
     for (int k = tid; k < 2 * p.samples; k += kThreads) s_re[k] = 0.f;
     if (p.do_guide)
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     double plen = 0.0;
                     f3 hp, n;
                     if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n, cosT)) {
-                        push_path<kPhase>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
+                        push_path<kPhase, kCap>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
                         alive = true;
                     }
                 }
@@ -280,8 +284,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             if (mine) {
                 const int slot = count - 1 - tid;
                 if (gst)
-                    g = Guided{gst[slot], gst[kStack + slot], gst[2 * kStack + slot],
-                               cf{gst[3 * kStack + slot], gst[4 * kStack + slot]}};
+                    g = Guided{gst[slot], gst[kCap + slot], gst[2 * kCap + slot],
+                               cf{gst[3 * kCap + slot], gst[4 * kCap + slot]}};
                 o = mk3(S.ox[slot], S.oy[slot], S.oz[slot]);
                 din = mk3(S.dx[slot], S.dy[slot], S.dz[slot]);
 #pragma unroll
@@ -323,7 +327,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     f3 hp, n2;
                     float cosT2;
                     if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n2, cosT2)) {
-                        push_path<kPhase>(S, gst, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
+                        push_path<kPhase, kCap>(S, gst, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
                         alive = true;
                     }
                 }
@@ -372,11 +376,37 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
 #undef HSR_BANDWIDTH
 }
 
-// The launch of one instantiation (dynamic shared memory `smem`).
-template <int kPhase, bool kMixed>
-void wave_instance(const TraceParams &p, int grid, size_t smem, cudaStream_t st) {
-    cudaFuncSetAttribute(k_wave<kPhase, kMixed>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k_wave<kPhase, kMixed><<<grid, kThreads, smem, st>>>(p);
+// Dynamic shared memory of a launch: the stack, the range row of N bins and, guided, the
+// CTA's training sums and the guiding part of the stacked paths.
+template <int kQueue> size_t wave_smem_for(int samples, bool guided) {
+    constexpr int kCap = kThreads + kQueue;
+    return sizeof(WaveShared<kCap>) + 2 * size_t(samples) * sizeof(float) +
+           (guided ? (kGuideMaxNodes + kGuideStackFields * kCap) * sizeof(float) : 0);
+}
+
+// The stack capacity a launch runs with: 320 entries when its queue threshold is set at
+// 64 or less (the mixed serving form always uses 384).
+inline bool wave_small_stack(const TraceParams &p) {
+    return !p.jobs && p.queue_threshold > 0 && p.queue_threshold <= kWaveSmallQueue;
+}
+
+// The launch of one instantiation.
+template <int kPhase, bool kMixed, int kQueue>
+void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
+    const size_t smem = wave_smem_for<kQueue>(p.samples, p.do_guide != 0);
+    cudaFuncSetAttribute(k_wave<kPhase, kMixed, kQueue>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k_wave<kPhase, kMixed, kQueue><<<grid, kThreads, smem, st>>>(p);
+}
+
+// Every instantiation of one phase mode: the mixed form, and the uniform form at both
+// stack capacities.
+template <int kPhase> void wave_dispatch(const TraceParams &p, int grid, cudaStream_t st) {
+    if (p.jobs)
+        wave_instance<kPhase, true, kWaveMaxQueueThreshold>(p, grid, st);
+    else if (wave_small_stack(p))
+        wave_instance<kPhase, false, kWaveSmallQueue>(p, grid, st);
+    else
+        wave_instance<kPhase, false, kWaveMaxQueueThreshold>(p, grid, st);
 }
 
 }  // namespace

@@ -7,11 +7,8 @@
 
 namespace hsr {
 
-void launch_wave_split(const TraceParams &p, bool mixed, int grid, size_t smem, cudaStream_t st) {
-    if (mixed)
-        wave_instance<HSR_PHASE_SPLIT_FP64, true>(p, grid, smem, st);
-    else
-        wave_instance<HSR_PHASE_SPLIT_FP64, false>(p, grid, smem, st);
+void launch_wave_split(const TraceParams &p, int grid, cudaStream_t st) {
+    wave_dispatch<HSR_PHASE_SPLIT_FP64>(p, grid, st);
 }
 
 }  // namespace hsr
