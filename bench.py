@@ -144,8 +144,8 @@ class ClockSampler:
         os.unlink(self.path)
         if not sm:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def l2_read_gbs(mib=32, sweeps=64):
@@ -499,12 +499,17 @@ def time_to_error():
                            the exact spectrum (its own estimator and reference)
       batched_split_guided[_synth]  the same with device path guiding (PathTracer::run's
                            doubling schedule; unbiased, the same reference)
+      served_split         every pose a request to the serving loop (hsr_server_*, split-FP64
+                           phase), all submitted at once and timed until the last row is on
+                           the host; a served row is the batched split row up to summation
+                           order (the same Halton samples), so it is timed at the budget the
+                           batched split form needs, and its error there is reported
     A form that does not reach the target by the scene's largest budget (2^31 sphere,
     2^26 dihedral) reports the budget extrapolated
     from the slope of its last six points (log error vs log budget) and the time for it
     at its measured throughput, marked "extrapolated"."""
     from hussar_gb300 import (HSR_PHASE_REFERENCE_FP32, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16,
-                              HSR_SPLAT_FINE_SYNTH, PathTracer, _lib, gb300, scenes)
+                              HSR_SPLAT_FINE_SYNTH, PathTracer, Server, _lib, gb300, scenes)
     L = _lib.lib()
     out = {"target_rel_l2": TTE_TARGET,
            "reference": "split-FP64 phase, same splat kernel, Halton indices from %d (disjoint from the forms'); "
@@ -516,6 +521,8 @@ def time_to_error():
              "batched_split_synth": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, False, False),
              "batched_split_guided": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16, False, True),
              "batched_split_synth_guided": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, False, True)}
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     for name, w in (("sphere_ground", scenes.sphere_ground_workload()), ("dihedral_91", scenes.dihedral_workload())):
         ref_guided, ref_log2, max_log2 = TTE_SCENES[name]
         plain_t, guided_t = PathTracer(), PathTracer()
@@ -575,16 +582,56 @@ def time_to_error():
                     entry["extrapolated"] = {"slope_per_doubling": slope, "samples_per_pose": timed_s * 2.0 ** extra,
                                              "seconds": sec * 2.0 ** extra}
             res[fname] = entry
+
+        # the served form, at the budget the batched split form reaches the target with
+        bs = res["batched_split"]
+        s_budget = bs["samples_per_pose"] or (1 << max_log2)
+        srv = Server(flags=plain_t, phase_mode=HSR_PHASE_SPLIT_FP64, max_slots=max(P, 1), max_samples_per_chirp=N)
+        try:
+            sid = srv.add_scene(be)
+
+            def serve_all():
+                reqs = [srv.submit(sid, w.rf, N, w.tx[k], w.rx[k], s_budget) for k in range(P)]
+                return np.stack([r.result()[0] for r in reqs]).astype(np.complex128)
+
+            rows = serve_all()
+            ref = refs[HSR_SPLAT_DIRICHLET16]
+            entry = {"samples_per_pose": bs["samples_per_pose"], "budget_timed": s_budget,
+                     "error_at_budget": float(np.linalg.norm(rows - ref) / np.linalg.norm(ref))}
+            # timed alternately with the batched split call at the same budget, so that both
+            # see the same clock state
+            times, batch_times = [], []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                serve_all()
+                times.append(time.perf_counter() - t0)
+                t0 = time.perf_counter()
+                run(forms["batched_split"], s_budget)
+                batch_times.append(time.perf_counter() - t0)
+            sec = float(np.median(times))
+            entry["batched_split_seconds_same_budget"] = float(np.median(batch_times))
+            if bs["samples_per_pose"]:
+                entry["seconds"] = sec
+            elif bs.get("extrapolated"):
+                scale = bs["extrapolated"]["samples_per_pose"] / s_budget
+                entry["extrapolated"] = {"samples_per_pose": bs["extrapolated"]["samples_per_pose"],
+                                         "seconds": sec * scale}
+            entry["server"] = {k: v for k, v in srv.stats().items() if k in ("ticks", "max_batch", "device_ms")}
+            res["served_split"] = entry
+        finally:
+            srv.close()
+
         def seconds(e):
             return e.get("seconds") or (e.get("extrapolated") or {}).get("seconds")
 
         plain = seconds(res["plain_gpu"])
-        for fname in forms:
+        for fname in list(forms) + ["served_split"]:
             if fname != "plain_gpu" and fname in res:
                 sec = seconds(res[fname])
                 res[fname]["speedup_vs_plain_gpu"] = (plain / sec) if (plain and sec) else None
         out[name] = dict(res, poses=P, range_bins=N, triangles=w.mesh.triangleCount(), reference_log2=ref_log2,
                          reference_guided=ref_guided)
+    out["clocks"] = clocks.stop()  # over the whole measurement
     return out
 
 

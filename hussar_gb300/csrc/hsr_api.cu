@@ -957,6 +957,9 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         d.tuned = saved;
         return st;
     }
+    // store the shape explicitly: a threshold of 0 means "the default" to the kernel, but
+    // the serving ticks read the scene's tuned threshold to pick their path stack
+    if (best.queue_threshold <= 0) best.queue_threshold = kWaveMaxQueueThreshold;
     d.tuned = best;
     out_best->tile = best.tile > 0 ? best.tile : kTile;
     out_best->ctas_per_sm = best.ctas_per_sm;

@@ -132,6 +132,9 @@ struct TraceParams {
     // wavefront kernel: GENERATE runs while a CTA holds at most this many live paths
     // (<= kWaveStack - 256; 0: that maximum)
     int32_t queue_threshold;
+    // uniform batch, wavefront kernel: the first double of each pose's 2N accumulators in
+    // acc (a serving tick whose requests share scene, chirp and N); nullptr: pose-major rows
+    const int64_t *acc_row;
 };
 
 

@@ -49,6 +49,7 @@ using Clock = std::chrono::steady_clock;
 constexpr int32_t kServeTile = 1024;  // samples per work item
 constexpr int kTickSlots = 2;
 constexpr int kTilesPerCta = 4;  // minimum tick size, in tiles per resident CTA
+constexpr int32_t kServeMaxTile = 16384;  // largest work item of a tick with large chunks
 constexpr int kEndRing = 4;      // tick-end events kept for the busy-time union
 
 struct FinJob {
@@ -138,7 +139,7 @@ using ReqPtr = std::shared_ptr<Req>;
 
 // Fixed layout of a tick's input block (host pinned and device), for `cap` segments.
 struct TickLayout {
-    size_t counters = 0, tile = 0, budget = 0, offset = 0, tx = 0, rx = 0, jobs = 0, fin = 0, bytes = 0;
+    size_t counters = 0, tile = 0, budget = 0, offset = 0, tx = 0, rx = 0, jobs = 0, acc_row = 0, fin = 0, bytes = 0;
     void init(int cap) {
         size_t o = 0;
         counters = o;
@@ -155,6 +156,8 @@ struct TickLayout {
         o = align256(o + sizeof(hsr_antenna) * cap);
         jobs = o;
         o = align256(o + sizeof(PoseJob) * cap);
+        acc_row = o;
+        o = align256(o + sizeof(int64_t) * cap);
         fin = o;
         o = align256(o + sizeof(FinJob) * cap);
         bytes = o;
@@ -324,6 +327,16 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     for (int i = 0; i < n; ++i) remaining[i] = cand[i]->r.budget - cand[i]->scheduled;
     const double target = std::min(std::max(rate * double(cfg.tick_ms), double(min_tick)), double(int64_t(1) << 32));
     plan_tick(n, remaining.data(), int64_t(target), kServeTile, chunk.data());
+    // work items of this tick: kServeTile samples, or larger (up to kServeMaxTile) when the
+    // tick still has kTilesPerCta items per resident CTA at the larger size. A CTA pulls
+    // items spaced by the number of CTAs, pose-major, so with many requests in a tick it
+    // changes pose (stack drain, row flush) nearly every item; larger items amortise that.
+    int64_t tick_samples = 0;
+    for (int i = 0; i < n; ++i) tick_samples += chunk[i];
+    const int64_t resident_ctas = min_tick / (int64_t(kTilesPerCta) * kServeTile);
+    int32_t tick_tile = kServeTile;
+    while (tick_tile < kServeMaxTile && tick_samples >= 2 * int64_t(tick_tile) * kTilesPerCta * resident_ctas)
+        tick_tile *= 2;
 
     // fill the tick block: segments in ascending remainder (shortest first)
     std::vector<int> order(n);
@@ -337,11 +350,16 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     hsr_antenna *tx = reinterpret_cast<hsr_antenna *>(h + layout.tx);
     hsr_antenna *rx = reinterpret_cast<hsr_antenna *>(h + layout.rx);
     PoseJob *jobs = reinterpret_cast<PoseJob *>(h + layout.jobs);
+    int64_t *acc_row = reinterpret_cast<int64_t *>(h + layout.acc_row);
     FinJob *fin = reinterpret_cast<FinJob *>(h + layout.fin);
     t.members.clear();
     t.finishing.clear();
     t.samples = 0;
     int P = 0, F = 0, maxN = 1;
+    int32_t queue_threshold = kWaveMaxQueueThreshold;  // lowered by any scene not tuned above 64
+    // a tick whose requests share one scene, chirp and N runs the uniform kernel
+    bool uniform = true;
+    const ReqPtr *first = nullptr;
     int64_t out_off = 0;
     tile[0] = 0;
     for (int i : order) {
@@ -358,8 +376,16 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             j.samples = q->r.samples_per_chirp;
             j.reserved = 0;
             j.acc_offset = q->arena_off / int64_t(sizeof(double));
-            tile[P + 1] = tile[P] + (chunk[i] + kServeTile - 1) / kServeTile;
+            acc_row[P] = j.acc_offset;
+            if (!first) {
+                first = &q;
+            } else if ((*first)->scene != q->scene || (*first)->r.samples_per_chirp != q->r.samples_per_chirp ||
+                       std::memcmp(&(*first)->r.rf, &q->r.rf, sizeof(hsr_rf_config)) != 0) {
+                uniform = false;
+            }
+            tile[P + 1] = tile[P] + (chunk[i] + tick_tile - 1) / tick_tile;
             maxN = std::max(maxN, q->r.samples_per_chirp);
+            if (q->scene->tuned.queue_threshold <= kWaveSmallQueue) queue_threshold = kWaveSmallQueue;
             ++P;
             q->scheduled += chunk[i];
             q->ticks += 1;
@@ -396,11 +422,27 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
         p.offset = reinterpret_cast<const int64_t *>(t.d_in + layout.offset);
         p.tile_start = reinterpret_cast<const int64_t *>(t.d_in + layout.tile);
         p.sample_weight = 1.f;
-        p.tile = kServeTile;
+        p.tile = tick_tile;
         p.acc = d_arena;
         p.status = reinterpret_cast<unsigned *>(t.d_in + layout.counters);
         p.work_counter = p.status + 2;
         p.jobs = reinterpret_cast<const PoseJob *>(t.d_in + layout.jobs);
+        // the path stack and GENERATE threshold of the tick: the large stack only when
+        // every scene in it was autotuned to a threshold above 64 (hsr_autotune_batch);
+        // otherwise, and for scenes never tuned, the small stack (the faster one on dense
+        // scenes, where it leaves more of the L1 to the BVH)
+        p.queue_threshold = queue_threshold;
+        if (uniform) {
+            // one scene, chirp and N: the uniform kernel (no per-pose job loads, fewer
+            // registers), writing each request's rows through acc_row
+            const ReqPtr &q0 = *first;
+            p.jobs = nullptr;
+            p.nodes = q0->scene->nodes;
+            p.tris = q0->scene->tris;
+            p.rf = q0->r.rf;
+            p.samples = q0->r.samples_per_chirp;
+            p.acc_row = reinterpret_cast<const int64_t *>(t.d_in + layout.acc_row);
+        }
         auto it = blocks_cache.find(maxN);
         if (it == blocks_cache.end()) it = blocks_cache.emplace(maxN, wave_blocks_per_sm(maxN, true)).first;
         if (launch_wave(p, cfg.phase_mode, sm_count * it->second, stream, err) != 0) e = cudaErrorLaunchFailure;

@@ -8,12 +8,13 @@ size_t wave_smem_bytes(int samples, bool guided) { return wave_smem_for<kWaveMax
 
 int wave_blocks_per_sm(int samples, bool mixed) {
     int nb = 0;
-    const size_t smem = wave_smem_bytes(samples, false);
     if (mixed) {
-        auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, true, kWaveMaxQueueThreshold>;
+        const size_t smem = wave_smem_for<kWaveSmallQueue>(samples, false);
+        auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, true, kWaveSmallQueue>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);
     } else {
+        const size_t smem = wave_smem_bytes(samples, false);
         auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, false, kWaveMaxQueueThreshold>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);

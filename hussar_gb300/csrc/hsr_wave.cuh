@@ -39,7 +39,7 @@ constexpr int kThreads = 256;
 // paths left when GENERATE runs (the queue threshold). Two capacities are built: 384
 // entries (threshold up to 128) and 320 (up to 64), whose 5 KB less shared memory per
 // CTA leaves more of the SM's L1 to the BVH (4 % on the dense boxes scenes, which the
-// autotuner runs at threshold 64).
+// autotuner runs at threshold 32 or 64; the serving ticks always use it).
 template <int kCap> struct WaveShared {
     float ox[kCap], oy[kCap], oz[kCap];  // hit point (origin of the next segment)
     float dx[kCap], dy[kCap], dz[kCap];  // incoming direction
@@ -135,10 +135,12 @@ __device__ __forceinline__ float max_distance(const hsr_rf_config &rf) {
 }
 __device__ __forceinline__ float chirp_bandwidth(const hsr_rf_config &rf) { return rf.freqSlope * rf.rampTime; }
 
-// FP64 accumulator row of a pose: pose-major rows of N, or the pose's job row.
+// FP64 accumulator row of a pose: the pose's job row (mixed), its listed row, or
+// pose-major rows of 2N.
 template <bool kMixed, class Shared>
 __device__ __forceinline__ double *pose_row(const TraceParams &p, const Shared &S, int pose) {
-    return kMixed ? p.acc + S.job.acc_offset : p.acc + 2 * int64_t(pose) * p.samples;
+    if (kMixed) return p.acc + S.job.acc_offset;
+    return p.acc + (p.acc_row ? __ldg(&p.acc_row[pose]) : 2 * int64_t(pose) * p.samples);
 }
 
 // Four CTAs per SM (64 registers): the spills cost less than the latency the extra
@@ -384,10 +386,10 @@ template <int kQueue> size_t wave_smem_for(int samples, bool guided) {
            (guided ? (kGuideMaxNodes + kGuideStackFields * kCap) * sizeof(float) : 0);
 }
 
-// The stack capacity a launch runs with: 320 entries when its queue threshold is set at
-// 64 or less (the mixed serving form always uses 384).
+// The stack capacity a uniform launch runs with: 320 entries when its queue threshold
+// is set at 64 or less.
 inline bool wave_small_stack(const TraceParams &p) {
-    return !p.jobs && p.queue_threshold > 0 && p.queue_threshold <= kWaveSmallQueue;
+    return p.queue_threshold > 0 && p.queue_threshold <= kWaveSmallQueue;
 }
 
 // The launch of one instantiation.
@@ -398,12 +400,17 @@ void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
     k_wave<kPhase, kMixed, kQueue><<<grid, kThreads, smem, st>>>(p);
 }
 
-// Every instantiation of one phase mode: the mixed form, and the uniform form at both
-// stack capacities.
+// Every instantiation of one phase mode: the mixed form (serving ticks) and the uniform
+// form, each at both stack capacities. The mixed form takes the small stack unless the
+// tick asks for a threshold above 64 (its default: on the serving mix of dense boxes
+// and urban scenes it gives 1.18x the capacity of the 384-entry stack).
 template <int kPhase> void wave_dispatch(const TraceParams &p, int grid, cudaStream_t st) {
-    if (p.jobs)
-        wave_instance<kPhase, true, kWaveMaxQueueThreshold>(p, grid, st);
-    else if (wave_small_stack(p))
+    if (p.jobs) {
+        if (p.queue_threshold > kWaveSmallQueue)
+            wave_instance<kPhase, true, kWaveMaxQueueThreshold>(p, grid, st);
+        else
+            wave_instance<kPhase, true, kWaveSmallQueue>(p, grid, st);
+    } else if (wave_small_stack(p))
         wave_instance<kPhase, false, kWaveSmallQueue>(p, grid, st);
     else
         wave_instance<kPhase, false, kWaveMaxQueueThreshold>(p, grid, st);

@@ -352,7 +352,10 @@ hsr_status hsr_batch_graph_destroy(hsr_batch_graph *graph);
  * device memory for their accumulators are free. A request's result is the row
  * hsr_simulate_batch gives for the same scene, pose, chirp, budget and index offset
  * (the same Halton samples; only the summation order differs). The tracer flags and the
- * phase mode are per server; geometrical optics must be on and guiding off. */
+ * phase mode are per server; geometrical optics must be on and guiding off. A tick runs
+ * the larger path stack (GENERATE threshold 128) only when every scene in it was
+ * autotuned (hsr_autotune_batch) to a threshold above 64, and larger work items when
+ * its requests' chunks are large. */
 typedef struct hsr_server hsr_server;
 
 typedef struct hsr_server_config {

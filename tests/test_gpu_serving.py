@@ -168,3 +168,33 @@ def test_close_with_work_queued_returns(resident):
     t0 = time.time()
     srv.close()
     assert time.time() - t0 < 20
+
+
+@pytest.mark.parametrize("threshold", [0, 128], ids=["untuned-small-stack", "tuned-large-stack"])
+def test_uniform_ticks_equal_batch_rows(resident, threshold):
+    """Requests that share one scene, chirp and N run as uniform ticks (the batch kernel
+    writing each request's arena row), on the small path stack for a scene never tuned
+    and the large one for a scene tuned to threshold 128; large budgets span several
+    ticks with work items above 1024 samples. Rows equal the batch call's."""
+    w, be = resident[1]
+    if threshold:
+        be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=threshold)
+    try:
+        t = tracer(w.max_depth)
+        rf = scenes.rf_chirp(bandwidth=2e9, samples=256)
+        P = 6
+        budget = np.array([(1 << 24) + 777 * k for k in range(P)], np.int64)
+        offset = np.array([0, 1 << 20, 0, 12345, 0, 7], np.int64)
+        tx = [w.tx[0]] * P
+        rx = [w.rx[0]] * P
+        with Server(flags=t, max_slots=16) as srv:
+            sid = srv.add_scene(be)
+            reqs = [srv.submit(sid, rf, 256, tx[k], rx[k], int(budget[k]), int(offset[k])) for k in range(P)]
+            rows = [r.result()[0] for r in reqs]
+            st = srv.stats()
+        ref = be.simulate_batch(rf, 256, t, tx, rx, budget, index_offset=offset)
+        assert st["ticks"] > 1
+        for k in range(P):
+            assert rel_l2(rows[k], ref[k]) <= 1e-5, k
+    finally:
+        be.set_launch_config(default=True)
