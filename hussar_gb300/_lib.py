@@ -56,6 +56,11 @@ class AntennaC(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("rotation", ctypes.c_float * 9)]
 
 
+class FfAntennaC(ctypes.Structure):
+    _fields_ = [("direction", ctypes.c_float * 3), ("polarization", ctypes.c_float * 6),
+                ("scene_center", ctypes.c_float * 3), ("radius", ctypes.c_float)]
+
+
 class FlagsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in
                 ("onlyIndirect", "maxDepth", "useGeometricalOptics", "poDiffraction", "doGuiding",
@@ -154,6 +159,8 @@ def lib():
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
         "hsr_debug_halton": [vp, ctypes.c_int64, ctypes.c_int32, vp],
+        "hsr_simulate_batch_ff": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
+                                  ctypes.c_int32, vp],
         "hsr_autotune_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                ctypes.c_int32, ctypes.c_int32, P(LaunchConfigC)],
         "hsr_set_launch_config": [vp, P(LaunchConfigC)],

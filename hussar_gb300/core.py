@@ -101,6 +101,33 @@ class NFAntenna:
         return a
 
 
+class FFAntenna:
+    """hussar::FFAntenna (emitter.h:218-291): a far-field antenna (plane wave), a disk of
+    `radius` at sceneCenter + dir * radius facing the scene. Rays leave it along -dir;
+    it is reached along +dir. `polarization` is the complex H field (3 components),
+    orthogonal to `dir`; `dir` is normalised (the reference asserts both)."""
+
+    def __init__(self, dir, polarization, sceneCenter, radius):
+        self.direction = np.asarray(dir, np.float32).reshape(3)
+        self.polarization = np.asarray(polarization, np.complex64).reshape(3)
+        self.scene_center = np.asarray(sceneCenter, np.float32).reshape(3)
+        self.radius = np.float32(radius)
+        if abs(float(np.linalg.norm(self.direction.astype(np.float64))) - 1.0) > 1e-3:
+            raise ValueError("normal of plane wave must be normalized")
+        if abs(complex(np.dot(self.direction.astype(np.complex128), self.polarization.astype(np.complex128)))) > 1e-3:
+            raise ValueError("H-field must be orthogonal to direction of propagation")
+        if not self.radius > 0:
+            raise ValueError("radius must be positive")
+
+    def to_c(self):
+        a = _lib.FfAntennaC()
+        a.direction[:] = [float(x) for x in self.direction]
+        a.polarization[:] = [float(x) for x in np.stack([self.polarization.real, self.polarization.imag], 1).reshape(-1)]
+        a.scene_center[:] = [float(x) for x in self.scene_center]
+        a.radius = float(self.radius)
+        return a
+
+
 class Scene:
     """hussar::Scene (scene.h:9-14): RF configuration plus the RX and TX antennas."""
 
@@ -340,6 +367,22 @@ class _GB300:
                 self._scene, ctypes.byref(rf.to_c()), int(samples_per_chirp), ctypes.byref(integrator.flags_c()),
                 P, ctypes.cast(txa, ctypes.c_void_p), ctypes.cast(rxa, ctypes.c_void_p), _lib.ptr(b), _lib.ptr(off),
                 int(phase_mode), int(splat_mode), _lib.ptr(out), ctypes.c_void_p(stream)))
+            return out
+
+        def simulate_batch_ff(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None,
+                              phase_mode=_lib.HSR_PHASE_REFERENCE_FP32):
+            """Far-field runs (hsr_simulate_batch_ff): tx, rx sequences of FFAntenna, one
+            per pose; returns each pose's fetchFrame() row (complex64)."""
+            P = len(tx)
+            txa = (_lib.FfAntennaC * P)(*[a.to_c() for a in tx])
+            rxa = (_lib.FfAntennaC * P)(*[a.to_c() for a in rx])
+            b = np.ascontiguousarray(budget, np.int64)
+            off = np.zeros(P, np.int64) if index_offset is None else np.ascontiguousarray(index_offset, np.int64)
+            out = np.zeros((P, samples_per_chirp), np.complex64)
+            _lib.check(_lib.lib().hsr_simulate_batch_ff(
+                self._scene, ctypes.byref(rf.to_c()), int(samples_per_chirp), ctypes.byref(integrator.flags_c()),
+                P, ctypes.cast(txa, ctypes.c_void_p), ctypes.cast(rxa, ctypes.c_void_p), _lib.ptr(b), _lib.ptr(off),
+                int(phase_mode), _lib.ptr(out)))
             return out
 
         def batch_graph(self, rf, samples_per_chirp, integrator, pose_count, d_tx, d_rx, d_budget, d_offset,

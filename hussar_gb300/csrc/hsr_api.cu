@@ -64,6 +64,8 @@ static hsr_status validate_phase(int32_t phase_mode, int32_t splat_mode) {
 // Per-batch scratch for P poses with N bins, carved from one allocation owned by the scene.
 struct Scratch {
     hsr_antenna *tx, *rx;
+    hsr_ff_antenna *ff_tx, *ff_rx;  // far-field poses (hsr_simulate_batch_ff)
+    bool far_field = false;         // the pass traces ff_tx/ff_rx instead of tx/rx
     int64_t *budget, *offset, *tile_start;
     float *weights;
     int *train, *active, *clear;
@@ -89,6 +91,8 @@ static Scratch carve(void *base, int32_t P, int32_t N, bool fine) {
     s.counters = reinterpret_cast<unsigned *>(take(64));
     s.tx = reinterpret_cast<hsr_antenna *>(take(sizeof(hsr_antenna) * P));
     s.rx = reinterpret_cast<hsr_antenna *>(take(sizeof(hsr_antenna) * P));
+    s.ff_tx = reinterpret_cast<hsr_ff_antenna *>(take(sizeof(hsr_ff_antenna) * P));
+    s.ff_rx = reinterpret_cast<hsr_ff_antenna *>(take(sizeof(hsr_ff_antenna) * P));
     s.budget = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * P));
     s.offset = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * P));
     s.tile_start = reinterpret_cast<int64_t *>(take(sizeof(int64_t) * (P + 1)));
@@ -246,6 +250,10 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     p.weights = per_pose_weights ? s.weights : nullptr;
     p.fine = splat_mode == HSR_SPLAT_FINE_SYNTH ? s.fine : nullptr;
     p.fine_bins = kFineOS * N;
+    if (s.far_field) {
+        p.ff_tx = s.ff_tx;
+        p.ff_rx = s.ff_rx;
+    }
     p.do_guide = (fl->doGuiding && g) ? 1 : 0;
     if (p.do_guide) {
         p.train = s.train;
@@ -256,7 +264,8 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     } else {
         p.flags.doGuiding = 0;
     }
-    const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
+    // far-field runs take the one-thread-per-sample kernel
+    const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters && !s.far_field;
     int per_sm = wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0);
     if (wave && tuned) {
         if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);
@@ -883,6 +892,40 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         cudaSuccess)
         return cuda_fail(e, "row download");
     if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "batch run");
+    return read_status(sc, strm);
+}
+
+hsr_status hsr_simulate_batch_ff(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,
+                                 int32_t P, const hsr_ff_antenna *tx, const hsr_ff_antenna *rx, const int64_t *budget,
+                                 const int64_t *offset, int32_t phase_mode, float *out_rows) {
+    if (!s || !tx || !rx || !budget || !offset || !out_rows || P <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no poses");
+    hsr_status st = validate_common(rf, N, fl);
+    if (st != HSR_OK) return st;
+    if (fl->doGuiding) return fail(HSR_ERR_NOT_SUPPORTED, "far-field runs are plain (doGuiding = 0)");
+    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
+    for (int32_t i = 0; i < P; ++i) {
+        if (budget[i] < 0 || offset[i] < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
+        for (const hsr_ff_antenna *a : {tx + i, rx + i})
+            if (!(a->radius > 0.f)) return fail(HSR_ERR_INVALID_ARGUMENT, "far-field antenna radius must be positive");
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scratch sc;
+    if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
+    sc.far_field = true;
+    cudaStream_t strm = nullptr;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(sc.ff_tx, tx, sizeof(hsr_ff_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(sc.ff_rx, rx, sizeof(hsr_ff_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(sc.budget, budget, sizeof(int64_t) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(sc.offset, offset, sizeof(int64_t) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess)
+        return cuda_fail(e, "far-field pose upload");
+    st = run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, HSR_SPLAT_DIRICHLET16, 1, sc.rows, strm);
+    if (st != HSR_OK) return st;
+    if ((e = cudaMemcpyAsync(out_rows, sc.rows, sizeof(float) * 2 * size_t(P) * N, cudaMemcpyDeviceToHost, strm)) !=
+        cudaSuccess)
+        return cuda_fail(e, "row download");
+    if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "far-field batch run");
     return read_status(sc, strm);
 }
 

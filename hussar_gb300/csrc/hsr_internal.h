@@ -132,6 +132,10 @@ struct TraceParams {
     // wavefront kernel: GENERATE runs while a CTA holds at most this many live paths
     // (<= kWaveStack - 256; 0: that maximum)
     int32_t queue_threshold;
+    // far-field runs (hsr_simulate_batch_ff), per-thread kernel: each pose's TX and RX;
+    // nullptr: the near-field antennas tx/rx above
+    const hsr_ff_antenna *ff_tx;
+    const hsr_ff_antenna *ff_rx;
     // uniform batch, wavefront kernel: the first double of each pose's 2N accumulators in
     // acc (a serving tick whose requests share scene, chirp and N); nullptr: pose-major rows
     const int64_t *acc_row;

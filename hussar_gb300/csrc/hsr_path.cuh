@@ -229,23 +229,80 @@ struct NeeOut {
     bool splat;    // passed the splat early-out
 };
 
+// FFAntenna (libhussar/include/hussar/core/emitter.h:226-291) of one pose, with what its
+// constructor and sample() derive: the disk centre (sceneCenter + dir * radius), the
+// disk frame buildFrame(-dir) (core/geometry.h:45-53) and the pdf 1 / (4 radius^2),
+// formed in double and rounded once, as the reference's
+// `Float pdf = 1 / (4 * std::pow(m_radius, 2))` is.
+struct FfAnt {
+    f3 dir, center, e0, e1;
+    c3 pol;
+    float radius, pdf;
+};
+
+__device__ __forceinline__ FfAnt load_ff(const hsr_ff_antenna *a) {
+    FfAnt r;
+    r.dir = mk3(__ldg(&a->direction[0]), __ldg(&a->direction[1]), __ldg(&a->direction[2]));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) r.pol.v[i] = cf{__ldg(&a->polarization[2 * i]), __ldg(&a->polarization[2 * i + 1])};
+    r.radius = __ldg(&a->radius);
+    const f3 c = mk3(__ldg(&a->scene_center[0]), __ldg(&a->scene_center[1]), __ldg(&a->scene_center[2]));
+    r.center = add3(c, scl3(r.radius, r.dir));
+    const f3 d = neg3(r.dir);
+    if (fabsf(d.x) > fabsf(d.y))
+        r.e0 = div3(mk3(-d.z, 0.f, d.x), sqrtf(d.x * d.x + d.z * d.z));
+    else
+        r.e0 = div3(mk3(0.f, d.z, -d.y), sqrtf(d.y * d.y + d.z * d.z));
+    r.e1 = crs3(d, r.e0);
+    r.pdf = __double2float_rn(1.0 / (4.0 * (double(r.radius) * double(r.radius))));
+    return r;
+}
+
+// FFAntenna::sample (emitter.h:241-248): a point of the disk's square (2u - 1, 2v - 1)
+// in the disk frame, scaled by the radius; the ray travels along -dir; H = pol / pdf.
+__device__ __forceinline__ void ff_sample(const FfAnt &a, float u0, float u1, f3 &o, f3 &d, c3 &H) {
+    const float s0 = 2.f * u0 - 1.f, s1 = 2.f * u1 - 1.f;
+    const f3 q = mk3(a.e0.x * s0 + a.e1.x * s1, a.e0.y * s0 + a.e1.y * s1, a.e0.z * s0 + a.e1.z * s1);
+    o = add3(scl3(a.radius, q), a.center);
+    d = neg3(a.dir);
+    H = c3_div(a.pol, a.pdf);
+}
+
 // Returns false when the estimate is occluded or skipped (no record, no splat).
 // depth == 0: direct TX->RX connection (only with onlyIndirect = false).
 // `nodes`/`tris` are the scene the pose traces, `rf`/`samples` its chirp and range bins
-// (uniform over a launch, or the pose's PoseJob in a mixed batch).
-template <int kPhase, bool kCount>
+// (uniform over a launch, or the pose's PoseJob in a mixed batch). kFF: far-field TX and
+// RX (`ff_rx` the receiver): FFAntenna::nee replaces NFAntenna::nee, and the direct term
+// is zero (FFAntenna::evaluate zeroes the ray, emitter.h:253-255).
+template <int kPhase, bool kCount, bool kFF = false>
 __device__ __forceinline__ bool nee_eval(const TraceParams &p, const DNode *nodes, const DTri *tris,
                                          const hsr_rf_config &rf, int samples, const Ant &tx, const Ant &rx, int depth,
                                          f3 o, f3 d, f3 tmpd, f3 hit_n, const c3 &inc_H, const c3 &H, float time,
                                          double plen, float r, float cosTheta, float freq, float sampleWeight,
-                                         NeeOut &out, TraversalCounters *cnt, unsigned *rays) {
+                                         NeeOut &out, TraversalCounters *cnt, unsigned *rays,
+                                         const FfAnt *ff_rx = nullptr) {
     const hsr_tracer_flags &fl = p.flags;
-    // NFAntenna::nee (emitter.h:195-203)
-    f3 nd = sub3(rx.pos, o);
-    float rr = nrm3(nd);
-    nd = div3(nd, rr);
+    f3 nd;
+    float rr;
+    c3 Hrx;
+    if (kFF) {
+        if (depth == 0) return false;
+        // FFAntenna::nee (emitter.h:261-273): along +dir to the disk's plane, while the
+        // point projects within 1 of the disk centre (else H = 0: nothing to splat)
+        f3 local = sub3(o, ff_rx->center);
+        local = sub3(local, scl3(dot3(local, ff_rx->dir), ff_rx->dir));
+        if (nrm3(local) > 1.f) return false;
+        nd = ff_rx->dir;
+        rr = nrm3(sub3(add3(local, ff_rx->center), o));
+        Hrx = c3_scl(ff_rx->pol, 4.f * kPi * rr);
+    } else {
+        // NFAntenna::nee (emitter.h:195-203)
+        nd = sub3(rx.pos, o);
+        rr = nrm3(nd);
+        nd = div3(nd, rr);
+        Hrx = mulcv(rx.rot, awr_eval(mulTv(rx.rot, neg3(nd))));
+    }
     const float tMax = rr;
-    c3 Hrx = mulcv(rx.rot, awr_eval(mulTv(rx.rot, neg3(nd))));
     if (!fl.poDiffraction) {
         if (kCount) (*rays)++;
         if (any_hit<kCount>(nodes, tris, o, nd, kEpsilon, tMax, p.status, cnt)) return false;

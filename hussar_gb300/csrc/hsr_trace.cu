@@ -27,9 +27,11 @@ struct PathRecord {  // one next-event estimate (tests only)
 };
 
 // One sample, one thread: PathTracer::sample (path.h:235-451) for every flag combination.
-template <int kPhase, bool kRecord, bool kCount>
+// kFF: the pose's TX and RX are far-field antennas (ftx, frx; FFAntenna, emitter.h:226-291).
+template <int kPhase, bool kRecord, bool kCount, bool kFF>
 __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t hindex, float *s_re, float *s_im,
-                             PathRecord *rec, int max_rec, TraversalCounters *cnt, unsigned *rays) {
+                             PathRecord *rec, int max_rec, TraversalCounters *cnt, unsigned *rays, const FfAnt &ftx,
+                             const FfAnt &frx) {
     const Ant &tx = pc.tx;
     const Ant &rx = pc.rx;
     const hsr_rf_config &rf = p.rf;
@@ -60,8 +62,12 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
             px = halton(hindex, dim++);
             py = halton(hindex, dim++);
             if (fl.doGuiding) primaryPdf = guide_sample(pc.samp_child, pc.samp_p, px, py);
-            o = tx.pos;
-            antenna_sample(tx, px, py, d, H);
+            if (kFF) {
+                ff_sample(ftx, px, py, o, d, H);
+            } else {
+                o = tx.pos;
+                antenna_sample(tx, px, py, d, H);
+            }
             H = c3_scl(H, 1.f / primaryPdf);
         } else if (!fl.useGeometricalOptics) {
             float u0 = halton(hindex, dim++);
@@ -75,8 +81,9 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
         // next event estimation towards the single RX antenna (path.h:292-397)
         if (!(depth == 0 && fl.onlyIndirect)) {
             NeeOut ne;
-            if (nee_eval<kPhase, kCount>(p, p.nodes, p.tris, p.rf, p.samples, tx, rx, depth, o, d, tmpd, hit_n,
-                                         inc_H, H, time, plen, r, cosTheta, freq, pc.weight, ne, cnt, rays)) {
+            if (nee_eval<kPhase, kCount, kFF>(p, p.nodes, p.tris, p.rf, p.samples, tx, rx, depth, o, d, tmpd, hit_n,
+                                              inc_H, H, time, plen, r, cosTheta, freq, pc.weight, ne, cnt, rays,
+                                              &frx)) {
                 gw = cadd(gw, ne.gw_add);
                 if (kRecord && nrec < max_rec) {
                     PathRecord *rc = rec + nrec++;
@@ -113,11 +120,15 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
         cosTheta = fabsf(dot3(hit_n, neg3(d)));
         if (cosTheta < 0.001f) break;
         r += th;
-        time += th / kSpeedOfLight;
-        plen += double(th);
+        // non-GO primary segment of a far-field TX: FFAntenna::connect does nothing (no
+        // time of flight, no 1 / (4 pi r)); every other segment adds its distance
+        if (!(kFF && depth == 0 && !fl.useGeometricalOptics)) {
+            time += th / kSpeedOfLight;
+            plen += double(th);
+        }
         if (!fl.useGeometricalOptics) {
             if (depth == 0) {
-                H = c3_scl(H, 1.f / (4.f * kPi * th));
+                if (!kFF) H = c3_scl(H, 1.f / (4.f * kPi * th));
             } else {
                 H = c3_cmul(H, green(k0, th));
             }
@@ -131,7 +142,7 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
     if (pc.train) guide_train(pc, pc.train_child, pc.train_acc + 2, 3, gw, primaryPdf, px, py);
 }
 
-template <int kPhase, bool kRecord, bool kCount>
+template <int kPhase, bool kRecord, bool kCount, bool kFF = false>
 __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
     TraversalCounters cnt{0u, 0u};
     unsigned rays = 0;
@@ -144,6 +155,7 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
     int cur_pose = -1;
     long long since_flush = 0;  // samples of cur_pose in the row since its last flush (CTA-uniform)
     PoseCtx pc;
+    FfAnt ftx{}, frx{};
     while (true) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = (long long)atomicAdd((unsigned long long *)p.work_counter, 1ull);
@@ -158,14 +170,19 @@ __global__ void __launch_bounds__(256, 2) k_trace(TraceParams p) {
             }
             cur_pose = pose;
             pc = load_pose(p, pose);
+            if (kFF) {
+                ftx = load_ff(p.ff_tx + pose);
+                frx = load_ff(p.ff_rx + pose);
+            }
             since_flush = 0;
         }
         const int64_t budget = __ldg(&p.budget[pose]);
         const int64_t first = (item - __ldg(&p.tile_start[pose])) * p.tile;
         const int64_t last = min(first + p.tile, budget);
         for (int64_t s = first + threadIdx.x; s < last; s += blockDim.x) {
-            trace_sample<kPhase, kRecord, kCount>(p, pc, uint64_t(pc.offset + s), s_re, s_im,
-                                                  kRecord ? records + s * max_rec : nullptr, max_rec, &cnt, &rays);
+            trace_sample<kPhase, kRecord, kCount, kFF>(p, pc, uint64_t(pc.offset + s), s_re, s_im,
+                                                       kRecord ? records + s * max_rec : nullptr, max_rec, &cnt, &rays,
+                                                       ftx, frx);
         }
         since_flush += last - first;
         if (since_flush >= kFlushSamples) {
@@ -298,7 +315,18 @@ int launch_trace(const TraceParams &p, int phase_mode, int splat_mode, int grid,
         cudaFuncSetAttribute(k_trace<HSR_PHASE_REFERENCE_FP32, false, true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
-    if (p.records) {
+    if (p.ff_tx) {
+        if (smem > 48 * 1024) {
+            cudaFuncSetAttribute(k_trace<HSR_PHASE_REFERENCE_FP32, false, false, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            cudaFuncSetAttribute(k_trace<HSR_PHASE_SPLIT_FP64, false, false, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        }
+        if (phase_mode == HSR_PHASE_SPLIT_FP64)
+            k_trace<HSR_PHASE_SPLIT_FP64, false, false, true><<<grid, 256, smem, st>>>(p);
+        else
+            k_trace<HSR_PHASE_REFERENCE_FP32, false, false, true><<<grid, 256, smem, st>>>(p);
+    } else if (p.records) {
         k_trace<HSR_PHASE_REFERENCE_FP32, true, false><<<grid, 256, smem, st>>>(p);
     } else if (p.counters) {
         k_trace<HSR_PHASE_REFERENCE_FP32, false, true><<<grid, 256, smem, st>>>(p);

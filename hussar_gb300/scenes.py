@@ -9,6 +9,9 @@ World frame: y up. Antennas use the mounting of examples/src/1_dihedral.cpp:96-1
   sphere_ground_workload icosphere level 6 (81,920 triangles, r = 0.5 m) on a 20 m x 20 m
                          ground quad, sensor at 10 m range and 0.5 m height, 3 bounces,
                          2^22 samples, 512 ADC samples at 10 MHz
+  dihedral_ff_workload   the same dihedral lit and observed by far-field antennas (plane
+                         waves, FFAntenna): monostatic, directions in the horizontal plane
+                         from 5 to 85 deg azimuth, H along y, disk radius 0.1 m
   boxes_workload         ~1 M triangles of random axis-aligned boxes (edges 0.2-5 m) on a
                          100 m x 100 m ground quad, 4096 poses at 1 m height with random
                          yaw, log-uniform budgets 2^16..2^22, 4 bounces, 256 samples
@@ -17,7 +20,7 @@ import dataclasses
 
 import numpy as np
 
-from .core import NFAntenna, TriangleMesh
+from .core import FFAntenna, NFAntenna, TriangleMesh
 from .radar import FrameConfig, RFConfig
 
 FACING = np.array([[0, 0, -1], [0, -1, 0], [-1, 0, 0]], np.float32)  # 1_dihedral.cpp:96-100
@@ -80,6 +83,23 @@ def dihedral_workload(poses=91, samples_per_pose=1 << 18, size=0.1, distance=1.0
         tx.append(a)
         rx.append(a)
     return Workload("dihedral-4tri-91poses", mesh, rf, fc, tx, rx, np.full(poses, samples_per_pose, np.int64), 2)
+
+
+def dihedral_ff_workload(poses=9, samples_per_pose=1 << 16, size=0.1, radius=0.1):
+    """Monostatic far-field sweep of the dihedral: TX = RX = FFAntenna with direction
+    (cos a, 0, sin a), a = 5..85 deg (the corner opens towards +x+z), H = (0, 1, 0),
+    scene centre the middle of the reflector's bounding cube."""
+    mesh = dihedral_mesh(size)
+    rf, fc = rf_77ghz(256, 5e6)
+    center = np.array([size / 2, size / 2, size / 2], np.float32)
+    tx = []
+    for k in range(poses):
+        a = np.deg2rad(5.0 + 80.0 * k / max(poses - 1, 1))
+        d = np.array([np.cos(a), 0.0, np.sin(a)], np.float32)
+        d /= np.float32(np.linalg.norm(d.astype(np.float64)))
+        tx.append(FFAntenna(d, np.array([0, 1, 0], np.complex64), center, radius))
+    return Workload("dihedral-ff-%dposes" % poses, mesh, rf, fc, tx, list(tx),
+                    np.full(poses, samples_per_pose, np.int64), 2)
 
 
 def icosphere(level, radius=1.0, center=(0, 0, 0)):

@@ -69,6 +69,23 @@ typedef struct hsr_antenna {
     float rotation[9];
 } hsr_antenna;
 
+/* FFAntenna (libhussar/include/hussar/core/emitter.h:218-291): a far-field antenna, a plane
+ * wave in the reference's terms. It is a disk of `radius` centred at
+ * scene_center + direction * radius, facing the scene: as a transmitter it launches rays
+ * along -direction from a uniformly sampled point of the disk's square (2u - 1, 2v - 1 in
+ * the frame of buildFrame(-direction), geometry.h:45-53) with H = polarization / pdf,
+ * pdf = 1 / (4 radius^2); as a receiver it is reached from a hit point p along
+ * +direction over the distance to the disk's plane, with H = polarization * 4 pi * that
+ * distance, and only while p projects within 1 (not `radius`, as the reference tests)
+ * of the disk's centre. `direction` must be normalised and `polarization` orthogonal
+ * to it (complex, re/im per axis). */
+typedef struct hsr_ff_antenna {
+    float direction[3];
+    float polarization[6];
+    float scene_center[3];
+    float radius;
+} hsr_ff_antenna;
+
 /* PathTracer's public configuration members (libhussar/include/hussar/integrators/path.h:153-169)
  * plus Integrator::produceDebugImage (core/integrator.h:58), which in the reference also
  * turns off the zero-contribution early-out of Integrator::splat (integrator.h:121-124).
@@ -230,6 +247,20 @@ hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const hsr_rf_conf
                                              const int64_t *d_budget,
                                              const int64_t *d_index_offset, int32_t phase_mode,
                                              float *d_out_rows, void *stream);
+
+/* Far-field runs (RCS-style): as hsr_simulate_batch for the plain method, with each
+ * pose's TX and RX a far-field antenna (hsr_ff_antenna). In the reference an FFAntenna
+ * derives from Antenna, while Scene holds NFAntenna by value (scene.h:9-14), so
+ * PathTracer::sample (path.h:235-451) is restated here with FFAntenna's sample, nee,
+ * evaluate and connect (emitter.h:241-283): the direct TX -> RX term is zero (evaluate
+ * zeroes the ray), and in the non-GO mode the primary segment adds no time of flight and
+ * no 1 / (4 pi r) (connect does nothing). Runs on the one-thread-per-sample kernel;
+ * doGuiding must be 0 (HSR_ERR_NOT_SUPPORTED otherwise). HOST inputs and outputs,
+ * synchronous. */
+hsr_status hsr_simulate_batch_ff(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
+                                 const hsr_tracer_flags *flags, int32_t pose_count, const hsr_ff_antenna *tx,
+                                 const hsr_ff_antenna *rx, const int64_t *budget, const int64_t *index_offset,
+                                 int32_t phase_mode, float *out_rows);
 
 /* As hsr_simulate_batch_device, with HOST inputs and outputs: copies poses and budgets
  * in, runs, copies the rows out and synchronises. */

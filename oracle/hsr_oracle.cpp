@@ -340,6 +340,50 @@ template <typename R> static inline CV3<R> antenna_nee(const Antenna<R> &a, Isec
     return mulcv(a.rot, H);
 }
 
+// FFAntenna (emitter.h:226-291): a far-field antenna, a disk of `radius` at
+// sceneCenter + dir * radius facing the scene; the frame is buildFrame(-dir)
+// (geometry.h:45-53) and the sample pdf 1 / (4 radius^2) (double, then rounded).
+template <typename R> struct FfAntenna {
+    V3<R> dir, center, e0, e1;
+    CV3<R> pol;
+    R radius, pdf;
+};
+template <typename R> static FfAntenna<R> to_ff(const hsr_ff_antenna_o &a) {
+    FfAntenna<R> f;
+    f.dir = {R(a.direction[0]), R(a.direction[1]), R(a.direction[2])};
+    for (int i = 0; i < 3; ++i) f.pol.c[i] = {R(a.polarization[2 * i]), R(a.polarization[2 * i + 1])};
+    f.radius = R(a.radius);
+    V3<R> c = {R(a.scene_center[0]), R(a.scene_center[1]), R(a.scene_center[2])};
+    f.center = add(c, scale(f.radius, f.dir));  // emitter.h:238
+    V3<R> d = neg(f.dir);
+    if (std::abs(d.x) > std::abs(d.y))
+        f.e0 = divs(v3(-d.z, R(0), d.x), R(std::sqrt(d.x * d.x + d.z * d.z)));
+    else
+        f.e0 = divs(v3(R(0), d.z, -d.y), R(std::sqrt(d.y * d.y + d.z * d.z)));
+    f.e1 = cross(d, f.e0);
+    f.pdf = R(1.0 / (4.0 * std::pow(double(a.radius), 2)));  // emitter.h:246
+    return f;
+}
+// FFAntenna::sample (emitter.h:241-248)
+template <typename R> static inline void ff_sample(const FfAntenna<R> &a, R u0, R u1, Ray<R> &ray) {
+    R s0 = R(2) * u0 - R(1), s1 = R(2) * u1 - R(1);
+    V3<R> q = {a.e0.x * s0 + a.e1.x * s1, a.e0.y * s0 + a.e1.y * s1, a.e0.z * s0 + a.e1.z * s1};
+    ray.o = add(scale(a.radius, q), a.center);
+    ray.d = neg(a.dir);
+    ray.H = cv3_divs(a.pol, a.pdf);
+}
+// FFAntenna::nee (emitter.h:261-273); false where it returns Vector3c::Zero() (the point
+// projects more than 1 from the disk centre), which contributes nothing
+template <typename R> static inline bool ff_nee(const FfAntenna<R> &a, Isect<R> &nee, CV3<R> &H) {
+    V3<R> local = sub(nee.ray.o, a.center);
+    local = sub(local, scale(dot(local, a.dir), a.dir));
+    if (norm(local) > R(1)) return false;
+    nee.ray.d = a.dir;
+    nee.tMax = norm(sub(add(local, a.center), nee.ray.o));
+    H = cv3_scale(a.pol, R(4) * Consts<R>::Pi * nee.tMax);
+    return true;
+}
+
 // SurfaceEmitter (emitter.h:53-82)
 template <typename R> static inline void surface_evaluate(const Isect<R> &incoming, Ray<R> &ray) {
     CV3<R> J = cross_rc(incoming.n, incoming.ray.H);
@@ -781,6 +825,8 @@ template <typename R> struct Tracer {
     const Scene *scene;
     Rf<R> rf;
     Antenna<R> tx, rx;
+    bool farField = false;  // TX and RX are the far-field antennas below
+    FfAntenna<R> ftx, frx;
     Flags fl;
     Frame<R> frame;
     R currentSampleWeight = 1;
@@ -856,7 +902,10 @@ template <typename R> struct Tracer {
             if (ray.depth == 0) {
                 R u0 = sampler.get1D();
                 R u1 = sampler.get1D();
-                antenna_sample(tx, u0, u1, ray);
+                if (farField)
+                    ff_sample(ftx, u0, u1, ray);
+                else
+                    antenna_sample(tx, u0, u1, ray);
                 ray.H = cv3_scale(ray.H, R(1) / primaryPdf);
             } else {
                 if (!fl.useGO) {
@@ -873,7 +922,14 @@ template <typename R> struct Tracer {
                 if (ray.depth == 0 && fl.onlyIndirect) break;
                 Isect<R> nee = isect;
                 nee.t = std::numeric_limits<R>::infinity();
-                CV3<R> Hrx = antenna_nee(rx, nee);
+                CV3<R> Hrx;
+                if (farField) {
+                    // the direct term: FFAntenna::evaluate zeroes the ray (emitter.h:253-255)
+                    if (ray.depth == 0) break;
+                    if (!ff_nee(frx, nee, Hrx)) break;
+                } else {
+                    Hrx = antenna_nee(rx, nee);
+                }
                 if (!fl.poDiffraction && !rt_visible(*scene, nee)) break;
                 nee.t = nee.tMax;
                 if (ray.depth == 0) {
@@ -950,7 +1006,7 @@ template <typename R> struct Tracer {
             r += isect.t;
             if (!fl.useGO) {
                 if (ray.depth == 0) {
-                    antenna_connect(isect);
+                    if (!farField) antenna_connect(isect);  // FFAntenna::connect does nothing
                 } else {
                     surface_connect(incoming, isect);
                 }
@@ -1030,9 +1086,15 @@ template <typename R>
 static int simulate(const Scene *s, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
                     int64_t budget, int64_t offset, float sampleWeight, int threads, double *frame_out,
-                    double *weight_out, bool floatSamples = false, bool exact = false) {
+                    double *weight_out, bool floatSamples = false, bool exact = false,
+                    const hsr_ff_antenna_o *ftx = nullptr, const hsr_ff_antenna_o *frx = nullptr) {
     Tracer<R> tr;
     setup_tracer(tr, s, rf, tx, rx, fl);
+    if (ftx) {
+        tr.farField = true;
+        tr.ftx = to_ff<R>(*ftx);
+        tr.frx = to_ff<R>(*frx);
+    }
     tr.floatSamples = floatSamples;
     tr.frame.exact = exact;
     tr.currentSampleWeight = R(sampleWeight);
@@ -1130,6 +1192,21 @@ int oracle_simulate(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_
         return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out,
                                false, true);
     return simulate<float>(s, rf, fc, tx, rx, fl, budget, offset, sample_weight, threads, frame_out, weight_out);
+}
+
+int oracle_simulate_ff(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc, const hsr_ff_antenna_o *tx,
+                       const hsr_ff_antenna_o *rx, const hsr_tracer_flags_o *fl, int64_t budget, int64_t offset,
+                       float sample_weight, int precision, int threads, double *frame_out, double *weight_out) {
+    if (!sp || !rf || !fc || !tx || !rx || !fl || !frame_out || !weight_out || budget < 0) return 1;
+    if (fc->chirpCount <= 0 || fc->samplesPerChirp <= 0 || fc->channelCount <= 0) return 1;
+    if (fl->doGuiding) return 2;
+    const Scene *s = static_cast<Scene *>(sp);
+    hsr_antenna_o unused{};  // the near-field antennas are not read in far-field runs
+    if (precision == 64 || precision == 65)
+        return simulate<double>(s, rf, fc, &unused, &unused, fl, budget, offset, sample_weight, threads, frame_out,
+                                weight_out, precision == 65, false, tx, rx);
+    return simulate<float>(s, rf, fc, &unused, &unused, fl, budget, offset, sample_weight, threads, frame_out,
+                           weight_out, false, false, tx, rx);
 }
 
 int oracle_records(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc, const hsr_antenna_o *tx,

@@ -25,6 +25,13 @@ typedef struct hsr_antenna_o {
     float rotation[9];
 } hsr_antenna_o;
 
+typedef struct hsr_ff_antenna_o {
+    float direction[3];
+    float polarization[6];
+    float scene_center[3];
+    float radius;
+} hsr_ff_antenna_o;
+
 typedef struct hsr_tracer_flags_o {
     int32_t onlyIndirect, maxDepth, useGeometricalOptics, poDiffraction, doGuiding, clearBeforeIteration,
         correctPhase, filterGuiding, doFiltering, filteringSphere, produceDebugImage;
@@ -61,6 +68,11 @@ int oracle_simulate(void *scene, const hsr_rf_config_o *rf, const hsr_frame_conf
                     const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
                     int64_t budget, int64_t offset, float sample_weight, int precision, int threads,
                     double *frame_out, double *weight_out);
+/* Far-field TX and RX (FFAntenna, emitter.h:226-291); precision 32, 64 or 65 as above. */
+int oracle_simulate_ff(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
+                       const hsr_ff_antenna_o *tx, const hsr_ff_antenna_o *rx, const hsr_tracer_flags_o *fl,
+                       int64_t budget, int64_t offset, float sample_weight, int precision, int threads,
+                       double *frame_out, double *weight_out);
 int oracle_records(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
                    const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
                    int64_t first, int64_t count, int64_t offset, int max_records, oracle_record *out);

@@ -26,6 +26,11 @@ class ANT(ctypes.Structure):
     _fields_ = [("position", ctypes.c_float * 3), ("rotation", ctypes.c_float * 9)]
 
 
+class FFANT(ctypes.Structure):
+    _fields_ = [("direction", ctypes.c_float * 3), ("polarization", ctypes.c_float * 6),
+                ("scene_center", ctypes.c_float * 3), ("radius", ctypes.c_float)]
+
+
 class FLAGS(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in
                 ("onlyIndirect", "maxDepth", "useGeometricalOptics", "poDiffraction", "doGuiding",
@@ -66,6 +71,9 @@ def lib():
         L.oracle_visible.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp]
         L.oracle_simulate.argtypes = [vp, P(RF), P(FC), P(ANT), P(ANT), P(FLAGS), ctypes.c_int64, ctypes.c_int64,
                                       ctypes.c_float, ctypes.c_int, ctypes.c_int, vp, P(ctypes.c_double)]
+        L.oracle_simulate_ff.argtypes = [vp, P(RF), P(FC), P(FFANT), P(FFANT), P(FLAGS), ctypes.c_int64,
+                                         ctypes.c_int64, ctypes.c_float, ctypes.c_int, ctypes.c_int, vp,
+                                         P(ctypes.c_double)]
         L.oracle_records.argtypes = [vp, P(RF), P(FC), P(ANT), P(ANT), P(FLAGS), ctypes.c_int64, ctypes.c_int64,
                                      ctypes.c_int64, ctypes.c_int, vp]
         fp = P(ctypes.c_float)
@@ -93,6 +101,17 @@ def ant_c(a):
     c = ANT()
     c.position[:] = [float(x) for x in a.position()]
     c.rotation[:] = [float(x) for x in np.asarray(a.rotation()).reshape(-1)]
+    return c
+
+
+def ffant_c(a):
+    """A far-field antenna (direction, complex polarization, scene centre, radius)."""
+    c = FFANT()
+    c.direction[:] = [float(x) for x in np.asarray(a.direction, np.float32)]
+    pol = np.asarray(a.polarization, np.complex64)
+    c.polarization[:] = [float(x) for x in np.stack([pol.real, pol.imag], 1).reshape(-1)]
+    c.scene_center[:] = [float(x) for x in np.asarray(a.scene_center, np.float32)]
+    c.radius = float(np.float32(a.radius))
     return c
 
 
@@ -158,6 +177,20 @@ class Scene:
         fr, w = self.simulate(rf, FrameConfig(1, samples, 1), tx, rx, tracer, budget, offset=offset,
                               precision=precision | (0x100 if exact else 0), threads=threads)
         return fr[0, :, 0] / w
+
+    def fetch_row_ff(self, rf, samples, tx, rx, tracer, budget, precision=32, threads=0, offset=0):
+        """fetchFrame() row of a plain run with far-field TX and RX (FFAntenna)."""
+        from hussar_gb300.radar import FrameConfig
+        fc = FrameConfig(1, samples, 1)
+        out = np.zeros(2 * samples, np.float64)
+        w = ctypes.c_double(0.0)
+        rc = lib().oracle_simulate_ff(self.h, ctypes.byref(rf_c(rf)), ctypes.byref(fc_c(fc)),
+                                      ctypes.byref(ffant_c(tx)), ctypes.byref(ffant_c(rx)),
+                                      ctypes.byref(flags_c(tracer)), int(budget), int(offset), 1.0, int(precision),
+                                      int(threads), _p(out), ctypes.byref(w))
+        if rc != 0:
+            raise RuntimeError("oracle_simulate_ff failed (%d)" % rc)
+        return out.view(np.complex128) / w.value
 
     def records(self, rf, fc, tx, rx, tracer, first, count, offset=0, max_records=None):
         mr = max_records or (tracer.maxDepth + 1)

@@ -68,6 +68,7 @@ int main(void) {
     F(hsr_server_stats, admitted_while_busy); F(hsr_server_stats, scene_bytes);
     S(hsr_tracer_flags); S(hsr_antenna); S(hsr_rf_config);
     S(hsr_launch_config); F(hsr_launch_config, queue_threshold); F(hsr_launch_config, default_trace_ms);
+    S(hsr_ff_antenna); F(hsr_ff_antenna, polarization); F(hsr_ff_antenna, scene_center); F(hsr_ff_antenna, radius);
     return 0;
 }
 """
@@ -85,7 +86,7 @@ def test_ctypes_mirrors_match_c_layout(tmp_path):
     mirrors = {"hsr_server_config": _lib.ServerConfigC, "hsr_request": _lib.RequestC,
                "hsr_request_result": _lib.RequestResultC, "hsr_server_stats": _lib.ServerStatsC,
                "hsr_tracer_flags": _lib.FlagsC, "hsr_antenna": _lib.AntennaC, "hsr_rf_config": _lib.RFConfigC,
-               "hsr_launch_config": _lib.LaunchConfigC}
+               "hsr_launch_config": _lib.LaunchConfigC, "hsr_ff_antenna": _lib.FfAntennaC}
     for key, val in c.items():
         if "." in key:
             t, m = key.split(".")
