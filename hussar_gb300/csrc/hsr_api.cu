@@ -977,7 +977,7 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     const float default_ms = best_ms;
     const int32_t tiles[] = {1024, 2048, 4096, 8192, 16384};
     const int32_t ctas[] = {2, 3, 4};
-    const int32_t thresholds[] = {32, 64, kWaveMaxQueueThreshold};
+    const int32_t thresholds[] = {32, 64, kWaveDefaultQueue, kWaveMaxQueueThreshold};
     for (int32_t t : tiles) {
         LaunchConfig c = best;
         c.tile = t;
@@ -990,7 +990,7 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         if ((st = trial(c, ms)) != HSR_OK) break;
         if (ms < best_ms) best_ms = ms, best = c;
     }
-    for (int32_t k = 0; st == HSR_OK && k < 3; ++k) {
+    for (int32_t k = 0; st == HSR_OK && k < 4; ++k) {
         LaunchConfig c = best;
         c.queue_threshold = thresholds[k];
         if ((st = trial(c, ms)) != HSR_OK) break;
@@ -1002,11 +1002,11 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     }
     // store the shape explicitly: a threshold of 0 means "the default" to the kernel, but
     // the serving ticks read the scene's tuned threshold to pick their path stack
-    if (best.queue_threshold <= 0) best.queue_threshold = kWaveMaxQueueThreshold;
+    if (best.queue_threshold <= 0) best.queue_threshold = kWaveDefaultQueue;
     d.tuned = best;
     out_best->tile = best.tile > 0 ? best.tile : kTile;
     out_best->ctas_per_sm = best.ctas_per_sm;
-    out_best->queue_threshold = best.queue_threshold > 0 ? best.queue_threshold : kWaveMaxQueueThreshold;
+    out_best->queue_threshold = best.queue_threshold > 0 ? best.queue_threshold : kWaveDefaultQueue;
     out_best->trace_ms = best_ms;
     out_best->default_trace_ms = default_ms;
     return HSR_OK;

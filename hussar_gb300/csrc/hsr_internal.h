@@ -32,7 +32,9 @@ struct LaunchConfig {
     int32_t ctas_per_sm = 0;      // persistent grid: SMs x this (<= the occupancy limit)
     int32_t queue_threshold = 0;  // see TraceParams::queue_threshold
 };
-constexpr int kWaveMaxQueueThreshold = 128;  // the wavefront CTA's 384-entry stack minus 256
+// wavefront path stacks: 256 + the GENERATE threshold entries; three capacities
+constexpr int kWaveMaxQueueThreshold = 256;  // thresholds above 128: the 512-entry stack
+constexpr int kWaveDefaultQueue = 128;       // threshold 0 (the default) and up to 128: 384 entries
 constexpr int kWaveSmallQueue = 64;          // thresholds up to this run with a 320-entry stack
 
 // A resident scene: triangles + BVH on the device, plus per-scene scratch reused by

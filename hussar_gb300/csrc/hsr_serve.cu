@@ -356,7 +356,9 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     t.finishing.clear();
     t.samples = 0;
     int P = 0, F = 0, maxN = 1;
-    int32_t queue_threshold = kWaveMaxQueueThreshold;  // lowered by any scene not tuned above 64
+    // the tick's GENERATE threshold: the smallest of its scenes' tuned thresholds, where a
+    // scene never tuned (or tuned to 64 or less) counts as 64
+    int32_t queue_threshold = kWaveMaxQueueThreshold;
     // a tick whose requests share one scene, chirp and N runs the uniform kernel
     bool uniform = true;
     const ReqPtr *first = nullptr;
@@ -385,6 +387,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             }
             tile[P + 1] = tile[P] + (chunk[i] + tick_tile - 1) / tick_tile;
             maxN = std::max(maxN, q->r.samples_per_chirp);
+            queue_threshold = std::min(queue_threshold, std::max(q->scene->tuned.queue_threshold, kWaveSmallQueue));
             if (q->scene->tuned.queue_threshold <= kWaveSmallQueue) queue_threshold = kWaveSmallQueue;
             ++P;
             q->scheduled += chunk[i];
@@ -427,8 +430,8 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
         p.status = reinterpret_cast<unsigned *>(t.d_in + layout.counters);
         p.work_counter = p.status + 2;
         p.jobs = reinterpret_cast<const PoseJob *>(t.d_in + layout.jobs);
-        // the path stack and GENERATE threshold of the tick: the large stack only when
-        // every scene in it was autotuned to a threshold above 64 (hsr_autotune_batch);
+        // the path stack and GENERATE threshold of the tick: a larger stack only when every
+        // scene in it was autotuned to a threshold above 64 (hsr_autotune_batch);
         // otherwise, and for scenes never tuned, the small stack (the faster one on dense
         // scenes, where it leaves more of the L1 to the BVH)
         p.queue_threshold = queue_threshold;

@@ -4,7 +4,7 @@
 
 namespace hsr {
 
-size_t wave_smem_bytes(int samples, bool guided) { return wave_smem_for<kWaveMaxQueueThreshold>(samples, guided); }
+size_t wave_smem_bytes(int samples, bool guided) { return wave_smem_for<kWaveDefaultQueue>(samples, guided); }
 
 int wave_blocks_per_sm(int samples, bool mixed) {
     int nb = 0;
@@ -15,7 +15,7 @@ int wave_blocks_per_sm(int samples, bool mixed) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);
     } else {
         const size_t smem = wave_smem_bytes(samples, false);
-        auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, false, kWaveMaxQueueThreshold>;
+        auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, false, kWaveDefaultQueue>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);
     }

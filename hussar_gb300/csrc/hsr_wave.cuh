@@ -36,10 +36,11 @@ namespace {
 constexpr int kThreads = 256;
 
 // A CTA's live path states: a stack of kThreads + kQueue entries, where kQueue bounds the
-// paths left when GENERATE runs (the queue threshold). Two capacities are built: 384
-// entries (threshold up to 128) and 320 (up to 64), whose 5 KB less shared memory per
-// CTA leaves more of the SM's L1 to the BVH (4 % on the dense boxes scenes, which the
-// autotuner runs at threshold 32 or 64; the serving ticks always use it).
+// paths left when GENERATE runs (the queue threshold). Three capacities are built: 384
+// entries (the default, thresholds up to 128), 320 (up to 64), whose 5 KB less shared
+// memory per CTA leaves more of the SM's L1 to the BVH (4 % on the dense boxes scenes,
+// which the autotuner runs at threshold 32 or 64), and 512 (up to 256), whose fuller
+// EXTEND stages pay where the BVH stays in L1 anyway (7 % on the sphere bench).
 template <int kCap> struct WaveShared {
     float ox[kCap], oy[kCap], oz[kCap];  // hit point (origin of the next segment)
     float dx[kCap], dy[kCap], dz[kCap];  // incoming direction
@@ -386,10 +387,11 @@ template <int kQueue> size_t wave_smem_for(int samples, bool guided) {
            (guided ? (kGuideMaxNodes + kGuideStackFields * kCap) * sizeof(float) : 0);
 }
 
-// The stack capacity a uniform launch runs with: 320 entries when its queue threshold
-// is set at 64 or less.
-inline bool wave_small_stack(const TraceParams &p) {
-    return p.queue_threshold > 0 && p.queue_threshold <= kWaveSmallQueue;
+// The stack capacity (as its GENERATE threshold) a launch with threshold q runs: 64 for
+// 1..64, 256 above 128, else (0 = the default, or 65..128) 128.
+inline int wave_capacity(int32_t q) {
+    return (q > 0 && q <= kWaveSmallQueue) ? kWaveSmallQueue : (q > kWaveDefaultQueue ? kWaveMaxQueueThreshold
+                                                                                      : kWaveDefaultQueue);
 }
 
 // The launch of one instantiation.
@@ -405,15 +407,19 @@ void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
 // tick asks for a threshold above 64 (its default: on the serving mix of dense boxes
 // and urban scenes it gives 1.18x the capacity of the 384-entry stack).
 template <int kPhase> void wave_dispatch(const TraceParams &p, int grid, cudaStream_t st) {
-    if (p.jobs) {
+    const int cap = wave_capacity(p.queue_threshold);
+    if (p.jobs) {  // the mixed form is built at the two smaller capacities
         if (p.queue_threshold > kWaveSmallQueue)
-            wave_instance<kPhase, true, kWaveMaxQueueThreshold>(p, grid, st);
+            wave_instance<kPhase, true, kWaveDefaultQueue>(p, grid, st);
         else
             wave_instance<kPhase, true, kWaveSmallQueue>(p, grid, st);
-    } else if (wave_small_stack(p))
+    } else if (cap == kWaveSmallQueue) {
         wave_instance<kPhase, false, kWaveSmallQueue>(p, grid, st);
-    else
+    } else if (cap == kWaveMaxQueueThreshold) {
         wave_instance<kPhase, false, kWaveMaxQueueThreshold>(p, grid, st);
+    } else {
+        wave_instance<kPhase, false, kWaveDefaultQueue>(p, grid, st);
+    }
 }
 
 }  // namespace

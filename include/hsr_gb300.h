@@ -310,8 +310,10 @@ hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, f
 /* ---- Autotuning of the plain wavefront launch ---------------------------------------
  * No counterpart in the reference. The launch shape of a plain batch: samples per work
  * item (tile), persistent CTAs per SM, and the queue threshold (GENERATE runs while a CTA
- * holds at most this many live paths; at most 128). Zero fields mean the default shape.
- * The shape changes the grouping of sums, not the samples traced. */
+ * holds at most this many live paths; at most 256: thresholds up to 64 run a 320-entry
+ * path stack, up to 128 a 384-entry one, above 128 a 512-entry one). Zero fields mean
+ * the default shape (threshold 128). The shape changes the grouping of sums, not the
+ * samples traced. */
 typedef struct hsr_launch_config {
     int32_t tile;
     int32_t ctas_per_sm;

@@ -27,7 +27,7 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(product_lib):
     best = be.autotune(w.rf, N, t, w.tx, w.rx, w.budget)
     print("autotuned", best)
     assert best["tile"] in (1024, 2048, 4096, 8192, 16384)
-    assert best["ctas_per_sm"] in (0, 2, 3, 4) and 1 <= best["queue_threshold"] <= 128
+    assert best["ctas_per_sm"] in (0, 2, 3, 4) and 1 <= best["queue_threshold"] <= 256
     assert 0 < best["trace_ms"] <= best["default_trace_ms"]
     tuned = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
     assert rel_l2(tuned, ref) <= 1e-5
