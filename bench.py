@@ -47,7 +47,7 @@ METRIC = "paths/s"
 # DRAM bytes of one k_wave launch of the sphere bench (dram__bytes_read.sum +
 # dram__bytes_write.sum from an ncu --set full capture of the first timed step of
 # `bench.py --kernel-only`)
-NCU_TRAFFIC = {"sphere": 4.123904e6 + 43.52e3}
+NCU_TRAFFIC = {"sphere": 4.415232e6 + 30.72e3}
 WORKLOAD = "icosphere-L6 (81,920 tris) + 20x20 m ground, sensor 10 m / 0.5 m, 3 bounces, 2^22 samples, N=512"
 
 
