@@ -1,5 +1,6 @@
 """The launch-shape autotuner (hsr_autotune_batch): it times the caller's batch under
-candidate shapes (work-item tile, CTAs per SM, queue threshold) and keeps the fastest.
+candidate shapes (work-item tile, CTAs per SM, queue threshold: 32, 64, 128, 256) and
+keeps the fastest.
 A shape changes only the grouping of sums, so rows agree with the default shape up to
 summation order (1e-5 relative L2)."""
 import numpy as np
@@ -31,8 +32,16 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(product_lib):
     assert 0 < best["trace_ms"] <= best["default_trace_ms"]
     tuned = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
     assert rel_l2(tuned, ref) <= 1e-5
-    # an explicit odd shape gives the same rows too, and the default can be restored
-    be.set_launch_config(tile=1024, ctas_per_sm=2, queue_threshold=32)
-    assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5
+    # explicit shapes at each path-stack capacity (320, 384 and 512 entries) give the same
+    # rows too, in both phase modes, and the default can be restored
+    for tile, ctas, q in ((1024, 2, 32), (2048, 3, 100), (1024, 4, 256), (4096, 4, 200)):
+        be.set_launch_config(tile=tile, ctas_per_sm=ctas, queue_threshold=q)
+        assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5, (tile, ctas, q)
+    from hussar_gb300 import HSR_PHASE_SPLIT_FP64
+    be.set_launch_config(default=True)
+    ref_split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
+    be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=256)
+    split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
+    assert rel_l2(split, ref_split) <= 1e-5
     be.set_launch_config(default=True)
     assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5
