@@ -264,8 +264,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     } else {
         p.flags.doGuiding = 0;
     }
-    // far-field runs take the one-thread-per-sample kernel
-    const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters && !s.far_field;
+    const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
     int per_sm = wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0);
     if (wave && tuned) {
         if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);

@@ -56,6 +56,7 @@ template <int kCap> struct WaveShared {
     long long gen, gen_end, pending_first, pending_last;
     long long since_flush;      // samples generated since the row was last flushed
     PoseJob job;                // mixed batches: the current pose's scene, chirp and row
+    FfAnt ff[2];                // far-field launches: the current pose's TX and RX
     float max_dist, bandwidth;  // mixed batches: derived from job.rf
 };
 
@@ -146,7 +147,7 @@ __device__ __forceinline__ double *pose_row(const TraceParams &p, const Shared &
 
 // Four CTAs per SM (64 registers): the spills cost less than the latency the extra
 // warps hide (measured: 1.2x on the sphere bench, 1.13x on the serving mix over two).
-template <int kPhase, bool kMixed, int kQueue>
+template <int kPhase, bool kMixed, int kQueue, bool kFF = false>
 __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
     constexpr int kCap = kThreads + kQueue;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -239,15 +240,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 const float freq = rf.startFreq + halton(hindex, 0) * HSR_BANDWIDTH;
                 Guided g{halton(hindex, 1), halton(hindex, 2), 1.f, cf{0.f, 0.f}};
                 if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
-                f3 o = pc.tx.pos, d;
+                f3 o, d;
                 c3 H;
-                antenna_sample(pc.tx, g.x0, g.x1, d, H);
+                if (kFF) {
+                    ff_sample(S.ff[0], g.x0, g.x1, o, d, H);
+                } else {
+                    o = pc.tx.pos;
+                    antenna_sample(pc.tx, g.x0, g.x1, d, H);
+                }
                 H = c3_scl(H, 1.f / g.pdf);
                 if (!fl.onlyIndirect) {
                     NeeOut ne;
-                    if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, 0, o, d,
-                                                mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H, 0.f, 0.0, 0.f, 1.f,
-                                                freq, pc.weight, ne, nullptr, nullptr) &&
+                    if (nee_eval<kPhase, false, kFF>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, 0, o, d,
+                                                     mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), H, H, 0.f, 0.0, 0.f,
+                                                     1.f, freq, pc.weight, ne, nullptr, nullptr, &S.ff[1]) &&
                         ne.splat) {
                         if (pc.fine_row) {
                             splat_fine(pc.fine_row, p.fine_bins, ne.sample, ne.value);
@@ -313,8 +319,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 c3 H = Hin;
                 reflect(nrm, d, H);
                 NeeOut ne;
-                if (nee_eval<kPhase, false>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, depth, o, d, din, nrm,
-                                            Hin, H, time, plen, r, cosT, freq, pc.weight, ne, nullptr, nullptr)) {
+                if (nee_eval<kPhase, false, kFF>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, depth, o, d, din,
+                                                 nrm, Hin, H, time, plen, r, cosT, freq, pc.weight, ne, nullptr,
+                                                 nullptr, &S.ff[1])) {
                     g.gw = cadd(g.gw, ne.gw_add);
                     if (ne.splat) {
                         if (pc.fine_row) {
@@ -356,6 +363,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     S.max_dist = max_distance(S.job.rf);
                     S.bandwidth = chirp_bandwidth(S.job.rf);
                 }
+                if (kFF) {
+                    S.ff[0] = load_ff(p.ff_tx + pending);
+                    S.ff[1] = load_ff(p.ff_rx + pending);
+                }
                 S.pose = pending;
                 S.since_flush = 0;
                 S.gen = S.pending_first;
@@ -395,11 +406,12 @@ inline int wave_capacity(int32_t q) {
 }
 
 // The launch of one instantiation.
-template <int kPhase, bool kMixed, int kQueue>
+template <int kPhase, bool kMixed, int kQueue, bool kFF = false>
 void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
     const size_t smem = wave_smem_for<kQueue>(p.samples, p.do_guide != 0);
-    cudaFuncSetAttribute(k_wave<kPhase, kMixed, kQueue>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k_wave<kPhase, kMixed, kQueue><<<grid, kThreads, smem, st>>>(p);
+    cudaFuncSetAttribute(k_wave<kPhase, kMixed, kQueue, kFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(smem));
+    k_wave<kPhase, kMixed, kQueue, kFF><<<grid, kThreads, smem, st>>>(p);
 }
 
 // Every instantiation of one phase mode: the mixed form (serving ticks) and the uniform
@@ -408,7 +420,9 @@ void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
 // and urban scenes it gives 1.18x the capacity of the 384-entry stack).
 template <int kPhase> void wave_dispatch(const TraceParams &p, int grid, cudaStream_t st) {
     const int cap = wave_capacity(p.queue_threshold);
-    if (p.jobs) {  // the mixed form is built at the two smaller capacities
+    if (p.ff_tx) {  // far-field runs: the uniform form at the default capacity
+        wave_instance<kPhase, false, kWaveDefaultQueue, true>(p, grid, st);
+    } else if (p.jobs) {  // the mixed form is built at the two smaller capacities
         if (p.queue_threshold > kWaveSmallQueue)
             wave_instance<kPhase, true, kWaveDefaultQueue>(p, grid, st);
         else
