@@ -254,9 +254,9 @@ hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const hsr_rf_conf
  * PathTracer::sample (path.h:235-451) is restated here with FFAntenna's sample, nee,
  * evaluate and connect (emitter.h:241-283): the direct TX -> RX term is zero (evaluate
  * zeroes the ray), and in the non-GO mode the primary segment adds no time of flight and
- * no 1 / (4 pi r) (connect does nothing). Runs on the one-thread-per-sample kernel;
- * doGuiding must be 0 (HSR_ERR_NOT_SUPPORTED otherwise). HOST inputs and outputs,
- * synchronous. */
+ * no 1 / (4 pi r) (connect does nothing). The GO mode runs on the wavefront kernel, the
+ * non-GO mode on the one-thread-per-sample one; doGuiding must be 0
+ * (HSR_ERR_NOT_SUPPORTED otherwise). HOST inputs and outputs, synchronous. */
 hsr_status hsr_simulate_batch_ff(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
                                  const hsr_tracer_flags *flags, int32_t pose_count, const hsr_ff_antenna *tx,
                                  const hsr_ff_antenna *rx, const int64_t *budget, const int64_t *index_offset,
