@@ -170,11 +170,11 @@ def test_close_with_work_queued_returns(resident):
     assert time.time() - t0 < 20
 
 
-@pytest.mark.parametrize("threshold", [0, 128], ids=["untuned-small-stack", "tuned-large-stack"])
+@pytest.mark.parametrize("threshold", [0, 128, 256], ids=["untuned-small-stack", "tuned-384", "tuned-512"])
 def test_uniform_ticks_equal_batch_rows(resident, threshold):
     """Requests that share one scene, chirp and N run as uniform ticks (the batch kernel
     writing each request's arena row), on the small path stack for a scene never tuned
-    and the large one for a scene tuned to threshold 128; large budgets span several
+    and the larger ones for a scene tuned to threshold 128 or 256; large budgets span several
     ticks with work items above 1024 samples. Rows equal the batch call's."""
     w, be = resident[1]
     if threshold:
