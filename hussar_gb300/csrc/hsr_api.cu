@@ -269,6 +269,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
     if (wave && tuned) {
         if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);
         p.queue_threshold = sc.tuned.queue_threshold;
+        p.field_on_hit = sc.tuned.field_on_hit;
     }
     int grid = sc.sm_count * per_sm;
     // timing events only outside stream capture (a captured graph must not record the
@@ -995,6 +996,11 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         if ((st = trial(c, ms)) != HSR_OK) break;
         if (ms < best_ms) best_ms = ms, best = c;
     }
+    if (st == HSR_OK) {  // the primary field formed on a hit (pays where most primaries miss)
+        LaunchConfig c = best;
+        c.field_on_hit = 1;
+        if ((st = trial(c, ms)) == HSR_OK && ms < best_ms) best_ms = ms, best = c;
+    }
     if (st != HSR_OK) {
         d.tuned = saved;
         return st;
@@ -1006,6 +1012,7 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     out_best->tile = best.tile > 0 ? best.tile : kTile;
     out_best->ctas_per_sm = best.ctas_per_sm;
     out_best->queue_threshold = best.queue_threshold > 0 ? best.queue_threshold : kWaveDefaultQueue;
+    out_best->field_on_hit = best.field_on_hit;
     out_best->trace_ms = best_ms;
     out_best->default_trace_ms = default_ms;
     return HSR_OK;
@@ -1016,11 +1023,13 @@ hsr_status hsr_set_launch_config(hsr_scene *s, const hsr_launch_config *c) {
     LaunchConfig l;
     if (c) {
         if (c->tile < 0 || (c->tile > 0 && (c->tile < 32 || c->tile > (1 << 20))) || c->ctas_per_sm < 0 ||
-            c->ctas_per_sm > 32 || c->queue_threshold < 0 || c->queue_threshold > kWaveMaxQueueThreshold)
+            c->ctas_per_sm > 32 || c->queue_threshold < 0 || c->queue_threshold > kWaveMaxQueueThreshold ||
+            (c->field_on_hit != 0 && c->field_on_hit != 1))
             return fail(HSR_ERR_INVALID_ARGUMENT, "launch config out of range");
         l.tile = c->tile;
         l.ctas_per_sm = c->ctas_per_sm;
         l.queue_threshold = c->queue_threshold;
+        l.field_on_hit = c->field_on_hit;
     }
     std::lock_guard<std::mutex> lk(s->mu);
     s->dev.tuned = l;  // null: back to the default shape
@@ -1032,6 +1041,7 @@ hsr_status hsr_get_launch_config(const hsr_scene *s, hsr_launch_config *out) {
     out->tile = s->dev.tuned.tile;
     out->ctas_per_sm = s->dev.tuned.ctas_per_sm;
     out->queue_threshold = s->dev.tuned.queue_threshold;
+    out->field_on_hit = s->dev.tuned.field_on_hit;
     out->trace_ms = 0.f;
     out->default_trace_ms = 0.f;
     return HSR_OK;

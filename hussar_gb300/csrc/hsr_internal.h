@@ -31,6 +31,7 @@ struct LaunchConfig {
     int32_t tile = 0;             // samples per work item
     int32_t ctas_per_sm = 0;      // persistent grid: SMs x this (<= the occupancy limit)
     int32_t queue_threshold = 0;  // see TraceParams::queue_threshold
+    int32_t field_on_hit = 0;     // see TraceParams::field_on_hit
 };
 // wavefront path stacks: 256 + the GENERATE threshold entries; three capacities
 constexpr int kWaveMaxQueueThreshold = 256;  // thresholds above 128: the 512-entry stack
@@ -134,7 +135,10 @@ struct TraceParams {
     // wavefront kernel: GENERATE runs while a CTA holds at most this many live paths
     // (<= kWaveStack - 256; 0: that maximum)
     int32_t queue_threshold;
-    // far-field runs (hsr_simulate_batch_ff), per-thread kernel: each pose's TX and RX;
+    // wavefront kernel, indirect-only paths: form a primary ray's antenna field only once
+    // it has hit something
+    int32_t field_on_hit;
+    // far-field runs (hsr_simulate_batch_ff): each pose's TX and RX;
     // nullptr: the near-field antennas tx/rx above
     const hsr_ff_antenna *ff_tx;
     const hsr_ff_antenna *ff_rx;

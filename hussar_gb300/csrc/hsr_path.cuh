@@ -174,6 +174,12 @@ __device__ __forceinline__ c3 awr_eval(f3 d) {
 }
 
 // NFAntenna::sample (emitter.h:174-180): primary ray from the TX antenna
+// Its field for the local direction ld (the rotated pattern over the sample density):
+// the same operations, so that a caller may form it only once the primary ray hits.
+__device__ __forceinline__ c3 antenna_field(const Ant &tx, f3 ld) {
+    return mulcv(tx.rot, c3_div(awr_eval(ld), kInv4Pi));
+}
+
 __device__ __forceinline__ void antenna_sample(const Ant &tx, float u0, float u1, f3 &d, c3 &H) {
     f3 ld = uniform_sample_sphere(u0, u1);
     c3 lH = c3_div(awr_eval(ld), kInv4Pi);

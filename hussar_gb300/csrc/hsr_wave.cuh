@@ -112,9 +112,11 @@ __device__ __forceinline__ void push_path(WaveShared<kCap> &S, float *gst, f3 o,
 }
 
 // Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
-// Returns true (and the new state) when the path continues with a stored hit.
+// Returns true (and the new state) when the path continues with a stored hit. The
+// reference's zero-field test (path.h:413, 439) is the caller's: in GO mode the field
+// does not change across the hit, so testing it before or after is the same.
 __device__ __forceinline__ bool walk(const TraceParams &p, const DNode *nodes, const DTri *tris, f3 o, f3 d,
-                                     const c3 &H, float &time, float &r, double &plen, f3 &hp, f3 &n, float &cosT) {
+                                     float &time, float &r, double &plen, f3 &hp, f3 &n, float &cosT) {
     float th;
     int primh;
     const int slot = closest_hit<false>(nodes, tris, o, d, kEpsilon, CUDART_INF_F, th, primh, p.status, nullptr);
@@ -127,7 +129,6 @@ __device__ __forceinline__ bool walk(const TraceParams &p, const DNode *nodes, c
     r += th;
     time += th / kSpeedOfLight;
     plen += double(th);
-    if (c3_is_zero(H)) return false;
     return true;
 }
 
@@ -147,7 +148,9 @@ __device__ __forceinline__ double *pose_row(const TraceParams &p, const Shared &
 
 // Four CTAs per SM (64 registers): the spills cost less than the latency the extra
 // warps hide (measured: 1.2x on the sphere bench, 1.13x on the serving mix over two).
-template <int kPhase, bool kMixed, int kQueue, bool kFF = false>
+// kLazy (the field_on_hit launch shape): with indirect-only paths, a primary ray's
+// antenna field is formed only once the ray has hit something.
+template <int kPhase, bool kMixed, int kQueue, bool kFF = false, bool kLazy = false>
 __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
     constexpr int kCap = kThreads + kQueue;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -242,13 +245,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
                 f3 o, d;
                 c3 H;
+                f3 ldir = mk3(0.f, 0.f, 0.f);  // kLazy: the local direction the field is formed from
+                const bool deferred = kLazy && fl.onlyIndirect;
                 if (kFF) {
                     ff_sample(S.ff[0], g.x0, g.x1, o, d, H);
+                    H = c3_scl(H, 1.f / g.pdf);
+                } else if (kLazy) {
+                    o = pc.tx.pos;
+                    ldir = uniform_sample_sphere(g.x0, g.x1);
+                    d = mulv(pc.tx.rot, ldir);
+                    if (!deferred) H = c3_scl(antenna_field(pc.tx, ldir), 1.f / g.pdf);
                 } else {
                     o = pc.tx.pos;
                     antenna_sample(pc.tx, g.x0, g.x1, d, H);
+                    H = c3_scl(H, 1.f / g.pdf);
                 }
-                H = c3_scl(H, 1.f / g.pdf);
                 if (!fl.onlyIndirect) {
                     NeeOut ne;
                     if (nee_eval<kPhase, false, kFF>(p, HSR_NODES, HSR_TRIS, rf, HSR_N, pc.tx, pc.rx, 0, o, d,
@@ -264,13 +275,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     }
                 }
                 bool alive = false;
-                if (!(0 >= fl.maxDepth || 0.f >= HSR_MAXDIST) && !c3_is_zero(H)) {
+                if (!(0 >= fl.maxDepth || 0.f >= HSR_MAXDIST) && (deferred || !c3_is_zero(H))) {
                     float time = 0.f, r = 0.f, cosT;
                     double plen = 0.0;
                     f3 hp, n;
-                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n, cosT)) {
-                        push_path<kPhase, kCap>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
-                        alive = true;
+                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, time, r, plen, hp, n, cosT)) {
+                        // deferred: the field now (the same operations as antenna_sample); a
+                        // zero field ends the path as the reference's test before tracing would
+                        if (deferred) H = c3_scl(antenna_field(pc.tx, ldir), 1.f / g.pdf);
+                        if (!deferred || !c3_is_zero(H)) {
+                            push_path<kPhase, kCap>(S, gst, hp, d, H, n, time, r, cosT, freq, 1, plen, g);
+                            alive = true;
+                        }
                     }
                 }
                 if (!alive) guide_train(pc, pc.train_child, s_g, 1, g.gw, g.pdf, g.x0, g.x1);
@@ -336,7 +352,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 if (!(depth >= fl.maxDepth || r >= HSR_MAXDIST) && !c3_is_zero(H)) {
                     f3 hp, n2;
                     float cosT2;
-                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, H, time, r, plen, hp, n2, cosT2)) {
+                    if (walk(p, HSR_NODES, HSR_TRIS, o, d, time, r, plen, hp, n2, cosT2)) {
                         push_path<kPhase, kCap>(S, gst, hp, d, H, n2, time, r, cosT2, freq, depth + 1, plen, g);
                         alive = true;
                     }
@@ -406,12 +422,20 @@ inline int wave_capacity(int32_t q) {
 }
 
 // The launch of one instantiation.
-template <int kPhase, bool kMixed, int kQueue, bool kFF = false>
+template <int kPhase, bool kMixed, int kQueue, bool kFF = false, bool kLazy = false>
 void wave_instance(const TraceParams &p, int grid, cudaStream_t st) {
     const size_t smem = wave_smem_for<kQueue>(p.samples, p.do_guide != 0);
-    cudaFuncSetAttribute(k_wave<kPhase, kMixed, kQueue, kFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_wave<kPhase, kMixed, kQueue, kFF, kLazy>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          int(smem));
-    k_wave<kPhase, kMixed, kQueue, kFF><<<grid, kThreads, smem, st>>>(p);
+    k_wave<kPhase, kMixed, kQueue, kFF, kLazy><<<grid, kThreads, smem, st>>>(p);
+}
+
+// The uniform form at one capacity, with the primary field formed eagerly or on a hit.
+template <int kPhase, int kQueue> void wave_uniform(const TraceParams &p, int grid, cudaStream_t st) {
+    if (p.field_on_hit)
+        wave_instance<kPhase, false, kQueue, false, true>(p, grid, st);
+    else
+        wave_instance<kPhase, false, kQueue>(p, grid, st);
 }
 
 // Every instantiation of one phase mode: the mixed form (serving ticks) and the uniform
@@ -428,11 +452,11 @@ template <int kPhase> void wave_dispatch(const TraceParams &p, int grid, cudaStr
         else
             wave_instance<kPhase, true, kWaveSmallQueue>(p, grid, st);
     } else if (cap == kWaveSmallQueue) {
-        wave_instance<kPhase, false, kWaveSmallQueue>(p, grid, st);
+        wave_uniform<kPhase, kWaveSmallQueue>(p, grid, st);
     } else if (cap == kWaveMaxQueueThreshold) {
-        wave_instance<kPhase, false, kWaveMaxQueueThreshold>(p, grid, st);
+        wave_uniform<kPhase, kWaveMaxQueueThreshold>(p, grid, st);
     } else {
-        wave_instance<kPhase, false, kWaveDefaultQueue>(p, grid, st);
+        wave_uniform<kPhase, kWaveDefaultQueue>(p, grid, st);
     }
 }
 

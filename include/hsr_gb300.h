@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HSR_ABI_VERSION 2
+#define HSR_ABI_VERSION 3
 
 typedef enum hsr_status {
     HSR_OK = 0,
@@ -312,14 +312,18 @@ hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, f
  * item (tile), persistent CTAs per SM, and the queue threshold (GENERATE runs while a CTA
  * holds at most this many live paths; at most 256: thresholds up to 64 run a 320-entry
  * path stack, up to 128 a 384-entry one, above 128 a 512-entry one). Zero fields mean
- * the default shape (threshold 128). The shape changes the grouping of sums, not the
- * samples traced. */
+ * the default shape (threshold 128). field_on_hit = 1 forms a primary ray's antenna field
+ * only once the ray has hit something (for indirect-only paths: the field of a ray that
+ * misses is never used), which pays where most primary rays miss and costs registers
+ * elsewhere. The shape changes the grouping of sums and the work done, not the samples
+ * traced nor their values. */
 typedef struct hsr_launch_config {
     int32_t tile;
     int32_t ctas_per_sm;
     int32_t queue_threshold;
     float trace_ms;          /* hsr_autotune_batch: the chosen shape's trace-kernel time */
     float default_trace_ms;  /* and the default shape's, on the same batch */
+    int32_t field_on_hit;
 } hsr_launch_config;
 
 /* Runs the given batch (host arrays, as hsr_simulate_batch; plain GO mode) under

@@ -6,7 +6,7 @@ summation order (1e-5 relative L2)."""
 import numpy as np
 import pytest
 
-from hussar_gb300 import PathTracer, gb300, scenes
+from hussar_gb300 import NFAntenna, PathTracer, gb300, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -34,14 +34,40 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(product_lib):
     assert rel_l2(tuned, ref) <= 1e-5
     # explicit shapes at each path-stack capacity (320, 384 and 512 entries) give the same
     # rows too, in both phase modes, and the default can be restored
-    for tile, ctas, q in ((1024, 2, 32), (2048, 3, 100), (1024, 4, 256), (4096, 4, 200)):
-        be.set_launch_config(tile=tile, ctas_per_sm=ctas, queue_threshold=q)
-        assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5, (tile, ctas, q)
+    for tile, ctas, q, lazy in ((1024, 2, 32, 0), (2048, 3, 100, 0), (1024, 4, 256, 0), (4096, 4, 200, 0),
+                                (1024, 4, 64, 1), (2048, 4, 128, 1), (1024, 4, 256, 1)):
+        be.set_launch_config(tile=tile, ctas_per_sm=ctas, queue_threshold=q, field_on_hit=lazy)
+        assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5, (tile, ctas, q, lazy)
     from hussar_gb300 import HSR_PHASE_SPLIT_FP64
     be.set_launch_config(default=True)
     ref_split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
-    be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=256)
-    split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
-    assert rel_l2(split, ref_split) <= 1e-5
+    for lazy in (0, 1):
+        be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=256, field_on_hit=lazy)
+        split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
+        assert rel_l2(split, ref_split) <= 1e-5, lazy
     be.set_launch_config(default=True)
     assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5
+
+
+def test_field_on_hit_keeps_rows_where_primaries_miss(product_lib):
+    """The dihedral (most primary rays miss the reflector): the primary field formed on a
+    hit gives the same rows as the eager form, with and without the direct TX -> RX term
+    (which needs the field of every primary ray; the RX sits 5 cm above the TX, since the
+    monostatic direct term is the reference's 0/0)."""
+    w = scenes.dihedral_workload(poses=24, samples_per_pose=1 << 16)
+    rx = [NFAntenna(a.position() + np.array([0, 0.05, 0], np.float32), a.rotation()) for a in w.tx]
+    be = gb300.Backend(w.mesh, None)
+    N = w.frame.samplesPerChirp
+    for only_indirect in (True, False):
+        t = PathTracer()
+        t.doGuiding = False
+        t.maxDepth = w.max_depth
+        t.onlyIndirect = only_indirect
+        be.set_launch_config(default=True)
+        ref = be.simulate_batch(w.rf, N, t, w.tx, rx, w.budget)
+        assert np.isfinite(ref).all() and (np.linalg.norm(ref, axis=1) > 0).all()
+        be.set_launch_config(tile=4096, ctas_per_sm=4, queue_threshold=64, field_on_hit=1)
+        got = be.simulate_batch(w.rf, N, t, w.tx, rx, w.budget)
+        for k in range(len(w.tx)):
+            assert rel_l2(got[k], ref[k]) <= 1e-5, (only_indirect, k)
+    be.set_launch_config(default=True)
