@@ -1,32 +1,37 @@
 """Benchmark of the radar path tracer on GB300 (one JSON line on rank 0).
 
-Workload (one step): the tessellated PEC sphere above a ground plane — icosphere level 6
-(81,920 triangles, r = 0.5 m) on a 20 m x 20 m ground quad, sensor at 10 m range and
-0.5 m height, up to 3 bounces, 2^22 Halton samples, one chirp 77-81 GHz with 512 ADC
-samples — traced by one persistent launch of the plain FP32 path with the reference's
-33-bin frame splat. The metric is paths/s.
+Workload (default, --workload boxes): the batched configuration -- one seeded scene of
+~1 M triangles (83,334 random axis-aligned boxes, edges 0.2-5 m, on a 100 m x 100 m
+ground quad) viewed from 4096 sensor poses at 1 m height with random yaw, per-pose
+budgets log-uniform in 2^16..2^22 Halton samples, up to 4 bounces, 256 range bins. One
+step is one batch of 256 of the 4096 poses (step k traces batch k mod 16, so 16 steps
+cover every pose once) run as one persistent launch inside a captured CUDA graph, in the
+product's batched form: split-FP64 phase and the fine range histogram synthesised into
+the 256 IF bins by the split-BF16 tcgen05 GEMM. The metric is paths/s.
 
-  value  device-timed (CUDA events on the launching stream) throughput with poses,
-         budgets and the scene BVH resident in HBM; L2 is flushed between steps by
+  value  device-timed (CUDA events on the launching stream) throughput with the 4096
+         poses, budgets and the scene BVH resident in HBM; L2 is flushed between steps by
          writing a 512 MiB buffer (outside the timed events).
   e2e    the same metric through the public C ABI call with HOST buffers
-         (hsr_simulate_batch: pinned poses/budgets in, the normalised frame row out,
+         (hsr_simulate_batch: pinned poses/budgets in, the normalised rows out,
          synchronised), wall-clock per step.
-  roofline  dominant kernel k_trace: algorithmic bytes = exact BVH node (64 B) and
-         triangle (48 B) fetches of a counting launch over the same samples, divided by
-         the kernel's CUDA-event time; peak = measured HBM copy bandwidth.
+  roofline  dominant kernel k_wave (the traversal): algorithmic bytes = exact BVH node
+         (64 B) and triangle (48 B) fetches of a counting launch over a quarter of the
+         batch's poses (scaled by paths), divided by the kernel's CUDA-event time. The BVH
+         (112 MB) is L2-resident, so the bound is the L2: peak = the L2 read bandwidth
+         measured live (hsr_measure_l2_read); the HBM fraction is reported beside it.
   cpu_baseline  the oracle's FP32 restatement with its own BVH, on all host cores, on a
          bounded sample of the same workload.
 
---workload serve: the serving loop (hsr_server_*): 8 resident scenes of 100 k .. 5 M
-triangles (boxes and urban-canyon generators), a Poisson request stream (--rate req/s
-for --duration s) with random scene, pose, log-uniform budget 2^16..2^24, chirp bandwidth
-1..4 GHz and N in {128, 256, 512}; reports p50/p99 latency (submit -> row on the host)
-and wall-clock paths/s through the public API.
+--workload sphere: the sphere+ground configuration (icosphere level 6 on a 20 m ground
+quad, 2^22 samples, 3 bounces, 512 bins) in the plain FP32 form with the reference's
+33-bin splat. --workload serve: the serving loop (hsr_server_*): 8 resident scenes of
+100 k .. 5 M triangles, a Poisson request stream (--rate req/s for --duration s);
+p50/p99 latency and paths/s through the public API. --workload tte: time to -40 dB only.
 
 --impl reference times the CPU restatement of the reference path (the reference itself
-needs Embree/OptiX/Eigen, absent here) on the host cores with the same metric.
-Multi-GPU: replicas (each rank traces its own disjoint Halton range of the same pose;
+needs Embree/OptiX/Eigen, absent here) on the host cores with the same metric and config.
+Multi-GPU: replicas (each rank traces its own disjoint Halton range of the same poses;
 no collective on the data path), reported as weak scaling.
 """
 import argparse
@@ -179,36 +184,58 @@ def cpu_baseline(w, tracer, samples, threads=0):
     return samples / dt, cores, dt
 
 
+BOXES_BATCH = 256  # poses per step of the batched configuration (4096 = 16 batches)
+REF_POSES, REF_LOG2 = 4, 17  # the CPU arm's bounded sample per step: poses x samples
+
+
 def run_reference(args, rank, world, dist):
-    """--impl reference: the CPU restatement of the reference path on the host cores."""
+    """--impl reference: the CPU restatement of the reference path on the host cores, on the
+    GPU arm's workload. Each step is a bounded sample of one step's batch: the first
+    REF_POSES poses of batch k mod 16 at 2^REF_LOG2 Halton samples each (sphere: 2^20 of
+    the pose's 2^22); the metric is the same paths/s."""
     if rank != 0:
         return
-    from hussar_gb300 import PathTracer, scenes
+    from hussar_gb300 import PathTracer
     from oracle import pyoracle
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
-    w = scenes.sphere_ground_workload(samples=1 << 22)
+    w, desc = load_workload(args.workload)
     t = PathTracer()
     t.doGuiding = False
     t.maxDepth = w.max_depth
     ora = pyoracle.Scene(w.mesh)
-    sample = args.ref_samples
-    for _ in range(args.warmup):
-        ora.simulate(w.rf, w.frame, w.tx[0], w.rx[0], t, sample // 8, precision=32)
-    times = []
+    if args.workload == "boxes":
+        def sample(k):
+            b = (k % (len(w.tx) // BOXES_BATCH)) * BOXES_BATCH
+            return [(w.tx[b + i], w.rx[b + i], 1 << REF_LOG2, 0) for i in range(REF_POSES)]
+        what = "the first %d poses of step k's 256-pose batch, 2^%d Halton samples each" % (REF_POSES, REF_LOG2)
+    else:
+        def sample(k):
+            return [(w.tx[0], w.rx[0], args.ref_samples, k * args.ref_samples)]
+        what = "%d Halton samples of the pose per step (of 2^22)" % args.ref_samples
+
+    def run(k, scale=1):
+        n = 0
+        for tx, rx, b, off in sample(k):
+            ora.simulate(w.rf, w.frame, tx, rx, t, max(1, b // scale), offset=off, precision=32)
+            n += max(1, b // scale)
+        return n
+
+    for k in range(args.warmup):
+        run(k, 8)
+    times, paths = [], 0
     for k in range(args.steps):
         t0 = time.perf_counter()
-        ora.simulate(w.rf, w.frame, w.tx[0], w.rx[0], t, sample, offset=k * sample, precision=32)
+        paths += run(k)
         times.append(time.perf_counter() - t0)
     ms = 1000.0 * sum(times) / len(times)
-    value = sample / (ms / 1000.0)
+    value = paths / sum(times)
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "samples_per_step": sample, "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port",
-                         "sample": "%d Halton samples of the same pose per step (of 2^22)" % sample},
+        "config": {"workload": desc, "samples_per_step": paths // args.steps, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": cores, "kind": "port", "sample": what},
         "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -222,8 +249,8 @@ def load_workload(name, poses=None):
         w = scenes.boxes_workload()
         if poses:
             w.tx, w.rx, w.budget = w.tx[:poses], w.rx[:poses], w.budget[:poses]
-        desc = ("boxes ~1M tris on 100x100 m ground, %d of 4096 poses at 1 m with random yaw, log-uniform "
-                "budgets 2^16..2^22, 4 bounces, N=256" % len(w.tx))
+        desc = ("boxes: %d triangles (83,334 random boxes) on a 100x100 m ground quad, %d poses at 1 m with random "
+                "yaw, log-uniform budgets 2^16..2^22, 4 bounces, N=256" % (w.mesh.triangleCount(), len(w.tx)))
         return w, desc
     return scenes.sphere_ground_workload(samples=1 << 22), WORKLOAD
 
@@ -420,6 +447,212 @@ def run_gb300(args, rank, world, local_rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, rank, world, local_rank, dist):
+    """The batched configuration (module docstring): 4096 poses resident on the device,
+    one step = one 256-pose batch through a captured graph of the batched form."""
+    import ctypes
+
+    import torch
+
+    from hussar_gb300 import HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, PathTracer, _lib, gb300
+
+    torch.cuda.set_device(local_rank)
+    L = _lib.lib()
+    w, desc = load_workload("boxes")
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    be = gb300.Backend(w.mesh, None)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    B = DeviceBatch(w, dev, rank, torch, _lib)  # all 4096 poses resident
+    N, Q = B.N, BOXES_BATCH
+    nb = B.P // Q
+    ant = ctypes.sizeof(_lib.AntennaC)
+    # the graph's input slots (one batch) and its output rows
+    s_tx = torch.empty(Q * ant, dtype=torch.uint8, device=dev)
+    s_rx = torch.empty(Q * ant, dtype=torch.uint8, device=dev)
+    s_budget = torch.empty(Q, dtype=torch.int64, device=dev)
+    s_offset = torch.empty(Q, dtype=torch.int64, device=dev)
+    s_rows = torch.zeros(2 * Q * N, dtype=torch.float32, device=dev)
+    batch_paths = [int(w.budget[k * Q:(k + 1) * Q].sum()) for k in range(nb)]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    vp = ctypes.c_void_p
+    rf_c, fl_c = w.rf.to_c(), t.flags_c()
+    phase, splat = HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH
+
+    # the product's autotuner picks the launch shape on a bounded sample of the batch (16
+    # poses, budgets capped at 2^20); the graph below is captured with it
+    tuned = be.autotune(w.rf, N, t, w.tx[:16], w.rx[:16], np.minimum(w.budget[:16], 1 << 20), phase_mode=phase,
+                        splat_mode=splat)
+    g = be.batch_graph(w.rf, N, t, Q, s_tx.data_ptr(), s_rx.data_ptr(), s_budget.data_ptr(), s_offset.data_ptr(),
+                       s_rows.data_ptr(), phase_mode=phase, splat_mode=splat)
+
+    def load_slot(k):
+        b = (k % nb) * Q
+        s_tx.copy_(B.d_tx[b * ant:(b + Q) * ant], non_blocking=True)
+        s_rx.copy_(B.d_rx[b * ant:(b + Q) * ant], non_blocking=True)
+        s_budget.copy_(B.d_budget[b:b + Q], non_blocking=True)
+        s_offset.copy_(B.d_offset[b:b + Q], non_blocking=True)
+
+    def step(k):
+        load_slot(k)
+        g.launch(stream.cuda_stream)
+
+    for k in range(max(args.warmup, 3)):
+        step(k)
+    g.status()
+
+    clocks = ClockSampler(local_rank)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = L.hsr_launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)  # > L2 (129 MB), outside the timed events
+        ev[k][0].record(stream)
+        step(k)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    launches = L.hsr_launch_count() - launches0
+    barrier(dist)
+    clk = clocks.stop()
+    g.status()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    timed_paths = sum(batch_paths[k % nb] for k in range(args.steps))
+    total_ms = max_over_ranks(dist, sum(step_ms))
+    ms = total_ms / args.steps
+    value = world * timed_paths / (total_ms / 1000.0)
+
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
+                              "steps": args.steps, "ms_per_step": ms, "kernel_only": True, "workload": desc,
+                              "gpu_launches": int(launches), "clocks": clk}), flush=True)
+        g.close()
+        return
+
+    # e2e through the public host-buffer API, the same batches and form: pinned poses in,
+    # normalised rows out, synchronous
+    h_tx = [(_lib.AntennaC * Q)(*[a.to_c() for a in w.tx[k * Q:(k + 1) * Q]]) for k in range(nb)]
+    h_rx = [(_lib.AntennaC * Q)(*[a.to_c() for a in w.rx[k * Q:(k + 1) * Q]]) for k in range(nb)]
+    h_rows = torch.zeros(2 * Q * N, dtype=torch.float32).pin_memory()
+
+    def e2e_step(k):
+        b = (k % nb) * Q
+        _lib.check(L.hsr_simulate_batch(
+            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), Q, ctypes.cast(h_tx[k % nb], vp),
+            ctypes.cast(h_rx[k % nb], vp), vp(B.h_budget[b:].data_ptr()), vp(B.h_offset[b:].data_ptr()), phase, splat,
+            vp(h_rows.data_ptr()), vp(stream.cuda_stream)))
+
+    e2e_step(0)
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step(k)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(dist, sum(e2e_times))
+    h2d = (2 * ant + 16) * Q
+    d2h = 8 * N * Q
+
+    # the traversal kernel alone (events around it inside the library) on batch 0, direct call
+    kms = ctypes.c_float()
+
+    def direct(k, ph, sp_):
+        b = (k % nb) * Q
+        _lib.check(L.hsr_simulate_batch_device(
+            be.handle, ctypes.byref(rf_c), N, ctypes.byref(fl_c), Q, vp(B.d_tx[b * ant:].data_ptr()),
+            vp(B.d_rx[b * ant:].data_ptr()), vp(B.d_budget[b:].data_ptr()), vp(B.d_offset[b:].data_ptr()), ph, sp_,
+            vp(B.d_rows.data_ptr()), vp(stream.cuda_stream)))
+
+    flush.fill_(1)
+    direct(0, phase, splat)
+    _lib.check(L.hsr_scene_status(be.handle, vp(stream.cuda_stream), None))
+    _lib.check(L.hsr_last_kernel_ms(be.handle, ctypes.byref(kms)))
+    trace_ms = kms.value
+
+    # the plain form on the same batches (reference FP32 phase, the reference's 33-bin
+    # splat, direct calls): the parity form, for comparison
+    modes = {}
+    pl_ms = []
+    for k in range(max(2, args.steps // 4)):
+        flush.fill_(k & 0xff)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        direct(k, _lib.HSR_PHASE_REFERENCE_FP32, _lib.HSR_SPLAT_DIRICHLET16)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pl_ms.append((batch_paths[k % nb], e0.elapsed_time(e1)))
+    modes["plain_reference_fp32_splat16"] = {
+        "value": world * sum(p for p, _ in pl_ms) / (max_over_ranks(dist, sum(m for _, m in pl_ms)) / 1000.0),
+        "unit": "paths/s", "steps": len(pl_ms), "note": "direct calls, reference FP32 phase, Frame::splat<16>"}
+    # the synthesis GEMM of one batch: graph step time minus the traversal kernel's time
+    synth_ms = max(ms - trace_ms, 1e-6)
+    useful = 8.0 * Q * (32 * N) * N  # complex [Q x 32N] x [32N x N] in real flops
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    modes["synthesis_in_step"] = {"ms": synth_ms, "useful_tflop": useful / 1e12,
+                                  "note": "graph step minus trace kernel (prefix, memsets, split, GEMM, rows); the "
+                                          "GEMM's own roofline is bench.py --workload synth"}
+    g.close()
+    if rank != 0:
+        return
+    # exact traversal work of batch 0 (counting instantiation over every 4th pose, scaled by paths)
+    sub = np.arange(0, Q, 4)
+    counts = be.traversal_counts(w.rf, N, t, [w.tx[i] for i in sub], [w.rx[i] for i in sub], w.budget[sub])
+    scale = batch_paths[0] / float(w.budget[sub].sum())
+    alg_bytes = counts["bytes"] * scale
+    hbm, peak_kind = measured_peaks()
+    l2 = l2_read_gbs()
+    achieved = alg_bytes / (trace_ms / 1000.0) / 1e9
+    cpu_val, cpu_cores, cpu_s, cpu_what = cpu_baseline_boxes(w, t)
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "batch": "%d of the %d poses per step; step k traces batch k mod %d" % (Q, B.P, nb),
+                   "paths_per_step_per_gpu": timed_paths / args.steps, "poses": B.P, "max_bounces": w.max_depth,
+                   "range_bins": N, "phase": "split-fp64", "splat": "fine histogram + split-BF16 tcgen05 synthesis",
+                   "launch": "captured CUDA graph (hsr_batch_graph_*), one persistent trace launch per step",
+                   "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas x%d" % world,
+                   "launch_config": {k: tuned[k] for k in ("tile", "ctas_per_sm", "queue_threshold", "field_on_hit")},
+                   "autotune_trace_ms": [tuned["default_trace_ms"], tuned["trace_ms"]]},
+        "e2e": {"value": world * timed_paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s / args.steps,
+                "call": "hsr_simulate_batch (host buffers, synchronous), split-FP64 phase, fine synthesis"},
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2,
+                     "traffic": args.traffic if args.traffic is not None else NCU_TRAFFIC.get("boxes"),
+                     "kernel": "k_wave", "kernel_ms": trace_ms, "algorithmic_bytes": alg_bytes,
+                     "rays": counts["rays"] * scale, "nodes": counts["nodes"] * scale, "tris": counts["tris"] * scale,
+                     "peak_source": "L2 read bandwidth measured live (hsr_measure_l2_read, 32 MiB x 64 sweeps)",
+                     "hbm_peak": hbm, "hbm_peak_source": peak_kind, "frac_of_hbm": achieved / hbm},
+        "cpu_baseline": {"value": cpu_val, "unit": "paths/s", "cores": cpu_cores, "kind": "port",
+                         "sample": "%s (%.1f s wall)" % (cpu_what, cpu_s)},
+        "modes": modes,
+        "time_to_minus40db": time_to_error(with_boxes=True) if not args.no_tte else None,
+        "batch_graph": graph_overhead(torch, dev),
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_boxes(w, tracer):
+    """The oracle's FP32 restatement on all host cores over a bounded sample of the batched
+    configuration: the first REF_POSES poses at 2^REF_LOG2 samples each."""
+    from oracle import pyoracle
+    ora = pyoracle.Scene(w.mesh)
+    t0 = time.perf_counter()
+    for i in range(REF_POSES):
+        ora.simulate(w.rf, w.frame, w.tx[i], w.rx[i], tracer, 1 << REF_LOG2, precision=32)
+    dt = time.perf_counter() - t0
+    return REF_POSES * (1 << REF_LOG2) / dt, os.cpu_count(), dt, \
+        "the first %d poses at 2^%d Halton samples each" % (REF_POSES, REF_LOG2)
+
+
 def graph_overhead(torch, dev, reps=50):
     """Per-batch device time of a small batch (the dihedral sweep, 91 poses x 2^12
     samples) through hsr_simulate_batch_device and through its captured CUDA graph
@@ -479,17 +712,39 @@ TTE_TARGET = 1e-2  # -40 dB: relative L2 of the complex IF signal
 # (error ~ budget^-0.49 with rare grazing next-event spikes; still 10 % off at 2^32), so
 # the reference there is the guided estimator (unbiased, same integrand) at 2^33: two
 # independent 2^32 guided runs agree to 0.3-0.6 %.
-TTE_SCENES = {"sphere_ground": (True, 33, 31), "dihedral_91": (False, 28, 26)}
+TTE_SCENES = {"sphere_ground": (True, 33, 31), "dihedral_91": (False, 28, 26), "boxes_16": (False, 26, 23)}
+TTE_BOXES_POSES = 16  # the batched configuration's first 16 poses
+TTE_ANCHOR = 1 << 16  # budget of the FP64-oracle anchor of each scene's converged reference
 TTE_REF_OFFSET = 1_000_000_000_007
 
 
-def time_to_error():
-    """Time to -40 dB IF-signal error against the plain GPU form, on the sphere+ground pose
-    and the 91-pose dihedral sweep. Each form's rows at budget 2^k (Halton indices
-    0 .. 2^k-1, k = 10, 11, ...) are compared with a converged run of the same estimator
-    (split-FP64 phase, Halton indices from TTE_REF_OFFSET: guided at 2^33 samples per
-    pose for the sphere, plain at 2^28 for the dihedral; relative L2 over all poses'
-    rows); the
+def fp64_anchor(w, be, tracer, poses):
+    """How far the GPU's split-FP64 form is from the FP64 oracle on the SAME samples: the
+    oracle in double precision fed the float Halton values of the FP32 run (precision 65),
+    against the GPU's split-FP64 rows, TTE_ANCHOR Halton indices from 0, on `poses`.
+    This is the part of a converged split-FP64 reference's distance to the FP64 oracle
+    that does not shrink with more samples (the FP32 geometry), so each scene's
+    time-to-error reference stands for the FP64 oracle to within it."""
+    from hussar_gb300 import HSR_PHASE_SPLIT_FP64
+    from oracle import pyoracle
+    ora = pyoracle.Scene(w.mesh)
+    N = w.frame.samplesPerChirp
+    budget = np.full(len(poses), TTE_ANCHOR, np.int64)
+    rows = be.simulate_batch(w.rf, N, tracer, [w.tx[i] for i in poses], [w.rx[i] for i in poses], budget,
+                             phase_mode=HSR_PHASE_SPLIT_FP64).astype(np.complex128)
+    ref = np.stack([ora.fetch_row(w.rf, N, w.tx[i], w.rx[i], tracer, TTE_ANCHOR, precision=65) for i in poses])
+    return {"poses": [int(i) for i in poses], "samples_per_pose": TTE_ANCHOR,
+            "rel_l2_split_fp64_vs_fp64_oracle": float(np.linalg.norm(rows - ref) / np.linalg.norm(ref))}
+
+
+def time_to_error(with_boxes=False):
+    """Time to -40 dB IF-signal error against the plain GPU form, on the sphere+ground pose,
+    the 91-pose dihedral sweep and (with_boxes) the first 16 poses of the batched boxes
+    configuration. Each form's rows at budget 2^k (Halton indices 0 .. 2^k-1, k = 10, 11,
+    ...) are compared with a converged run of the same estimator (split-FP64 phase, Halton
+    indices from TTE_REF_OFFSET: guided at 2^33 samples per pose for the sphere, plain at
+    2^28 for the dihedral and 2^26 for the boxes; relative L2 over all poses' rows), whose
+    own distance to the FP64 oracle on identical samples is reported (fp64_anchor); the
     smallest such budget reaching 1e-2 is then timed through the host API (wall clock,
     synchronous calls, median of 3).
       plain_gpu            one pose per call, one-thread-per-sample kernel, FP32 phase of
@@ -505,7 +760,7 @@ def time_to_error():
                            order (the same Halton samples), so it is timed at the budget the
                            batched split form needs, and its error there is reported
     A form that does not reach the target by the scene's largest budget (2^31 sphere,
-    2^26 dihedral) reports the budget extrapolated
+    2^26 dihedral, 2^23 boxes) reports the budget extrapolated
     from the slope of its last six points (log error vs log budget) and the time for it
     at its measured throughput, marked "extrapolated"."""
     from hussar_gb300 import (HSR_PHASE_REFERENCE_FP32, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16,
@@ -513,8 +768,9 @@ def time_to_error():
     L = _lib.lib()
     out = {"target_rel_l2": TTE_TARGET,
            "reference": "split-FP64 phase, same splat kernel, Halton indices from %d (disjoint from the forms'); "
-                        "sphere: guided 2^%d samples per pose, dihedral: plain 2^%d"
-                        % (TTE_REF_OFFSET, TTE_SCENES["sphere_ground"][1], TTE_SCENES["dihedral_91"][1]),
+                        "sphere: guided 2^%d samples per pose, dihedral: plain 2^%d, boxes: plain 2^%d"
+                        % (TTE_REF_OFFSET, TTE_SCENES["sphere_ground"][1], TTE_SCENES["dihedral_91"][1],
+                           TTE_SCENES["boxes_16"][1]),
            "timing": "wall clock through hsr_simulate_batch, median of 3"}
     forms = {"plain_gpu": (1, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, True, False),
              "batched_split": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16, False, False),
@@ -523,7 +779,12 @@ def time_to_error():
              "batched_split_synth_guided": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_FINE_SYNTH, False, True)}
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
-    for name, w in (("sphere_ground", scenes.sphere_ground_workload()), ("dihedral_91", scenes.dihedral_workload())):
+    todo = [("sphere_ground", scenes.sphere_ground_workload()), ("dihedral_91", scenes.dihedral_workload())]
+    if with_boxes:
+        wb = scenes.boxes_workload()
+        wb.tx, wb.rx, wb.budget = wb.tx[:TTE_BOXES_POSES], wb.rx[:TTE_BOXES_POSES], wb.budget[:TTE_BOXES_POSES]
+        todo.append(("boxes_16", wb))
+    for name, w in todo:
         ref_guided, ref_log2, max_log2 = TTE_SCENES[name]
         plain_t, guided_t = PathTracer(), PathTracer()
         plain_t.doGuiding = False
@@ -629,8 +890,9 @@ def time_to_error():
             if fname != "plain_gpu" and fname in res:
                 sec = seconds(res[fname])
                 res[fname]["speedup_vs_plain_gpu"] = (plain / sec) if (plain and sec) else None
+        anchor_poses = list(range(0, P, max(1, P // 4)))[:4]
         out[name] = dict(res, poses=P, range_bins=N, triangles=w.mesh.triangleCount(), reference_log2=ref_log2,
-                         reference_guided=ref_guided)
+                         reference_guided=ref_guided, fp64_anchor=fp64_anchor(w, be, plain_t, anchor_poses))
     out["clocks"] = clocks.stop()  # over the whole measurement
     return out
 
@@ -885,8 +1147,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=1 << 20)
     ap.add_argument("--ref-samples", type=int, default=1 << 20)
-    ap.add_argument("--workload", default="sphere",
-                    choices=["sphere", "boxes", "serve", "tte", "urban_mimo", "synth"])
+    ap.add_argument("--workload", default="boxes",
+                    choices=["boxes", "sphere", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
@@ -912,7 +1174,9 @@ def main():
         if rank == 0:
             import torch
             torch.cuda.set_device(local_rank)
-            print(json.dumps({"time_to_minus40db": time_to_error()}), flush=True)
+            print(json.dumps({"time_to_minus40db": time_to_error(with_boxes=True)}), flush=True)
+    elif args.workload == "boxes":
+        run_batched(args, rank, world, local_rank, dist)
     else:
         run_gb300(args, rank, world, local_rank, dist)
     if dist is not None:

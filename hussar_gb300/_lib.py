@@ -119,6 +119,7 @@ def lib():
     L.hsr_abi_version.restype = ctypes.c_int32
     L.hsr_last_error.restype = ctypes.c_char_p
     L.hsr_launch_count.restype = ctypes.c_int64
+    L.hsr_debug_alloc_count.restype = ctypes.c_int64
     L.hsr_default_flags.argtypes = [P(FlagsC)]
     L.hsr_default_flags.restype = None
     L.hsr_default_server_config.argtypes = [P(ServerConfigC)]
@@ -141,6 +142,8 @@ def lib():
                                ctypes.c_int32, ctypes.c_int32, vp, vp],
         "hsr_simulate_batch_device_noalloc": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp,
                                               vp, vp, ctypes.c_int32, vp, vp],
+        "hsr_scene_status": [vp, vp, P(ctypes.c_uint32)],
+        "hsr_noalloc_status": [vp, P(ctypes.c_uint32)],
         "hsr_debug_records": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), P(AntennaC), P(AntennaC),
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_traversal_counts": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp,
@@ -167,7 +170,7 @@ def lib():
         "hsr_get_launch_config": [vp, P(LaunchConfigC)],
         "hsr_measure_l2_read": [ctypes.c_int64, ctypes.c_int32, P(ctypes.c_double)],
         "hsr_batch_graph_create": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
-                                   ctypes.c_int32, vp, P(vp)],
+                                   ctypes.c_int32, ctypes.c_int32, vp, P(vp)],
         "hsr_batch_graph_launch": [vp, vp],
         "hsr_batch_graph_status": [vp],
         "hsr_batch_graph_destroy": [vp],

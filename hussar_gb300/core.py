@@ -386,15 +386,15 @@ class _GB300:
             return out
 
         def batch_graph(self, rf, samples_per_chirp, integrator, pose_count, d_tx, d_rx, d_budget, d_offset,
-                        d_out_rows, phase_mode=_lib.HSR_PHASE_REFERENCE_FP32):
+                        d_out_rows, phase_mode=_lib.HSR_PHASE_REFERENCE_FP32, splat_mode=_lib.HSR_SPLAT_DIRICHLET16):
             """The plain batch over device buffers (addresses as integers) captured into a
             CUDA graph (hsr_batch_graph_create); BatchGraph.launch(stream) replays it."""
             h = ctypes.c_void_p()
             vp = ctypes.c_void_p
             _lib.check(_lib.lib().hsr_batch_graph_create(
                 self._scene, ctypes.byref(rf.to_c()), int(samples_per_chirp), ctypes.byref(integrator.flags_c()),
-                int(pose_count), vp(d_tx), vp(d_rx), vp(d_budget), vp(d_offset), int(phase_mode), vp(d_out_rows),
-                ctypes.byref(h)))
+                int(pose_count), vp(d_tx), vp(d_rx), vp(d_budget), vp(d_offset), int(phase_mode), int(splat_mode),
+                vp(d_out_rows), ctypes.byref(h)))
             return BatchGraph(h, self)
 
         def autotune(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None,

@@ -21,6 +21,8 @@ int g_synth_engine = 0;
 static std::atomic<int64_t> g_launches{0};
 
 void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+static std::atomic<int64_t> g_allocs{0};
+void note_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 
 static hsr_status fail(hsr_status s, const std::string &msg) {
     g_err = msg;
@@ -108,7 +110,10 @@ static Scratch carve(void *base, int32_t P, int32_t N, bool fine) {
     return s;
 }
 
-static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &out, bool fine = false) {
+// Carves the scene's scratch for P poses with N bins (growing it when needed) and clears
+// the status word on `st`: every call reports the device status of its own work only.
+static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &out, cudaStream_t st,
+                                 bool fine = false) {
     Scratch need = carve(nullptr, P, N, fine);
     if (need.bytes > sc.scratch_bytes) {
         if (sc.scratch) {
@@ -117,14 +122,16 @@ static hsr_status ensure_scratch(SceneDev &sc, int32_t P, int32_t N, Scratch &ou
         }
         sc.scratch = nullptr;
         sc.scratch_bytes = 0;
-        cudaError_t e = cudaMalloc(&sc.scratch, need.bytes);
-        if (e != cudaSuccess) return cuda_fail(e, "scratch allocation");
+        std::string err;
+        if (!dev_alloc(&sc.scratch, need.bytes, err)) return fail(HSR_ERR_OUT_OF_MEMORY, "scratch allocation: " + err);
         // the status word must start clear; the rest is initialised per call
-        e = cudaMemset(sc.scratch, 0, 256);
+        cudaError_t e = cudaMemset(sc.scratch, 0, 256);
         if (e != cudaSuccess) return cuda_fail(e, "scratch clear");
         sc.scratch_bytes = need.bytes;
     }
     out = carve(sc.scratch, P, N, fine);
+    cudaError_t e = cudaMemsetAsync(out.counters, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return cuda_fail(e, "status clear");
     return HSR_OK;
 }
 
@@ -146,8 +153,8 @@ static hsr_status ensure_synth(SceneDev &sc, int32_t N, int32_t P, cudaStream_t 
         cudaFree(sc.synth_scratch);
         sc.synth_scratch = nullptr;
         sc.synth_scratch_bytes = 0;
-        cudaError_t e = cudaMalloc(&sc.synth_scratch, need);
-        if (e != cudaSuccess) return cuda_fail(e, "synthesis scratch");
+        std::string err;
+        if (!dev_alloc(&sc.synth_scratch, need, err)) return fail(HSR_ERR_OUT_OF_MEMORY, "synthesis scratch: " + err);
         sc.synth_scratch_bytes = need;
     }
     return HSR_OK;
@@ -202,8 +209,8 @@ static hsr_status ensure_guide(SceneDev &sc, int P, GuideMem &out) {
         sc.guide = nullptr;
         sc.guide_cap = 0;
         const size_t bytes = guide_bytes_per_pose() * size_t(P) + 8 * 256;
-        cudaError_t e = cudaMalloc(&sc.guide, bytes);
-        if (e != cudaSuccess) return cuda_fail(e, "guiding allocation");
+        std::string err;
+        if (!dev_alloc(&sc.guide, bytes, err)) return fail(HSR_ERR_OUT_OF_MEMORY, "guiding allocation: " + err);
         sc.guide_cap = P;
     }
     out = carve_guide(sc.guide, P);
@@ -465,6 +472,16 @@ static hsr_status run_guided(SceneDev &sc, const Scratch &s, const hsr_rf_config
     return HSR_OK;
 }
 
+// The status word's bits as text (kStatus* in hsr_common.cuh; bit 3 from hsr_synth.cu).
+std::string status_text(unsigned bits) {
+    std::string m = "device status:";
+    if (bits & kStatusStackOverflow) m += " traversal-stack-overflow";
+    if (bits & kStatusBadBin) m += " bin-out-of-range";
+    if (bits & kStatusBadWorkItem) m += " bad-work-item";
+    if (bits & (1u << 3)) m += " synthesis-wait-timeout";
+    return m;
+}
+
 static hsr_status read_status(const Scratch &s, cudaStream_t st) {
     unsigned bits = 0;
     cudaError_t e = cudaMemcpyAsync(&bits, s.counters, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
@@ -473,12 +490,7 @@ static hsr_status read_status(const Scratch &s, cudaStream_t st) {
     if (bits) {
         cudaMemsetAsync(s.counters, 0, sizeof(unsigned), st);
         cudaStreamSynchronize(st);
-        std::string m = "device status:";
-        if (bits & kStatusStackOverflow) m += " traversal-stack-overflow";
-        if (bits & kStatusBadBin) m += " bin-out-of-range";
-        if (bits & kStatusBadWorkItem) m += " bad-work-item";
-        if (bits & (1u << 3)) m += " synthesis-wait-timeout";
-        return fail(HSR_ERR_DEVICE, m);
+        return fail(HSR_ERR_DEVICE, status_text(bits));
     }
     return HSR_OK;
 }
@@ -507,6 +519,7 @@ namespace hsr {
 // Read access to a scene's device state, and the calling thread's error message, for
 // entry points defined in other translation units.
 const SceneDev *scene_device_state(const hsr_scene *s) { return s ? &s->dev : nullptr; }
+std::mutex *scene_mutex(hsr_scene *s) { return s ? &s->mu : nullptr; }
 void set_last_error(const std::string &msg) { g_err = msg; }
 }  // namespace hsr
 
@@ -517,6 +530,23 @@ int32_t hsr_abi_version(void) { return HSR_ABI_VERSION; }
 const char *hsr_last_error(void) { return g_err.c_str(); }
 
 int64_t hsr_launch_count(void) { return g_launches.load(); }
+
+int64_t hsr_debug_alloc_count(void) { return g_allocs.load(); }
+
+hsr_status hsr_scene_status(hsr_scene *s, void *stream, uint32_t *out_bits) {
+    if (out_bits) *out_bits = 0;
+    if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->dev.scratch) return HSR_OK;  // no call has run on this scene yet
+    cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    unsigned bits = 0;
+    cudaError_t e = cudaStreamSynchronize(strm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, s->dev.scratch, sizeof(unsigned), cudaMemcpyDeviceToHost, strm);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    if (out_bits) *out_bits = bits;
+    return bits ? fail(HSR_ERR_DEVICE, status_text(bits)) : HSR_OK;
+}
 
 void hsr_default_flags(hsr_tracer_flags *f) {
     if (!f) return;
@@ -718,7 +748,7 @@ hsr_status hsr_debug_records(hsr_scene *s, const hsr_rf_config *rf, int32_t samp
         return fail(HSR_ERR_INVALID_ARGUMENT, "bad record request");
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, 1, samples, sc)) != HSR_OK) return st;
+    if ((st = ensure_scratch(s->dev, 1, samples, sc, 0)) != HSR_OK) return st;
     const size_t rec_bytes = size_t(budget) * max_rec * 36;
     void *d_rec = nullptr;
     std::string err;
@@ -763,8 +793,8 @@ hsr_status hsr_backend_run(const hsr_scene *cs, const hsr_rf_config *rf, const h
     const int32_t N = frame->samplesPerChirp;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, 1, N, sc)) != HSR_OK) return st;
     cudaStream_t strm = 0;
+    if ((st = ensure_scratch(s->dev, 1, N, sc, strm)) != HSR_OK) return st;
     if ((st = upload_poses(sc, 1, tx, rx, &budget, &index_offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
     st = run_plain(s->dev, sc, rf, N, fl, 1, sample_weight, phase_mode, HSR_SPLAT_DIRICHLET16, 0, sc.rows, strm);
     if (st != HSR_OK) return st;
@@ -811,8 +841,8 @@ hsr_status hsr_path_tracer_run(hsr_scene *s, const hsr_rf_config *rf, const hsr_
     const int32_t N = frame->samplesPerChirp;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, 1, N, sc)) != HSR_OK) return st;
     cudaStream_t strm = 0;
+    if ((st = ensure_scratch(s->dev, 1, N, sc, strm)) != HSR_OK) return st;
     int64_t zero = 0;
     if ((st = upload_poses(sc, 1, tx, rx, &samples, &zero, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
     double tw = 0.0;
@@ -847,8 +877,8 @@ hsr_status hsr_simulate_batch_device(hsr_scene *s, const hsr_rf_config *rf, int3
     if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    if ((st = ensure_scratch(s->dev, P, N, sc, strm, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     if ((st = upload_poses(sc, P, d_tx, d_rx, d_budget, d_offset, cudaMemcpyDeviceToDevice, strm)) != HSR_OK)
         return st;
     if (!fl->doGuiding)
@@ -876,8 +906,8 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    if ((st = ensure_scratch(s->dev, P, N, sc, strm, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
     if (!fl->doGuiding) {
         st = run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, sc.rows, strm);
@@ -911,9 +941,9 @@ hsr_status hsr_simulate_batch_ff(hsr_scene *s, const hsr_rf_config *rf, int32_t 
     }
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
-    sc.far_field = true;
     cudaStream_t strm = nullptr;
+    if ((st = ensure_scratch(s->dev, P, N, sc, strm)) != HSR_OK) return st;
+    sc.far_field = true;
     cudaError_t e;
     if ((e = cudaMemcpyAsync(sc.ff_tx, tx, sizeof(hsr_ff_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
         (e = cudaMemcpyAsync(sc.ff_rx, rx, sizeof(hsr_ff_antenna) * P, cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
@@ -951,7 +981,7 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     std::lock_guard<std::mutex> lk(s->mu);
     SceneDev &d = s->dev;
     Scratch sc;
-    if ((st = ensure_scratch(d, P, N, sc, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
+    if ((st = ensure_scratch(d, P, N, sc, nullptr, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
     if ((st = upload_poses(sc, P, tx, rx, budget, offset, cudaMemcpyHostToDevice, nullptr)) != HSR_OK) return st;
     const LaunchConfig saved = d.tuned;
     auto trial = [&](const LaunchConfig &c, float &ms) -> hsr_status {
@@ -1056,7 +1086,7 @@ hsr_status hsr_debug_traversal_counts(hsr_scene *s, const hsr_rf_config *rf, int
     if (st != HSR_OK) return st;
     std::lock_guard<std::mutex> lk(s->mu);
     Scratch sc;
-    if ((st = ensure_scratch(s->dev, P, N, sc)) != HSR_OK) return st;
+    if ((st = ensure_scratch(s->dev, P, N, sc, nullptr)) != HSR_OK) return st;
     unsigned long long *d_cnt = nullptr;
     std::string err;
     if (!dev_alloc(&d_cnt, 4 * sizeof(unsigned long long), err)) return fail(HSR_ERR_OUT_OF_MEMORY, err);
@@ -1168,39 +1198,61 @@ struct hsr_batch_graph {
     hsr_scene *scene = nullptr;
     void *scratch = nullptr;
     unsigned *status = nullptr;
+    // fine-histogram synthesis: the graph's own twiddle operand and synthesis scratch
+    // (the scene's are rebuilt when another call uses another N)
+    SynthOperand synth;
+    void *synth_scratch = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    int64_t kernel_nodes = 0;  // kernels one replay launches (hsr_launch_count)
 };
 
 hsr_status hsr_batch_graph_create(hsr_scene *s, const hsr_rf_config *rf, int32_t N, const hsr_tracer_flags *fl,
                                   int32_t P, const hsr_antenna *d_tx, const hsr_antenna *d_rx,
                                   const int64_t *d_budget, const int64_t *d_offset, int32_t phase_mode,
-                                  float *d_out_rows, hsr_batch_graph **out) {
+                                  int32_t splat_mode, float *d_out_rows, hsr_batch_graph **out) {
     if (!out) return fail(HSR_ERR_INVALID_ARGUMENT, "out is null");
     *out = nullptr;
     if (!s || !d_tx || !d_rx || !d_budget || !d_offset || !d_out_rows || P <= 0)
         return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no poses");
     hsr_status st = validate_common(rf, N, fl);
     if (st != HSR_OK) return st;
-    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
+    if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
     if (fl->doGuiding)
         return fail(HSR_ERR_NOT_SUPPORTED, "a batch graph runs the plain method (doGuiding must be 0)");
     std::lock_guard<std::mutex> lk(s->mu);
     std::unique_ptr<hsr_batch_graph> g(new hsr_batch_graph());
     g->scene = s;
-    const Scratch need = carve(nullptr, P, N, false);
-    cudaError_t e = cudaMalloc(&g->scratch, need.bytes);
-    if (e != cudaSuccess) return cuda_fail(e, "graph scratch allocation");
+    const bool fine = splat_mode == HSR_SPLAT_FINE_SYNTH;
+    const Scratch need = carve(nullptr, P, N, fine);
+    std::string aerr;
+    if (!dev_alloc(&g->scratch, need.bytes, aerr)) return fail(HSR_ERR_OUT_OF_MEMORY, "graph scratch: " + aerr);
+    cudaError_t e;
+    // the scene's state as the capture sees it, with the graph's own synthesis operand and
+    // scratch (allocated here, before the capture; run_plain's ensure_synth then finds
+    // them in place)
+    SceneDev gdev = s->dev;
+    gdev.synth = SynthOperand{};
+    gdev.synth_scratch = nullptr;
+    gdev.synth_scratch_bytes = 0;
     auto cleanup = [&]() {
         if (g->exec) cudaGraphExecDestroy(g->exec);
         if (g->graph) cudaGraphDestroy(g->graph);
         cudaFree(g->scratch);
+        synth_free_operand(gdev.synth);
+        cudaFree(gdev.synth_scratch);
     };
     if ((e = cudaMemset(g->scratch, 0, 256)) != cudaSuccess) {
         cleanup();
         return cuda_fail(e, "graph scratch clear");
     }
-    const Scratch sc = carve(g->scratch, P, N, false);
+    if (fine) {
+        if ((st = ensure_synth(gdev, N, P, nullptr)) != HSR_OK || (e = cudaDeviceSynchronize()) != cudaSuccess) {
+            cleanup();
+            return st != HSR_OK ? st : cuda_fail(e, "graph synthesis operand");
+        }
+    }
+    const Scratch sc = carve(g->scratch, P, N, fine);
     g->status = sc.counters;
     cudaStream_t cs = nullptr;
     if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -1212,8 +1264,7 @@ hsr_status hsr_batch_graph_create(hsr_scene *s, const hsr_rf_config *rf, int32_t
         rst = cuda_fail(e, "begin capture");
     } else {
         rst = upload_poses(sc, P, d_tx, d_rx, d_budget, d_offset, cudaMemcpyDeviceToDevice, cs);
-        if (rst == HSR_OK)
-            rst = run_plain(s->dev, sc, rf, N, fl, P, 1.f, phase_mode, HSR_SPLAT_DIRICHLET16, 1, d_out_rows, cs);
+        if (rst == HSR_OK) rst = run_plain(gdev, sc, rf, N, fl, P, 1.f, phase_mode, splat_mode, 1, d_out_rows, cs);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(cs, &graph);
         g->graph = graph;
@@ -1227,6 +1278,19 @@ hsr_status hsr_batch_graph_create(hsr_scene *s, const hsr_rf_config *rf, int32_t
         cleanup();
         return rst;
     }
+    g->synth = gdev.synth;
+    g->synth_scratch = gdev.synth_scratch;
+    size_t n_nodes = 0;
+    if (cudaGraphGetNodes(g->graph, nullptr, &n_nodes) == cudaSuccess && n_nodes > 0) {
+        std::vector<cudaGraphNode_t> nodes(n_nodes);
+        if (cudaGraphGetNodes(g->graph, nodes.data(), &n_nodes) == cudaSuccess)
+            for (size_t i = 0; i < n_nodes; ++i) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nodes[i], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                    ++g->kernel_nodes;
+            }
+    }
+    cudaGetLastError();
     *out = g.release();
     return HSR_OK;
 }
@@ -1235,7 +1299,7 @@ hsr_status hsr_batch_graph_launch(hsr_batch_graph *g, void *stream) {
     if (!g || !g->exec) return fail(HSR_ERR_INVALID_ARGUMENT, "null graph");
     cudaError_t e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "graph launch");
-    note_launches(1);
+    note_launches(std::max<int64_t>(g->kernel_nodes, 1));
     return HSR_OK;
 }
 
@@ -1256,6 +1320,8 @@ hsr_status hsr_batch_graph_destroy(hsr_batch_graph *g) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->scratch);
+    synth_free_operand(g->synth);
+    cudaFree(g->synth_scratch);
     delete g;
     return HSR_OK;
 }

@@ -23,6 +23,45 @@ enum StatusBits : unsigned {
     // bit 3: a synthesis GEMM wait gave up (hsr_synth.cu)
 };
 
+// sin and cos of a float angle, each rounded once to float (for |x| up to a few 2pi).
+// x - k pi/2 (k = nearest integer to x 2/pi) in double by a two-part pi/2 with fused
+// multiply-adds, then the Taylor series of sin (to degree 15) and cos (to degree 16) on
+// the remainder (|r| <= pi/4: truncation below 7e-17 relative) by Horner's rule in
+// double, rounded to float. Every operation is an IEEE double operation with a single
+// rounding (fma, *, +, rint, the final conversion), so the host and the device compute
+// the same bits for the same x; the float results are the correctly rounded ones except
+// where the exact value lies within ~2^-50 of a float rounding midpoint. Coefficients are
+// 1/n! rounded to double (hex literals).
+__host__ __device__ inline void sincos_rounded(float x, float *s, float *c) {
+    const double xd = double(x);
+    const double k = rint(xd * 0x1.45f306dc9c883p-1);                 // x 2/pi
+    double r = fma(-k, 0x1.921fb54442d18p+0, xd);                       // pi/2, high part
+    r = fma(-k, 0x1.1a62633145c07p-54, r);                              // pi/2, low part
+    const double z = r * r;
+    double ps = -0x1.ae7f3e733b81fp-41;                                 // -1/15!
+    ps = fma(ps, z, 0x1.6124613a86d09p-33);                             //  1/13!
+    ps = fma(ps, z, -0x1.ae64567f544e4p-26);                            // -1/11!
+    ps = fma(ps, z, 0x1.71de3a556c734p-19);                             //  1/9!
+    ps = fma(ps, z, -0x1.a01a01a01a01ap-13);                            // -1/7!
+    ps = fma(ps, z, 0x1.1111111111111p-7);                              //  1/5!
+    ps = fma(ps, z, -0x1.5555555555555p-3);                             // -1/3!
+    const double sr = fma(r * z, ps, r);
+    double pc = 0x1.ae7f3e733b81fp-45;                                  //  1/16!
+    pc = fma(pc, z, -0x1.93974a8c07c9dp-37);                            // -1/14!
+    pc = fma(pc, z, 0x1.1eed8eff8d898p-29);                             //  1/12!
+    pc = fma(pc, z, -0x1.27e4fb7789f5cp-22);                            // -1/10!
+    pc = fma(pc, z, 0x1.a01a01a01a01ap-16);                             //  1/8!
+    pc = fma(pc, z, -0x1.6c16c16c16c17p-10);                            // -1/6!
+    pc = fma(pc, z, 0x1.5555555555555p-5);                              //  1/4!
+    pc = fma(pc, z, -0.5);                                              // -1/2!
+    const double cr = fma(z, pc, 1.0);
+    const int q = int(k) & 3;
+    const double sv = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+    const double cv = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+    *s = static_cast<float>(sv);
+    *c = static_cast<float>(cv);
+}
+
 struct f3 {
     float x, y, z;
 };

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 
 #include "../../include/hsr_gb300.h"
@@ -64,7 +65,11 @@ struct SceneDev {
     int sm_count = 0;
 };
 
+// Counts every device allocation the library makes (hsr_debug_alloc_count).
+void note_alloc();
+
 template <typename T> inline bool dev_alloc(T **p, size_t bytes, std::string &err) {
+    note_alloc();
     cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), bytes ? bytes : 16);
     if (e != cudaSuccess) {
         err = std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e);
@@ -77,6 +82,10 @@ template <typename T> inline bool dev_alloc(T **p, size_t bytes, std::string &er
 
 void note_launches(int64_t n);
 const SceneDev *scene_device_state(const hsr_scene *s);
+// The device status word's bits as a message ("device status: ...").
+std::string status_text(unsigned bits);
+// The scene's call lock (calls on one scene are serialised).
+std::mutex *scene_mutex(hsr_scene *s);
 void set_last_error(const std::string &msg);
 
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,

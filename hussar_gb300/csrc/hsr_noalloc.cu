@@ -18,6 +18,13 @@
 // the same array and race: serialise them. The first call on a device looks up the
 // array's device address (cudaGetSymbolAddress) with that device current; make that first
 // call before any stream capture.
+//
+// The call runs the launch shape the scene was tuned to (hsr_autotune_batch /
+// hsr_set_launch_config) and the kernel hsr_set_path_kernel selects, as
+// hsr_simulate_batch_device does. Device-side conditions (traversal stack overflow, a bin
+// out of range, a bad work item) set bits in the array's status word; the call returns
+// before the GPU has run, so the caller reads them with hsr_noalloc_status once the work
+// is done (it synchronises the stream; the word is cleared by the next call).
 #include <mutex>
 
 #include "hsr_common.cuh"
@@ -86,6 +93,13 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
         set_last_error("null argument");
         return HSR_ERR_INVALID_ARGUMENT;
     }
+    // the scene's BVH lives on the device it was built on: the call must be issued there
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != sc->device) {
+        cudaGetLastError();
+        set_last_error("the current device is not the device the scene was built on");
+        return HSR_ERR_INVALID_ARGUMENT;
+    }
     const int32_t N = samples_per_chirp, P = pose_count;
     if (P <= 0 || P > kNoAllocMaxPoses) {
         set_last_error("pose_count must be in [1, " + std::to_string(kNoAllocMaxPoses) +
@@ -112,6 +126,9 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
     NoAllocScratch *s = nullptr;
     hsr_status st = noalloc_scratch(&s);
     if (st != HSR_OK) return st;
+    // serialised with the scene's other calls (its tuned shape is read below); the scene
+    // must not be destroyed while this call's work is in flight
+    std::lock_guard<std::mutex> lk(*scene_mutex(scene));
     cudaStream_t strm = static_cast<cudaStream_t>(stream);
     // what must start at zero: status word, work counter, this call's accumulators
     cudaError_t e = cudaMemsetAsync(s->counters, 0, sizeof(s->counters), strm);
@@ -121,9 +138,11 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
         set_last_error(std::string("clearing the static scratch: ") + cudaGetErrorString(e));
         return HSR_ERR_CUDA;
     }
-    constexpr int32_t kTile = 4096;
+    // the scene's tuned work-item size where it has one, else 4096 samples (the prefix
+    // holds pose_count + 1 entries whatever the tile)
+    const int32_t tile = sc->tuned.tile > 0 ? sc->tuned.tile : 4096;
     int64_t *tile_start = reinterpret_cast<int64_t *>(s->tile_start);
-    if (launch_tile_prefix(d_budget, P, kTile, tile_start, strm) != 0) {
+    if (launch_tile_prefix(d_budget, P, tile, tile_start, strm) != 0) {
         set_last_error("tile prefix launch failed");
         return HSR_ERR_CUDA;
     }
@@ -140,13 +159,19 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
     p.offset = d_index_offset;
     p.tile_start = tile_start;
     p.sample_weight = 1.f;
-    p.tile = kTile;
+    p.tile = tile;
     p.acc = s->acc;
     p.status = s->counters;
     p.work_counter = s->counters + 2;
     std::string err;
-    const bool wave = flags->useGeometricalOptics != 0;
-    const int grid = sc->sm_count * (wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, HSR_SPLAT_DIRICHLET16, 0));
+    const bool wave = g_path_kernel == 0 && flags->useGeometricalOptics != 0;
+    int per_sm = wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, HSR_SPLAT_DIRICHLET16, 0);
+    if (wave) {
+        if (sc->tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc->tuned.ctas_per_sm);
+        p.queue_threshold = sc->tuned.queue_threshold;
+        p.field_on_hit = sc->tuned.field_on_hit;
+    }
+    const int grid = sc->sm_count * per_sm;
     const int rc = wave ? launch_wave(p, phase_mode, grid, strm, err)
                         : launch_trace(p, phase_mode, HSR_SPLAT_DIRICHLET16, grid, strm, err);
     if (rc != 0) {
@@ -156,6 +181,29 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
     if (launch_finalize(s->acc, P, N, d_budget, 1.f, nullptr, 1, d_out_rows, strm) != 0) {
         set_last_error("finalize launch failed");
         return HSR_ERR_CUDA;
+    }
+    return HSR_OK;
+}
+
+extern "C" hsr_status hsr_noalloc_status(void *stream, uint32_t *out_bits) {
+    if (out_bits) *out_bits = 0;
+    NoAllocScratch *s = nullptr;
+    hsr_status st = noalloc_scratch(&s);
+    if (st != HSR_OK) return st;
+    cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    unsigned bits = 0;
+    cudaError_t e = cudaStreamSynchronize(strm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, s->counters, sizeof(unsigned), cudaMemcpyDeviceToHost, strm);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(strm);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error(std::string("reading the static scratch's status word: ") + cudaGetErrorString(e));
+        return HSR_ERR_CUDA;
+    }
+    if (out_bits) *out_bits = bits;
+    if (bits) {
+        set_last_error(status_text(bits));
+        return HSR_ERR_DEVICE;
     }
     return HSR_OK;
 }

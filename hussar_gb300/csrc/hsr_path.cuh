@@ -144,13 +144,24 @@ __device__ __forceinline__ Ant load_ant(const hsr_antenna *a) {
     return r;
 }
 
-// UniformSampleSphere (libhussar/include/hussar/core/sampling.h:38-43)
-__device__ __forceinline__ f3 uniform_sample_sphere(float u0, float u1) {
+// UniformSampleSphere (libhussar/include/hussar/core/sampling.h:38-43). kExact (the
+// reference-phase parity instantiations): sin and cos of phi correctly rounded
+// (sincos_rounded), bit for bit what the CPU restatement computes; the reference's
+// std::sin/std::cos of a float resolve to the platform's sinf/cosf, which are not
+// correctly rounded everywhere (glibc 2.39: one ulp off on 1.3 % of uniformly
+// distributed angles), and CUDA's sincosf differs from both by up to two ulps. A one-ulp
+// change of a primary direction moves the hit points of far sensors by micrometres,
+// enough to change PO amplitudes measurably on large scenes. The split-phase form keeps
+// the fast sincosf (it is bounded against the FP64 oracle, not matched bit for bit).
+template <bool kExact = true> __device__ __forceinline__ f3 uniform_sample_sphere(float u0, float u1) {
     float phi = 2.f * kPi * u0;
     float y = 2.f * u1 - 1.f;
     float r = sqrtf(fmaxf(0.f, 1.f - y * y));
     float s, c;
-    sincosf(phi, &s, &c);
+    if (kExact)
+        sincos_rounded(phi, &s, &c);
+    else
+        sincosf(phi, &s, &c);
     return mk3(-r * s, y, -r * c);
 }
 
@@ -180,8 +191,9 @@ __device__ __forceinline__ c3 antenna_field(const Ant &tx, f3 ld) {
     return mulcv(tx.rot, c3_div(awr_eval(ld), kInv4Pi));
 }
 
+template <bool kExact = true>
 __device__ __forceinline__ void antenna_sample(const Ant &tx, float u0, float u1, f3 &d, c3 &H) {
-    f3 ld = uniform_sample_sphere(u0, u1);
+    f3 ld = uniform_sample_sphere<kExact>(u0, u1);
     c3 lH = c3_div(awr_eval(ld), kInv4Pi);
     d = mulv(tx.rot, ld);
     H = mulcv(tx.rot, lH);

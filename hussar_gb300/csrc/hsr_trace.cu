@@ -66,13 +66,13 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
                 ff_sample(ftx, px, py, o, d, H);
             } else {
                 o = tx.pos;
-                antenna_sample(tx, px, py, d, H);
+                antenna_sample<kPhase == HSR_PHASE_REFERENCE_FP32>(tx, px, py, d, H);
             }
             H = c3_scl(H, 1.f / primaryPdf);
         } else if (!fl.useGeometricalOptics) {
             float u0 = halton(hindex, dim++);
             float u1 = halton(hindex, dim++);
-            d = uniform_sample_sphere(u0, u1);
+            d = uniform_sample_sphere<kPhase == HSR_PHASE_REFERENCE_FP32>(u0, u1);
             H = surface_eval(hit_n, inc_H, d);
         } else {
             reflect(hit_n, d, H);

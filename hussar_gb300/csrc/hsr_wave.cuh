@@ -252,12 +252,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                     H = c3_scl(H, 1.f / g.pdf);
                 } else if (kLazy) {
                     o = pc.tx.pos;
-                    ldir = uniform_sample_sphere(g.x0, g.x1);
+                    ldir = uniform_sample_sphere<kPhase == HSR_PHASE_REFERENCE_FP32>(g.x0, g.x1);
                     d = mulv(pc.tx.rot, ldir);
                     if (!deferred) H = c3_scl(antenna_field(pc.tx, ldir), 1.f / g.pdf);
                 } else {
                     o = pc.tx.pos;
-                    antenna_sample(pc.tx, g.x0, g.x1, d, H);
+                    antenna_sample<kPhase == HSR_PHASE_REFERENCE_FP32>(pc.tx, g.x0, g.x1, d, H);
                     H = c3_scl(H, 1.f / g.pdf);
                 }
                 if (!fl.onlyIndirect) {

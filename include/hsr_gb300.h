@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HSR_ABI_VERSION 3
+#define HSR_ABI_VERSION 4
 
 typedef enum hsr_status {
     HSR_OK = 0,
@@ -136,6 +136,10 @@ int32_t hsr_abi_version(void);
 const char *hsr_last_error(void);
 /* Number of kernel launches this library has issued in the calling process. */
 int64_t hsr_launch_count(void);
+/* Device allocations (cudaMalloc) the library has made so far in this process: scenes,
+ * scratch, operands, graphs. No counterpart in the reference; lets a caller check that a
+ * call allocated nothing. */
+int64_t hsr_debug_alloc_count(void);
 
 /* Fills default PathTracer flags exactly as the reference initialises them
  * (path.h:153-169: onlyIndirect=1, maxDepth=10, useGeometricalOptics=1,
@@ -228,6 +232,17 @@ hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
                                      const int64_t *d_index_offset, int32_t phase_mode,
                                      int32_t splat_mode, float *d_out_rows, void *stream);
 
+/* Device status of the last call on this scene: synchronises `stream` (the stream that
+ * call ran on) and reads the status word that call's kernels set, into *out_bits (may be
+ * NULL): traversal stack overflow (bit 0), a bin out of range (bit 1), a bad work item
+ * (bit 2), a synthesis wait that gave up (bit 3). Returns HSR_ERR_DEVICE with the bits
+ * named in hsr_last_error() when any is set. The synchronous entry points report their
+ * own status on return; hsr_simulate_batch_device returns before the GPU has run, so its
+ * status is read here. Every call on a scene starts with a clear word, so read it before
+ * the next call on the scene. The reference throws on device errors from its synchronous
+ * launch (sutil::Exception, Exception.h:91-191); this is the asynchronous counterpart. */
+hsr_status hsr_scene_status(hsr_scene *scene, void *stream, uint32_t *out_bits);
+
 /* Allocation-free form of hsr_simulate_batch_device, for callers that cannot allocate
  * device memory while they simulate (a real-time loop, work recorded into a larger
  * asynchronous pipeline, a framework whose memory pool must own every allocation).
@@ -239,7 +254,10 @@ hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
  * and 1024 range bins per call; larger requests return HSR_ERR_INVALID_ARGUMENT.
  * The array is shared by all calls on a device and keeps the last call's contents:
  * calls that overlap on the GPU race and must be serialised by the caller. The first
- * call on a device looks the array's address up (make it before any stream capture). */
+ * call on a device looks the array's address up (make it before any stream capture).
+ * The call must be issued with the scene's device current, uses the scene's tuned launch
+ * shape and the kernel hsr_set_path_kernel selects, and returns before the GPU has run:
+ * read its device status with hsr_noalloc_status. */
 hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const hsr_rf_config *rf,
                                              int32_t samples_per_chirp,
                                              const hsr_tracer_flags *flags, int32_t pose_count,
@@ -247,6 +265,13 @@ hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const hsr_rf_conf
                                              const int64_t *d_budget,
                                              const int64_t *d_index_offset, int32_t phase_mode,
                                              float *d_out_rows, void *stream);
+
+/* Device status of the last hsr_simulate_batch_device_noalloc call on the current
+ * device: synchronises `stream` and reads the status word in the library's static
+ * scratch (bits as hsr_scene_status; HSR_ERR_DEVICE when any is set). Allocates nothing.
+ * The next allocation-free call on the device clears the word. No counterpart in the
+ * reference. */
+hsr_status hsr_noalloc_status(void *stream, uint32_t *out_bits);
 
 /* Far-field runs (RCS-style): as hsr_simulate_batch for the plain method, with each
  * pose's TX and RX a far-field antenna (hsr_ff_antenna). In the reference an FFAntenna
@@ -358,20 +383,21 @@ hsr_status hsr_last_kernel_ms(const hsr_scene *scene, float *out_ms);
 /* ---- A plain batch captured into a CUDA graph --------------------------------------
  *
  * No counterpart in the reference (its GPU backend launches one pose per call). Captures
- * hsr_simulate_batch_device's plain method (doGuiding = 0, HSR_SPLAT_DIRICHLET16) for
- * fixed device buffers once; every launch replays the whole batch (pose upload, work-item
- * prefix, the persistent trace launch, fetchFrame rows) as one graph launch and reads the
- * buffers' current contents, so poses, budgets and offsets may change between launches
- * (the pose count, N, chirp and flags may not). The graph owns its scratch; it uses the
- * scene's BVH, so destroy it before the scene. hsr_launch_count counts a graph launch as
- * one launch. */
+ * hsr_simulate_batch_device's plain method (doGuiding = 0) with the given phase and splat
+ * modes for fixed device buffers once; every launch replays the whole batch (pose upload,
+ * work-item prefix, the persistent trace launch, then the fetchFrame rows, or with
+ * HSR_SPLAT_FINE_SYNTH the tensor-core synthesis of the rows) as one graph launch and
+ * reads the buffers' current contents, so poses, budgets and offsets may change between
+ * launches (the pose count, N, chirp and flags may not). The graph owns its scratch (and,
+ * for synthesis, its own twiddle operand); it uses the scene's BVH and launch shape, so
+ * destroy it before the scene. hsr_launch_count counts a replay as the kernels it runs. */
 typedef struct hsr_batch_graph hsr_batch_graph;
 
 hsr_status hsr_batch_graph_create(hsr_scene *scene, const hsr_rf_config *rf, int32_t samples_per_chirp,
                                   const hsr_tracer_flags *flags, int32_t pose_count, const hsr_antenna *d_tx,
                                   const hsr_antenna *d_rx, const int64_t *d_budget,
-                                  const int64_t *d_index_offset, int32_t phase_mode, float *d_out_rows,
-                                  hsr_batch_graph **out_graph);
+                                  const int64_t *d_index_offset, int32_t phase_mode, int32_t splat_mode,
+                                  float *d_out_rows, hsr_batch_graph **out_graph);
 /* Asynchronous on `stream` (a cudaStream_t; NULL = legacy default stream). */
 hsr_status hsr_batch_graph_launch(hsr_batch_graph *graph, void *stream);
 /* Synchronises the device; HSR_ERR_DEVICE if any launch so far set the status word. */

@@ -254,11 +254,55 @@ template <typename R> struct Halton {
 // ----------------------------------------------------------------------------------
 // Sampling, antenna pattern, antennas (sampling.h:38-47, emitter.h:109-214)
 // ----------------------------------------------------------------------------------
+// The reference's std::sin/std::cos of a float angle resolve to the platform's sinf/cosf,
+// which are not correctly rounded everywhere (glibc 2.39: one ulp off on 1.3 % of
+// uniformly distributed angles), so the reference's primary directions depend on the libm
+// it was built against. The FP32 restatement therefore offers both: the libm's sinf/cosf
+// (g_libm_trig = 1, what a glibc build of the reference computes; used to pin against the
+// reference's own code) and, by default, sin and cos rounded once to float from a double
+// evaluation whose every step is a single IEEE rounding (x - k pi/2 by a two-part pi/2 with
+// fma, Taylor series to degree 15/16 by Horner's rule with fma), which any IEEE machine,
+// the GPU included, evaluates to the same bits.
+static int g_libm_trig = 0;
+
+static inline void sincos_once_rounded(float x, float &s, float &c) {
+    const double xd = double(x);
+    const double k = std::rint(xd * 0x1.45f306dc9c883p-1);
+    double r = std::fma(-k, 0x1.921fb54442d18p+0, xd);
+    r = std::fma(-k, 0x1.1a62633145c07p-54, r);
+    const double z = r * r;
+    // sin(r) = r + r z (-1/3! + z (1/5! - z (1/7! - ...))), cos(r) = 1 + z (-1/2! + z (1/4! - ...))
+    static const double S[7] = {-0x1.ae7f3e733b81fp-41, 0x1.6124613a86d09p-33, -0x1.ae64567f544e4p-26,
+                                0x1.71de3a556c734p-19, -0x1.a01a01a01a01ap-13, 0x1.1111111111111p-7,
+                                -0x1.5555555555555p-3};
+    static const double C[8] = {0x1.ae7f3e733b81fp-45, -0x1.93974a8c07c9dp-37, 0x1.1eed8eff8d898p-29,
+                                -0x1.27e4fb7789f5cp-22, 0x1.a01a01a01a01ap-16, -0x1.6c16c16c16c17p-10,
+                                0x1.5555555555555p-5, -0.5};
+    double ps = S[0];
+    for (int i = 1; i < 7; ++i) ps = std::fma(ps, z, S[i]);
+    double pc = C[0];
+    for (int i = 1; i < 8; ++i) pc = std::fma(pc, z, C[i]);
+    const double sr = std::fma(r * z, ps, r), cr = std::fma(z, pc, 1.0);
+    switch (int(k) & 3) {
+        case 0: s = float(sr); c = float(cr); break;
+        case 1: s = float(cr); c = float(-sr); break;
+        case 2: s = float(-sr); c = float(-cr); break;
+        default: s = float(-cr); c = float(sr); break;
+    }
+}
+
 template <typename R> static inline V3<R> uniform_sample_sphere(R u0, R u1) {
     R phi = R(2) * Consts<R>::Pi * u0;
     R y = R(2) * u1 - R(1);
     R r = std::sqrt(std::max(R(0), R(1) - y * y));
-    return {-r * std::sin(phi), y, -r * std::cos(phi)};
+    R sp = std::sin(phi), cp = std::cos(phi);
+    if (sizeof(R) == 4 && !g_libm_trig) {
+        float fs, fc;
+        sincos_once_rounded(float(phi), fs, fc);
+        sp = R(fs);
+        cp = R(fc);
+    }
+    return {-r * sp, y, -r * cp};
 }
 
 // AWRAngularDistribution::evaluate (emitter.h:126-136)
@@ -424,6 +468,7 @@ struct BNode {
 struct Bvh {
     std::vector<BNode> nodes;
     std::vector<int32_t> prims;  // triangle ids in leaf order
+    std::vector<float> tv;       // the vertices (v0, v1, v2) of prims[i] at 9 i: one fetch per test
 };
 
 struct Scene {
@@ -459,7 +504,7 @@ static void build_bvh(Scene &s) {
     std::vector<Task> stack;
     s.bvh.nodes.push_back(BNode{});
     stack.push_back({0, 0, int32_t(nt)});
-    const int kBins = 16;
+    const int kBins = 32;
     while (!stack.empty()) {
         Task tk = stack.back();
         stack.pop_back();
@@ -488,7 +533,7 @@ static void build_bvh(Scene &s) {
             s.bvh.nodes[tk.node] = nd;
             continue;
         }
-        // binned SAH over the widest centroid axis
+        // binned SAH (32 bins) over each axis with a centroid extent; the cheapest split wins
         int axis = 0;
         float ext = chi[0] - clo[0];
         for (int a = 1; a < 3; ++a)
@@ -497,70 +542,81 @@ static void build_bvh(Scene &s) {
                 axis = a;
             }
         int32_t mid = tk.first + tk.count / 2;
-        if (ext > 0.f) {
+        {
             struct Bin {
                 float lo[3], hi[3];
                 int n;
-            } bins[kBins];
-            for (auto &b : bins) {
-                for (int a = 0; a < 3; ++a) {
-                    b.lo[a] = std::numeric_limits<float>::infinity();
-                    b.hi[a] = -b.lo[a];
-                }
-                b.n = 0;
-            }
-            auto binOf = [&](int32_t p) {
-                int b = int((cen[3 * p + axis] - clo[axis]) / ext * kBins);
-                return std::min(std::max(b, 0), kBins - 1);
             };
-            for (int32_t i = tk.first; i < tk.first + tk.count; ++i) {
-                int32_t p = s.bvh.prims[i];
-                Bin &b = bins[binOf(p)];
-                b.n++;
-                for (int a = 0; a < 3; ++a) {
-                    b.lo[a] = std::min(b.lo[a], lo[3 * p + a]);
-                    b.hi[a] = std::max(b.hi[a], hi[3 * p + a]);
-                }
-            }
             auto area = [](const float *l, const float *h) {
                 float dx = h[0] - l[0], dy = h[1] - l[1], dz = h[2] - l[2];
                 if (dx < 0) return 0.f;
                 return dx * dy + dy * dz + dz * dx;
             };
             float best = std::numeric_limits<float>::infinity();
-            int bestSplit = -1;
-            for (int sp = 1; sp < kBins; ++sp) {
-                float L[3], H[3], L2[3], H2[3];
+            int bestSplit = -1, bestAxis = -1;
+            for (int ax = 0; ax < 3; ++ax) {
+                const float ex = chi[ax] - clo[ax];
+                if (!(ex > 0.f)) continue;
+                Bin bins[kBins];
+                for (auto &b : bins) {
+                    for (int a = 0; a < 3; ++a) {
+                        b.lo[a] = std::numeric_limits<float>::infinity();
+                        b.hi[a] = -b.lo[a];
+                    }
+                    b.n = 0;
+                }
+                for (int32_t i = tk.first; i < tk.first + tk.count; ++i) {
+                    int32_t p = s.bvh.prims[i];
+                    int bi = std::min(std::max(int((cen[3 * p + ax] - clo[ax]) / ex * kBins), 0), kBins - 1);
+                    Bin &b = bins[bi];
+                    b.n++;
+                    for (int a = 0; a < 3; ++a) {
+                        b.lo[a] = std::min(b.lo[a], lo[3 * p + a]);
+                        b.hi[a] = std::max(b.hi[a], hi[3 * p + a]);
+                    }
+                }
+                // suffix sweep for the right side, prefix for the left
+                float rlo[kBins][3], rhi[kBins][3];
+                int rn[kBins];
+                for (int b = kBins - 1; b >= 0; --b) {
+                    for (int a = 0; a < 3; ++a) {
+                        rlo[b][a] = b + 1 < kBins ? std::min(rlo[b + 1][a], bins[b].lo[a]) : bins[b].lo[a];
+                        rhi[b][a] = b + 1 < kBins ? std::max(rhi[b + 1][a], bins[b].hi[a]) : bins[b].hi[a];
+                    }
+                    rn[b] = (b + 1 < kBins ? rn[b + 1] : 0) + bins[b].n;
+                }
+                float L[3], H[3];
                 for (int a = 0; a < 3; ++a) {
-                    L[a] = L2[a] = std::numeric_limits<float>::infinity();
-                    H[a] = H2[a] = -L[a];
+                    L[a] = std::numeric_limits<float>::infinity();
+                    H[a] = -L[a];
                 }
-                int nl = 0, nr = 0;
-                for (int b = 0; b < sp; ++b) {
-                    nl += bins[b].n;
+                int nl = 0;
+                for (int sp = 1; sp < kBins; ++sp) {
+                    nl += bins[sp - 1].n;
                     for (int a = 0; a < 3; ++a) {
-                        L[a] = std::min(L[a], bins[b].lo[a]);
-                        H[a] = std::max(H[a], bins[b].hi[a]);
+                        L[a] = std::min(L[a], bins[sp - 1].lo[a]);
+                        H[a] = std::max(H[a], bins[sp - 1].hi[a]);
                     }
-                }
-                for (int b = sp; b < kBins; ++b) {
-                    nr += bins[b].n;
-                    for (int a = 0; a < 3; ++a) {
-                        L2[a] = std::min(L2[a], bins[b].lo[a]);
-                        H2[a] = std::max(H2[a], bins[b].hi[a]);
+                    const int nr = rn[sp];
+                    if (nl == 0 || nr == 0) continue;
+                    float c = area(L, H) * nl + area(rlo[sp], rhi[sp]) * nr;
+                    if (c < best) {
+                        best = c;
+                        bestSplit = sp;
+                        bestAxis = ax;
                     }
-                }
-                if (nl == 0 || nr == 0) continue;
-                float c = area(L, H) * nl + area(L2, H2) * nr;
-                if (c < best) {
-                    best = c;
-                    bestSplit = sp;
                 }
             }
             if (bestSplit > 0) {
-                auto it = std::partition(s.bvh.prims.begin() + tk.first, s.bvh.prims.begin() + tk.first + tk.count,
-                                         [&](int32_t p) { return binOf(p) < bestSplit; });
+                const int ax = bestAxis;
+                const float ex = chi[ax] - clo[ax];
+                auto it = std::partition(
+                    s.bvh.prims.begin() + tk.first, s.bvh.prims.begin() + tk.first + tk.count, [&](int32_t p) {
+                        return std::min(std::max(int((cen[3 * p + ax] - clo[ax]) / ex * kBins), 0), kBins - 1) <
+                               bestSplit;
+                    });
                 mid = int32_t(it - s.bvh.prims.begin());
+                axis = ax;
             }
         }
         if (mid <= tk.first || mid >= tk.first + tk.count) {
@@ -578,14 +634,16 @@ static void build_bvh(Scene &s) {
         stack.push_back({l, tk.first, mid - tk.first});
         stack.push_back({l + 1, mid, tk.first + tk.count - mid});
     }
+    s.bvh.tv.resize(size_t(9) * nt);
+    for (int64_t i = 0; i < nt; ++i)
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) s.bvh.tv[9 * i + 3 * k + a] = s.mesh.v[3 * s.mesh.f[3 * s.bvh.prims[i] + k] + a];
 }
 
 // Moller-Trumbore in precision R. Accepts tnear < t <= tfar.
 template <typename R>
-static inline bool tri_hit(const Mesh &m, int32_t prim, V3<R> o, V3<R> d, R tnear, R tfar, R &t_out) {
-    const float *v0f = &m.v[3 * m.f[3 * prim + 0]];
-    const float *v1f = &m.v[3 * m.f[3 * prim + 1]];
-    const float *v2f = &m.v[3 * m.f[3 * prim + 2]];
+static inline bool tri_hit(const float *vtx, V3<R> o, V3<R> d, R tnear, R tfar, R &t_out) {
+    const float *v0f = vtx, *v1f = vtx + 3, *v2f = vtx + 6;
     V3<R> v0{R(v0f[0]), R(v0f[1]), R(v0f[2])};
     V3<R> v1{R(v1f[0]), R(v1f[1]), R(v1f[2])};
     V3<R> v2{R(v2f[0]), R(v2f[1]), R(v2f[2])};
@@ -627,6 +685,17 @@ static inline bool box_hit(const BNode &n, V3<R> o, V3<R> inv, R tnear, R tfar) 
     return tmin <= tmax * R(1.0000004);
 }
 
+// entry distance of a box the ray reaches (box_hit's test), +inf for one it misses
+template <typename R>
+static inline R box_entry(const BNode &n, V3<R> o, V3<R> inv, R tnear, R tfar) {
+    R t0x = (R(n.lo[0]) - o.x) * inv.x, t1x = (R(n.hi[0]) - o.x) * inv.x;
+    R t0y = (R(n.lo[1]) - o.y) * inv.y, t1y = (R(n.hi[1]) - o.y) * inv.y;
+    R t0z = (R(n.lo[2]) - o.z) * inv.z, t1z = (R(n.hi[2]) - o.z) * inv.z;
+    R tmin = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)), std::fmax(std::fmin(t0z, t1z), tnear));
+    R tmax = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)), std::fmin(std::fmax(t0z, t1z), tfar));
+    return tmin <= tmax * R(1.0000004) ? tmin : std::numeric_limits<R>::infinity();
+}
+
 // closest hit; returns prim or -1
 template <typename R>
 static int32_t closest_hit(const Scene &s, V3<R> o, V3<R> d, R tnear, R tfar, R &t_best) {
@@ -644,7 +713,7 @@ static int32_t closest_hit(const Scene &s, V3<R> o, V3<R> d, R tnear, R tfar, R 
             for (int32_t i = n.left; i < n.left + n.count; ++i) {
                 int32_t p = s.bvh.prims[i];
                 R t;
-                if (tri_hit(s.mesh, p, o, d, tnear, tfar, t)) {
+                if (tri_hit(&s.bvh.tv[size_t(9) * i], o, d, tnear, tfar, t)) {
                     if (t < t_best || (t == t_best && (best < 0 || p < best))) {
                         t_best = t;
                         best = p;
@@ -652,8 +721,17 @@ static int32_t closest_hit(const Scene &s, V3<R> o, V3<R> d, R tnear, R tfar, R 
                 }
             }
         } else {
-            stack[sp++] = n.left + 1;
-            stack[sp++] = n.left;
+            // nearer child first (pops last): only the pruning order changes, every node
+            // is still re-tested against the current closest hit when it is popped
+            const R e0 = box_entry(s.bvh.nodes[n.left], o, inv, tnear, t_best);
+            const R e1 = box_entry(s.bvh.nodes[n.left + 1], o, inv, tnear, t_best);
+            if (e1 < e0) {
+                stack[sp++] = n.left;
+                stack[sp++] = n.left + 1;
+            } else {
+                stack[sp++] = n.left + 1;
+                stack[sp++] = n.left;
+            }
         }
     }
     return best;
@@ -671,7 +749,7 @@ template <typename R> static bool occluded(const Scene &s, V3<R> o, V3<R> d, R t
         if (n.count) {
             for (int32_t i = n.left; i < n.left + n.count; ++i) {
                 R t;
-                if (tri_hit(s.mesh, s.bvh.prims[i], o, d, tnear, tfar, t)) return true;
+                if (tri_hit(&s.bvh.tv[size_t(9) * i], o, d, tnear, tfar, t)) return true;
             }
         } else {
             stack[sp++] = n.left + 1;
@@ -808,6 +886,22 @@ template <typename R> static void frame_splat_exact(Frame<R> &f, double b, Cx<R>
 // ----------------------------------------------------------------------------------
 // Integrator + PathTracer::sample (path.h:235-451, integrator.h:107-168)
 // ----------------------------------------------------------------------------------
+// Integrator::measureRay (integrator.h:107-110): exp(j 2 pi (f0 - dt S / 2) dt), the
+// angle in R and its cos/sin through radar::polar (cexpj)
+template <typename R> static inline Cx<R> measure_ray(R dt, R startFreq, R freqSlope) {
+    R angle = R(2) * Consts<R>::Pi * (startFreq - dt * freqSlope / R(2)) * dt;
+    return cexpj(angle);
+}
+
+// PIndex::setTime (radar.h:232-241): the fractional range bin N frac(dt S / adcRate);
+// a CW configuration (slope 0) puts everything in bin 0
+template <typename R> static inline R set_time_sample(R delta_t, R freqSlope, R adcRate, int samples) {
+    if (freqSlope == R(0)) return R(0);
+    R delta_f = delta_t * freqSlope;
+    R x = delta_f / adcRate;
+    return R(samples) * (x - std::floor(x));
+}
+
 template <typename R> struct Rf {
     R startFreq, freqSlope, adcRate, idleTime, rampTime, antennaDelay;
     R bandwidth() const { return freqSlope * rampTime; }
@@ -835,11 +929,7 @@ template <typename R> struct Tracer {
     oracle_record *records = nullptr;  // optional per-sample event log
     int maxRecords = 0;
 
-    // Integrator::measureRay (integrator.h:107-110)
-    Cx<R> measureRay(R dt) const {
-        R angle = R(2) * Consts<R>::Pi * (rf.startFreq - dt * rf.freqSlope / R(2)) * dt;
-        return cexpj(angle);
-    }
+    Cx<R> measureRay(R dt) const { return measure_ray(dt, rf.startFreq, rf.freqSlope); }
 
     // Integrator::splat (integrator.h:113-148) without the debug image
     void splat(int channel, R delta_t, R dphase, Cx<R> measurement, R weight, oracle_record *rec) {
@@ -847,14 +937,7 @@ template <typename R> struct Tracer {
             if (weight == R(0) || (measurement.re == R(0) || measurement.im == R(0))) return;
         }
         delta_t += rf.antennaDelay;
-        R sample;
-        if (rf.freqSlope == R(0)) {
-            sample = 0;
-        } else {
-            R delta_f = delta_t * rf.freqSlope;
-            R x = delta_f / rf.adcRate;
-            sample = R(frame.samples) * (x - std::floor(x));
-        }
+        R sample = set_time_sample(delta_t, rf.freqSlope, rf.adcRate, frame.samples);
         R delta_p = R(2) * rf.startFreq * R(0) / Consts<R>::SpeedOfLight;
         R y = delta_p / rf.chirpFrequency();
         R chirp = R(frame.chirps) * (y - std::floor(y));
@@ -1262,11 +1345,24 @@ void oracle_uniform_sample_sphere(float u0, float u1, float *d) {
 }
 
 void oracle_measure_ray(float dt, float startFreq, float freqSlope, float *out2) {
-    float angle = 2.f * Consts<float>::Pi * (startFreq - dt * freqSlope / 2.f) * dt;
+    Cx<float> c = measure_ray(dt, startFreq, freqSlope);
+    out2[0] = c.re;
+    out2[1] = c.im;
+}
+
+float oracle_set_time(float delta_t, float freqSlope, float adcRate, int samples) {
+    return set_time_sample(delta_t, freqSlope, adcRate, samples);
+}
+
+void oracle_cexp(float angle, float *out2) {
     Cx<float> c = cexpj(angle);
     out2[0] = c.re;
     out2[1] = c.im;
 }
+
+void oracle_set_libm_trig(int on) { g_libm_trig = on ? 1 : 0; }
+
+void oracle_sincos_rounded(float x, float *s, float *c) { sincos_once_rounded(x, *s, *c); }
 
 int64_t oracle_bvh_nodes(void *sp) { return int64_t(static_cast<Scene *>(sp)->bvh.nodes.size()); }
 

@@ -81,6 +81,15 @@ void oracle_frame_splat(int chirps, int samples, int channels, float ic, float i
 void oracle_awr_evaluate(const float *d, float *H6);
 void oracle_uniform_sample_sphere(float u0, float u1, float *d);
 void oracle_measure_ray(float dt, float startFreq, float freqSlope, float *out2);
+/* PIndex::setTime's fractional bin for a delay that already includes antennaDelay. */
+/* std::exp(Complex(0, angle)) as radar::polar forms it (cos/sin of the widened angle). */
+void oracle_cexp(float angle, float *out2);
+float oracle_set_time(float delta_t, float freqSlope, float adcRate, int samples);
+/* 1: primary directions from the libm's sinf/cosf (a glibc build of the reference);
+ * 0 (default): sin/cos rounded once to float, what the GPU computes. Not thread-safe:
+ * set it before a simulation starts. */
+void oracle_set_libm_trig(int on);
+void oracle_sincos_rounded(float x, float *s, float *c);
 
 #ifdef __cplusplus
 }

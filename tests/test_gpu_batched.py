@@ -16,9 +16,12 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+ORACLE_CAP = 1 << 16  # per-pose budget the oracle traces (the bottom of the 2^16..2^22 range)
+
+
 @pytest.fixture(scope="module")
 def boxes(product_lib, oracle_lib):
-    w = scenes.boxes_workload(poses=96, min_log2=12, max_log2=15)
+    w = scenes.boxes_workload(poses=96)
     be = gb300.Backend(w.mesh, None)
     return w, be, oracle_lib.Scene(w.mesh)
 
@@ -38,23 +41,25 @@ def test_million_triangle_bvh(boxes):
 
 
 def test_batch_matches_oracle_per_pose(boxes):
-    """Per pose against the oracle. This scene is ill-conditioned in FP32: sensors sit at
-    up to 50 m from the origin (4 um float spacing) among walls millimetres apart, so a
-    one-ulp difference in a primary direction (CUDA's sincosf vs glibc's sinf/cosf) moves
-    short segments by a measurable fraction and with them the PO amplitudes; per-sample
-    event structure stays identical. Compared at 1e-3 relative L2 instead of 1e-4."""
+    """Every one of 96 poses of the batched configuration (log-uniform budgets
+    2^16..2^22, capped at 2^16 so the CPU oracle finishes), traced in one launch, against
+    the oracle at 1e-4 relative L2 of the IF signal. Sensors stand up to 70 m from the
+    origin among walls millimetres apart, so the rows are only this close because the
+    primary directions are bit-identical on both sides (sin/cos rounded once to float)."""
     w, be, ora = boxes
     t = tracer(w)
-    rows = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, w.budget)
-    checked = 0
-    for k in range(0, len(w.tx), 8):
-        ref = ora.fetch_row(w.rf, 256, w.tx[k], w.rx[k], t, int(w.budget[k]))
+    budget = np.minimum(w.budget, ORACLE_CAP)
+    rows = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, budget)
+    errs = []
+    for k in range(len(w.tx)):
+        ref = ora.fetch_row(w.rf, 256, w.tx[k], w.rx[k], t, int(budget[k]))
         if np.linalg.norm(ref) == 0:
-            assert np.linalg.norm(rows[k]) == 0
+            assert np.linalg.norm(rows[k]) == 0, k
             continue
-        assert rel_l2(rows[k], ref) <= 1e-3, k
-        checked += 1
-    assert checked >= 8
+        errs.append(rel_l2(rows[k], ref))
+    print("boxes: %d poses, max rel L2 %.2e, median %.2e" % (len(errs), max(errs), float(np.median(errs))))
+    assert len(errs) >= 90
+    assert max(errs) <= 1e-4, (max(errs), int(np.argmax(errs)))
 
 
 def test_batch_rows_independent_of_batch_composition(boxes):

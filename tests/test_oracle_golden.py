@@ -34,24 +34,68 @@ def test_frame_splat_matches_reference(oracle_lib):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (k, cases[k])
 
 
-def test_settime_and_cexp_match_reference(oracle_lib):
+def test_settime_matches_reference_bit_exact(oracle_lib):
+    """The oracle's PIndex::setTime (the function its splat uses) against the reference's
+    own setTime on 4000 delays x 3 RF configurations: identical bits."""
     import ctypes
     g = np.load(os.path.join(GOLD, "settime_ref.npz"))
     L = oracle_lib.lib()
-    # setTime is a float expression: sample = N * frac(dt * S / adc)
+    L.oracle_set_time.restype = ctypes.c_float
+    L.oracle_set_time.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int]
     for j, (f0, sl, ad, n) in enumerate(g["cfg"]):
-        dt = g["dt"]
-        x = (dt * np.float32(sl)) / np.float32(ad)
-        got = np.float32(n) * (x - np.floor(x))
-        assert np.array_equal(got.astype(np.float32).view(np.uint32), g["sample"][j].view(np.uint32))
+        got = np.array([L.oracle_set_time(float(dt), float(sl), float(ad), int(n)) for dt in g["dt"]], np.float32)
+        assert np.array_equal(got.view(np.uint32), g["sample"][j].view(np.uint32)), j
+
+
+def test_cexp_matches_reference_bit_exact(oracle_lib):
+    """The oracle's exp(j angle) (radar::polar, the function its measureRay uses) against the
+    reference's std::exp(Complex(0, angle)) on 4000 angles up to 7e4 rad: identical bits."""
+    import ctypes
     c = np.load(os.path.join(GOLD, "cexp_ref.npz"))
-    out = np.zeros(2, np.float32)
+    L = oracle_lib.lib()
     fp = ctypes.POINTER(ctypes.c_float)
-    for a, want in zip(c["angle"][::7], c["value"][::7]):
-        # measureRay with f0 chosen so the angle is exactly `a`: use the double cos/sin path
-        got = np.array([np.cos(np.float64(a)), np.sin(np.float64(a))], np.float32)
-        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
-    L.oracle_measure_ray(np.float32(1e-9), np.float32(77e9), np.float32(78.125e12), out.ctypes.data_as(fp))
-    ang = np.float32(2) * np.float32(np.pi) * (np.float32(77e9) - np.float32(1e-9) * np.float32(78.125e12) /
-                                               np.float32(2)) * np.float32(1e-9)
-    assert np.allclose(out, [np.cos(np.float64(ang)), np.sin(np.float64(ang))], atol=0)
+    L.oracle_cexp.argtypes = [ctypes.c_float, fp]
+    out = np.zeros(2, np.float32)
+    got = np.zeros((len(c["angle"]), 2), np.float32)
+    for i, a in enumerate(c["angle"]):
+        L.oracle_cexp(float(a), out.ctypes.data_as(fp))
+        got[i] = out
+    assert np.array_equal(got.view(np.uint32), c["value"].view(np.uint32))
+
+
+def test_measure_ray_is_cexp_of_the_float_angle(oracle_lib):
+    """measureRay forms its angle in float in the reference's order, then exp(j angle)."""
+    import ctypes
+    L = oracle_lib.lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.oracle_measure_ray.argtypes = [ctypes.c_float] * 3 + [fp]
+    L.oracle_cexp.argtypes = [ctypes.c_float, fp]
+    rng = np.random.default_rng(3)
+    a, b = np.zeros(2, np.float32), np.zeros(2, np.float32)
+    f32 = np.float32
+    for dt in rng.uniform(0, 2.5e-7, 500).astype(np.float32):
+        L.oracle_measure_ray(float(dt), 77e9, 78.125e12, a.ctypes.data_as(fp))
+        ang = f32(2) * f32(np.pi) * (f32(77e9) - dt * f32(78.125e12) / f32(2)) * dt
+        L.oracle_cexp(float(ang), b.ctypes.data_as(fp))
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_rounded_sincos_is_correctly_rounded(oracle_lib):
+    """The primary direction's sin/cos (what the GPU computes): the correctly rounded float
+    values, checked against sin/cos in double rounded to float, on every angle 2 pi u of a
+    2^20-point grid of u and on random angles in [0, 2 pi)."""
+    import ctypes
+    L = oracle_lib.lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.oracle_sincos_rounded.argtypes = [ctypes.c_float, fp, fp]
+    f32 = np.float32
+    u = np.arange(0, 1 << 20, 7, dtype=np.float64) / (1 << 20)
+    x = np.concatenate([f32(2) * f32(np.pi) * u.astype(np.float32),
+                        np.random.default_rng(1).uniform(0, 2 * np.pi, 20000).astype(np.float32)])
+    s, c = np.zeros(1, np.float32), np.zeros(1, np.float32)
+    got = np.zeros((len(x), 2), np.float32)
+    for i, v in enumerate(x):
+        L.oracle_sincos_rounded(float(v), s.ctypes.data_as(fp), c.ctypes.data_as(fp))
+        got[i] = s[0], c[0]
+    want = np.stack([np.sin(x.astype(np.float64)), np.cos(x.astype(np.float64))], 1).astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

@@ -24,7 +24,14 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def test_no_alloc_matches_allocating_entry_point(product_lib):
+@pytest.mark.parametrize("go", [1, 0], ids=["wavefront-GO", "per-thread-nonGO"])
+@pytest.mark.parametrize("phase", ["reference_fp32", "split_fp64"])
+def test_no_alloc_matches_allocating_entry_point(product_lib, phase, go):
+    """Two allocation-free calls in a row against the allocating entry point on the same
+    device inputs (uneven budgets), in both phase modes, on the wavefront kernel (GO mode)
+    and the one-thread-per-sample kernel (non-GO mode). The second call allocates nothing
+    (the library's allocation count and the device's free memory stay put) and the
+    allocation-free status query reports a clean run."""
     torch = pytest.importorskip("torch")
     from hussar_gb300 import PathTracer, _lib, gb300, scenes
 
@@ -34,9 +41,11 @@ def test_no_alloc_matches_allocating_entry_point(product_lib):
     t = PathTracer()
     t.doGuiding = False
     t.maxDepth = w.max_depth
+    t.useGeometricalOptics = bool(go)
     be = gb300.Backend(w.mesh, None)
     dev = torch.device("cuda")
     stream = torch.cuda.current_stream(dev)
+    mode = getattr(_lib, "HSR_PHASE_" + phase.upper())
 
     def to_dev(arr):
         return torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
@@ -44,23 +53,37 @@ def test_no_alloc_matches_allocating_entry_point(product_lib):
     d_tx = to_dev((_lib.AntennaC * P)(*[a.to_c() for a in w.tx]))
     d_rx = to_dev((_lib.AntennaC * P)(*[a.to_c() for a in w.rx]))
     budget = np.array([(1 << 16) - 37 * k for k in range(P)], np.int64)  # uneven budgets
+    if not go:
+        budget //= 8  # the non-GO estimator traces random directions: fewer samples suffice
     d_budget = torch.from_numpy(budget).to(dev)
     d_offset = torch.zeros(P, dtype=torch.int64, device=dev)
     rf, fl = w.rf.to_c(), t.flags_c()
     ptr = lambda x: ctypes.c_void_p(x.data_ptr())
+    sp = ctypes.c_void_p(stream.cuda_stream)
 
     d_ref = torch.zeros(2 * P * N, dtype=torch.float32, device=dev)
     _lib.check(L.hsr_simulate_batch_device(be.handle, ctypes.byref(rf), N, ctypes.byref(fl), P, ptr(d_tx),
-                                           ptr(d_rx), ptr(d_budget), ptr(d_offset), _lib.HSR_PHASE_REFERENCE_FP32,
-                                           _lib.HSR_SPLAT_DIRICHLET16, ptr(d_ref), ctypes.c_void_p(stream.cuda_stream)))
-    outs = []
-    for _ in range(2):
-        d_out = torch.full((2 * P * N,), float("nan"), dtype=torch.float32, device=dev)
+                                           ptr(d_rx), ptr(d_budget), ptr(d_offset), mode,
+                                           _lib.HSR_SPLAT_DIRICHLET16, ptr(d_ref), sp))
+    bits = ctypes.c_uint32(7)
+    _lib.check(L.hsr_scene_status(be.handle, sp, ctypes.byref(bits)))
+    assert bits.value == 0
+    outs = [torch.full((2 * P * N,), float("nan"), dtype=torch.float32, device=dev) for _ in range(2)]
+    torch.cuda.synchronize()
+    allocs, free = [], []
+    for d_out in outs:
+        allocs.append(L.hsr_debug_alloc_count())
+        free.append(torch.cuda.mem_get_info()[0])
         _lib.check(L.hsr_simulate_batch_device_noalloc(
             be.handle, ctypes.byref(rf), N, ctypes.byref(fl), P, ptr(d_tx), ptr(d_rx), ptr(d_budget), ptr(d_offset),
-            _lib.HSR_PHASE_REFERENCE_FP32, ptr(d_out), ctypes.c_void_p(stream.cuda_stream)))
-        outs.append(d_out)
+            mode, ptr(d_out), sp))
+        bits = ctypes.c_uint32(7)
+        _lib.check(L.hsr_noalloc_status(sp, ctypes.byref(bits)))
+        assert bits.value == 0
     torch.cuda.synchronize()
+    # the second call (the first may look the array's address up) allocates nothing
+    assert L.hsr_debug_alloc_count() == allocs[1]
+    assert torch.cuda.mem_get_info()[0] == free[1]
     ref = d_ref.cpu().numpy().view(np.complex64).reshape(P, N)
     assert np.linalg.norm(ref) > 0
     for d_out in outs:
