@@ -458,15 +458,18 @@ def run_batched(args, rank, world, local_rank, dist):
 
     torch.cuda.set_device(local_rank)
     L = _lib.lib()
-    w, desc = load_workload("boxes")
+    w, desc = load_workload("boxes", args.poses)
+    if args.max_log2:  # profiling cases: budgets capped (say so in the line's config)
+        w.budget = np.minimum(w.budget, 1 << args.max_log2)
+        desc += ", budgets capped at 2^%d" % args.max_log2
     t = PathTracer()
     t.doGuiding = False
     t.maxDepth = w.max_depth
     be = gb300.Backend(w.mesh, None)
     dev = torch.device("cuda", local_rank)
     stream = torch.cuda.current_stream(dev)
-    B = DeviceBatch(w, dev, rank, torch, _lib)  # all 4096 poses resident
-    N, Q = B.N, BOXES_BATCH
+    B = DeviceBatch(w, dev, rank, torch, _lib)  # every pose resident
+    N, Q = B.N, min(BOXES_BATCH, B.P)
     nb = B.P // Q
     ant = ctypes.sizeof(_lib.AntennaC)
     # the graph's input slots (one batch) and its output rows
@@ -1150,6 +1153,8 @@ def main():
     ap.add_argument("--workload", default="boxes",
                     choices=["boxes", "sphere", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
+    ap.add_argument("--max-log2", type=int, default=None,
+                    help="boxes workload: cap every budget at 2^k (small profiling cases only)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per trace launch from an ncu capture of the same workload (reported as-is)")
     ap.add_argument("--kernel-only", action="store_true",

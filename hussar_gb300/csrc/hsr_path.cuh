@@ -114,6 +114,13 @@ template <int kBase> __device__ __forceinline__ float radical_inverse(uint64_t v
     return fminf(__ull2float_rn(reversed) * invBaseN, ome);
 }
 
+// HaltonSampler::get2D (halton.h:23-26) is Vector2f(get1D(), get1D()): C++ leaves the order
+// of the two calls unspecified and GCC evaluates the second argument first, so a GCC build
+// of the reference draws (dimension d + 1, dimension d) for the pair that starts at d.
+// The pairs here follow that build: primary = (halton(i, 2), halton(i, 1)).
+constexpr int kGet2DFirst = 1;   // dimension offset of the pair's first component
+constexpr int kGet2DSecond = 0;  // and of its second
+
 // HaltonSampler::get1D dimension table (halton.h:56-67; dims >= 10 return 0, :1082-1084)
 __device__ __forceinline__ float halton(uint64_t index, int dim) {
     switch (dim) {
@@ -169,8 +176,12 @@ template <bool kExact = true> __device__ __forceinline__ f3 uniform_sample_spher
 // H = (0,1,0) x d scaled by 2.622/(cos_h-1.8)^6 and 0.625/(cos_e-1.5)^4. The reference
 // forms the two scale factors in double; here they are single precision (a few ulps).
 __device__ __forceinline__ c3 awr_eval(f3 d) {
-    float cos_h = sqrtf(1.f - d.x * d.x);
-    float cos_e = sqrtf(1.f - d.y * d.y);
+    // 1 - d.x^2 can round below zero for a direction within ~1e-4 rad of the antenna's x
+    // (or y) axis (a receiver's rotation and the unit direction each carry rounding), where
+    // the reference takes the square root of a negative number and its frame turns NaN;
+    // the argument is clamped at zero (a deliberate deviation, only on those directions)
+    float cos_h = sqrtf(fmaxf(1.f - d.x * d.x, 0.f));
+    float cos_e = sqrtf(fmaxf(1.f - d.y * d.y, 0.f));
     float a = cos_h - 1.8f;
     float a2 = a * a;
     float s1 = 2.622f / (a2 * a2 * a2);

@@ -59,8 +59,9 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
     while (true) {
         const f3 tmpd = d;
         if (depth == 0) {
-            px = halton(hindex, dim++);
-            py = halton(hindex, dim++);
+            px = halton(hindex, dim + kGet2DFirst);  // get2D (GCC order, hsr_path.cuh)
+            py = halton(hindex, dim + kGet2DSecond);
+            dim += 2;
             if (fl.doGuiding) primaryPdf = guide_sample(pc.samp_child, pc.samp_p, px, py);
             if (kFF) {
                 ff_sample(ftx, px, py, o, d, H);
@@ -70,8 +71,9 @@ __device__ void trace_sample(const TraceParams &p, const PoseCtx &pc, uint64_t h
             }
             H = c3_scl(H, 1.f / primaryPdf);
         } else if (!fl.useGeometricalOptics) {
-            float u0 = halton(hindex, dim++);
-            float u1 = halton(hindex, dim++);
+            const float u0 = halton(hindex, dim + kGet2DFirst);
+            const float u1 = halton(hindex, dim + kGet2DSecond);
+            dim += 2;
             d = uniform_sample_sphere<kPhase == HSR_PHASE_REFERENCE_FP32>(u0, u1);
             H = surface_eval(hit_n, inc_H, d);
         } else {

@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             if (s < gen_end) {
                 const uint64_t hindex = uint64_t(pc.offset + s);
                 const float freq = rf.startFreq + halton(hindex, 0) * HSR_BANDWIDTH;
-                Guided g{halton(hindex, 1), halton(hindex, 2), 1.f, cf{0.f, 0.f}};
+                Guided g{halton(hindex, 1 + kGet2DFirst), halton(hindex, 1 + kGet2DSecond), 1.f, cf{0.f, 0.f}};
                 if (fl.doGuiding) g.pdf = guide_sample(pc.samp_child, pc.samp_p, g.x0, g.x1);
                 f3 o, d;
                 c3 H;

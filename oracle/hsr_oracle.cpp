@@ -249,6 +249,13 @@ template <typename R> struct Halton {
         R u = radical_inverse<R>(index, dim++);
         return float_samples ? R(float(radical_inverse<float>(index, unsigned(dim - 1)))) : u;
     }
+    // HaltonSampler::get2D (halton.h:23-26) returns Vector2f(get1D(), get1D()); C++ leaves
+    // the order of the two calls unspecified, and GCC evaluates the second argument first,
+    // so a GCC build of the reference gets (next dimension + 1, next dimension).
+    void get2D(R &u0, R &u1) {
+        u1 = get1D();
+        u0 = get1D();
+    }
 };
 
 // ----------------------------------------------------------------------------------
@@ -312,8 +319,10 @@ template <typename R> static inline CV3<R> awr_evaluate(V3<R> d) {
     H.c[0] = {R(1) * d.z - R(0) * d.y, -(R(0) * d.z - R(0) * d.y)};
     H.c[1] = {R(0) * d.x - R(0) * d.z, -(R(0) * d.x - R(0) * d.z)};
     H.c[2] = {R(0) * d.y - R(1) * d.x, -(R(0) * d.y - R(0) * d.x)};
-    R cos_h = std::sqrt(R(1) - d.x * d.x);
-    R cos_e = std::sqrt(R(1) - d.y * d.y);
+    // clamped at zero where 1 - d.x^2 rounds negative (the reference's sqrt would give NaN
+    // and a NaN frame): a deliberate deviation, on directions within ~1e-4 rad of an axis
+    R cos_h = std::sqrt(std::max(R(1) - d.x * d.x, R(0)));
+    R cos_e = std::sqrt(std::max(R(1) - d.y * d.y, R(0)));
     // 2.622 / pow(double, 6) is evaluated in double and converted to the scalar type
     R s1 = R(2.622 / std::pow(double(cos_h) - 1.8, 6));
     R s2 = R(0.625 / std::pow(double(cos_e) - 1.5, 4));
@@ -983,8 +992,8 @@ template <typename R> struct Tracer {
         while (true) {
             V3<R> tmpd = ray.d;
             if (ray.depth == 0) {
-                R u0 = sampler.get1D();
-                R u1 = sampler.get1D();
+                R u0, u1;
+                sampler.get2D(u0, u1);
                 if (farField)
                     ff_sample(ftx, u0, u1, ray);
                 else
@@ -992,8 +1001,8 @@ template <typename R> struct Tracer {
                 ray.H = cv3_scale(ray.H, R(1) / primaryPdf);
             } else {
                 if (!fl.useGO) {
-                    R u0 = sampler.get1D();
-                    R u1 = sampler.get1D();
+                    R u0, u1;
+                    sampler.get2D(u0, u1);
                     surface_sample(incoming, u0, u1, ray);
                 } else {
                     reflectRay(ray, isect);

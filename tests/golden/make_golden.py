@@ -9,7 +9,17 @@ place) and records their outputs for seeded inputs:
   settime_ref.npz  PIndex::setTime                               (radar.h:232-241)
   cexp_ref.npz     std::exp(Complex(0, angle)) via radar::polar   (complex.h:184-187,249-251)
 
-Usage: python tests/golden/make_golden.py
+and, from oracle/_ref/libhsr_refpath.so (the reference's PathTracer::run and
+PathTracer::sample with its emitters, geometry, integrator and frame, over stand-ins
+for the absent Eigen, libguiding and Embree; oracle/ref_path.cpp):
+
+  path_ref.npz     raw frame sums and total weight of PathTracer::run (doGuiding =
+                   false) on the dihedral, a small sphere above ground and a small boxes
+                   scene, across the tracer flags (path.h:153-169); the meshes are stored
+  sample_ref.npz   UniformSampleSphere (sampling.h:38-43), Integrator::measureRay
+                   (integrator.h:107-110) and HaltonSampler::get2D (halton.h:23-26)
+
+Usage: HUSSAR_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 import ctypes
 import os
@@ -91,7 +101,111 @@ def main():
         ref.ref_cexp(float(a), tmp.ctypes.data_as(fp))
         ce[i] = tmp
     np.savez_compressed(os.path.join(HERE, "cexp_ref.npz"), angle=ang, value=ce)
+    path_fixtures(rng)
     print("golden fixtures written to", HERE)
+
+
+def path_fixtures(rng):
+    import sys
+    sys.path.insert(0, ROOT)
+    from hussar_gb300 import PathTracer, _lib, scenes
+    from hussar_gb300.core import NFAntenna, TriangleMesh
+
+    R = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libhsr_refpath.so"))
+    fp = ctypes.POINTER(ctypes.c_float)
+    vp = ctypes.c_void_p
+    R.ref_path_frame.argtypes = [vp, ctypes.c_int64, vp, ctypes.c_int64, vp, vp, vp, vp, vp, ctypes.c_int64, vp,
+                                 ctypes.POINTER(ctypes.c_double)]
+    R.ref_uniform_sample_sphere.argtypes = [ctypes.c_float, ctypes.c_float, fp]
+    R.ref_measure_ray.argtypes = [ctypes.c_float] * 3 + [fp]
+    R.ref_halton_get2d.argtypes = [ctypes.c_uint64, ctypes.c_int, fp]
+
+    dih = scenes.dihedral_workload()
+    sph = scenes.sphere_ground_workload(level=3)
+    box_mesh = scenes.boxes_mesh(seed=5, count=400, extent=30.0)
+    one = TriangleMesh()
+    one.append(np.array([[0, -0.2, -0.2], [0, 0.3, -0.2], [0, 0.0, 0.4]], np.float32), [[0, 1, 2]])
+    meshes = [dih.mesh, sph.mesh, box_mesh, one]
+    rf_sph = sph.rf
+    rf_dih = dih.rf
+    box_pose = NFAntenna(np.array([2.0, 1.0, -3.0], np.float32), scenes.looking(0.7))
+    a1 = NFAntenna([1.0, 0.05, 0.3], scenes.looking(0.3))
+    a2 = NFAntenna([1.0, 0.05, 0.35], scenes.looking(0.3))
+    cw = scenes.RFConfig(startFreq=78e9, freqSlope=0.0, adcRate=5e6, idleTime=1e-4, rampTime=5e-5)
+
+    def tr(depth, **kw):
+        t = PathTracer()
+        t.doGuiding = False
+        t.maxDepth = depth
+        for k, v in kw.items():
+            setattr(t, k, v)
+        return t
+
+    # (mesh, rf, N, tx, rx, tracer, budget)
+    cases = [
+        (0, rf_dih, 256, dih.tx[45], dih.rx[45], tr(2), 1 << 14),
+        (0, rf_dih, 256, dih.tx[10], dih.rx[10], tr(2), 1 << 13),
+        (0, rf_dih, 256, dih.tx[20], dih.rx[22], tr(2, onlyIndirect=False), 1 << 13),
+        (0, rf_dih, 256, dih.tx[60], dih.rx[60], tr(2, useGeometricalOptics=False), 1 << 12),
+        (0, rf_dih, 200, dih.tx[45], dih.rx[45], tr(2), 1 << 12),
+        (0, rf_dih, 256, dih.tx[30], dih.rx[30], tr(2, produceDebugImage=True), 1 << 12),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3), 1 << 13),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3, doFiltering=False), 1 << 12),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3, filteringSphere=False), 1 << 12),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3, correctPhase=True), 1 << 12),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3, poDiffraction=True), 1 << 12),
+        (1, rf_sph, 512, sph.tx[0], sph.rx[0], tr(3, useGeometricalOptics=False), 1 << 12),
+        (2, rf_dih, 256, box_pose, box_pose, tr(4), 1 << 12),
+        (3, rf_dih, 256, a1, a1, tr(3), 1 << 13),
+        (3, rf_dih, 256, a1, a2, tr(3, onlyIndirect=False), 1 << 12),
+        (3, cw, 1, a1, a1, tr(3), 1 << 12),
+    ]
+    rows, out_frames, weights, offs = [], [], [], [0]
+    for mi, rf, N, tx, rx, t, budget in cases:
+        m = meshes[mi]
+        v = np.ascontiguousarray(m.vertexBuffer, np.float32)
+        f = np.ascontiguousarray(m.indexBuffer, np.int32)
+        rfc, fcc = rf.to_c(), _lib.FrameConfigC(1, N, 1)
+        txc, rxc, flc = tx.to_c(), rx.to_c(), t.flags_c()
+        fr = np.zeros(2 * N, np.float32)
+        w = ctypes.c_double()
+        rc = R.ref_path_frame(v.ctypes.data, len(v), f.ctypes.data, len(f), ctypes.addressof(rfc),
+                              ctypes.addressof(fcc), ctypes.addressof(txc), ctypes.addressof(rxc),
+                              ctypes.addressof(flc), int(budget), fr.ctypes.data, ctypes.byref(w))
+        assert rc == 0
+        rows.append(np.concatenate([[mi, N, budget], np.frombuffer(bytes(rfc), np.float32),
+                                    np.frombuffer(bytes(txc), np.float32), np.frombuffer(bytes(rxc), np.float32),
+                                    np.frombuffer(bytes(flc), np.uint8).view(np.int32).astype(np.float64)]))
+        out_frames.append(fr)
+        weights.append(w.value)
+        offs.append(offs[-1] + len(fr))
+    mesh_arrays = {}
+    for i, m in enumerate(meshes):
+        mesh_arrays["mesh%d_v" % i] = np.ascontiguousarray(m.vertexBuffer, np.float32)
+        mesh_arrays["mesh%d_f" % i] = np.ascontiguousarray(m.indexBuffer, np.int32)
+    np.savez_compressed(os.path.join(HERE, "path_ref.npz"), cases=np.array(rows, np.float64),
+                        frames=np.concatenate(out_frames), offsets=np.array(offs, np.int64),
+                        weights=np.array(weights, np.float64), **mesh_arrays)
+
+    # primary direction, de-chirp phase and the get2D pair order
+    u = rng.random((4000, 2)).astype(np.float32)
+    d = np.zeros((len(u), 3), np.float32)
+    tmp = np.zeros(3, np.float32)
+    for i, (a, b) in enumerate(u):
+        R.ref_uniform_sample_sphere(float(a), float(b), tmp.ctypes.data_as(fp))
+        d[i] = tmp
+    dts = rng.uniform(0, 2.5e-7, 2000).astype(np.float32)
+    mr = np.zeros((len(dts), 2), np.float32)
+    for i, dt in enumerate(dts):
+        R.ref_measure_ray(float(dt), 77e9, 78.125e12, tmp.ctypes.data_as(fp))
+        mr[i] = tmp[:2]
+    idx = rng.integers(0, 2**40, 500).astype(np.uint64)
+    g2 = np.zeros((len(idx), 2), np.float32)
+    for i, k in enumerate(idx):
+        R.ref_halton_get2d(int(k), 1, tmp.ctypes.data_as(fp))
+        g2[i] = tmp[:2]
+    np.savez_compressed(os.path.join(HERE, "sample_ref.npz"), u=u, dir=d, dt=dts, measure=mr, get2d_index=idx,
+                        get2d=g2)
 
 
 if __name__ == "__main__":

@@ -99,3 +99,80 @@ def test_rounded_sincos_is_correctly_rounded(oracle_lib):
         got[i] = s[0], c[0]
     want = np.stack([np.sin(x.astype(np.float64)), np.cos(x.astype(np.float64))], 1).astype(np.float32)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_path_frames_match_reference_bit_exact(oracle_lib):
+    """The restatement's PathTracer::run (FP32, one thread, the platform's sinf/cosf in the
+    primary direction as a GCC build of the reference uses) against the reference's own
+    PathTracer::run compiled from its sources (oracle/ref_path.cpp over stand-ins for
+    Eigen, libguiding and Embree; tests/golden/make_golden.py): identical raw frame sums,
+    bit for bit, and identical total weights, on the dihedral, a sphere above ground and a
+    boxes scene, over the tracer flags and edge cases (direct path, non-GO sampling,
+    non-power-of-two N, debug-image early-out, CW chirp)."""
+    import ctypes
+    g = np.load(os.path.join(GOLD, "path_ref.npz"))
+    L = oracle_lib.lib()
+    scenes_ = {}
+    L.oracle_set_libm_trig(1)
+    try:
+        for k, row in enumerate(g["cases"]):
+            mi, N, budget = int(row[0]), int(row[1]), int(row[2])
+            rf = row[3:9].astype(np.float32)
+            tx = row[9:21].astype(np.float32)
+            rx = row[21:33].astype(np.float32)
+            fl = row[33:47].astype(np.int64).astype(np.int32)
+            if mi not in scenes_:
+                v, f = g["mesh%d_v" % mi], g["mesh%d_f" % mi]
+                scenes_[mi] = L.oracle_scene_create(v.ctypes.data_as(ctypes.c_void_p), len(v),
+                                                    f.ctypes.data_as(ctypes.c_void_p), len(f))
+                assert scenes_[mi]
+            fc = np.array([1, N, 1], np.int32)
+            out = np.zeros(2 * N, np.float64)
+            w = ctypes.c_double(0.0)
+            P = oracle_lib
+            rc = L.oracle_simulate(ctypes.c_void_p(scenes_[mi]), ctypes.byref(P.RF.from_buffer_copy(rf.tobytes())),
+                                   ctypes.byref(P.FC.from_buffer_copy(fc.tobytes())),
+                                   ctypes.byref(P.ANT.from_buffer_copy(tx.tobytes())),
+                                   ctypes.byref(P.ANT.from_buffer_copy(rx.tobytes())),
+                                   ctypes.byref(P.FLAGS.from_buffer_copy(fl.tobytes())), budget, 0, 1.0, 32, 1,
+                                   out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(w))
+            assert rc == 0, k
+            want = g["frames"][g["offsets"][k]:g["offsets"][k + 1]]
+            got = out.astype(np.float32)
+            assert np.array_equal(out, got.astype(np.float64)), k  # float sums, carried exactly
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (k, np.abs(got - want).max())
+            assert w.value == g["weights"][k], k
+    finally:
+        L.oracle_set_libm_trig(0)
+        for h in scenes_.values():
+            L.oracle_scene_destroy(ctypes.c_void_p(h))
+
+
+def test_sampling_and_phase_match_reference_bit_exact(oracle_lib):
+    """UniformSampleSphere (with the platform's sinf/cosf), Integrator::measureRay and the
+    order of HaltonSampler::get2D's pair against the reference's own compiled code."""
+    import ctypes
+    g = np.load(os.path.join(GOLD, "sample_ref.npz"))
+    L = oracle_lib.lib()
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.oracle_uniform_sample_sphere.argtypes = [ctypes.c_float, ctypes.c_float, fp]
+    L.oracle_measure_ray.argtypes = [ctypes.c_float] * 3 + [fp]
+    tmp = np.zeros(3, np.float32)
+    L.oracle_set_libm_trig(1)
+    try:
+        d = np.zeros_like(g["dir"])
+        for i, (a, b) in enumerate(g["u"]):
+            L.oracle_uniform_sample_sphere(float(a), float(b), tmp.ctypes.data_as(fp))
+            d[i] = tmp
+    finally:
+        L.oracle_set_libm_trig(0)
+    assert np.array_equal(d.view(np.uint32), g["dir"].view(np.uint32))
+    m = np.zeros_like(g["measure"])
+    for i, dt in enumerate(g["dt"]):
+        L.oracle_measure_ray(float(dt), 77e9, 78.125e12, tmp.ctypes.data_as(fp))
+        m[i] = tmp[:2]
+    assert np.array_equal(m.view(np.uint32), g["measure"].view(np.uint32))
+    # get2D after one get1D: (dimension 2, dimension 1) in a GCC build
+    pair = np.array([[oracle_lib.radical_inverse(int(k), 2), oracle_lib.radical_inverse(int(k), 1)]
+                     for k in g["get2d_index"]], np.float32)
+    assert np.array_equal(pair.view(np.uint32), g["get2d"].view(np.uint32))
