@@ -486,8 +486,14 @@ def run_batched(args, rank, world, local_rank, dist):
 
     # the product's autotuner picks the launch shape on a bounded sample of the batch (16
     # poses, budgets capped at 2^20); the graph below is captured with it
-    tuned = be.autotune(w.rf, N, t, w.tx[:16], w.rx[:16], np.minimum(w.budget[:16], 1 << 20), phase_mode=phase,
-                        splat_mode=splat)
+    if args.launch_config:  # a fixed shape (profiling runs reproduce the tuned one without tuning)
+        tile, ctas, thr, foh = (int(x) for x in args.launch_config.split(","))
+        be.set_launch_config(tile, ctas, thr, foh)
+        tuned = dict(tile=tile, ctas_per_sm=ctas, queue_threshold=thr, field_on_hit=foh, trace_ms=None,
+                     default_trace_ms=None)
+    else:
+        tuned = be.autotune(w.rf, N, t, w.tx[:16], w.rx[:16], np.minimum(w.budget[:16], 1 << 20), phase_mode=phase,
+                            splat_mode=splat)
     g = be.batch_graph(w.rf, N, t, Q, s_tx.data_ptr(), s_rx.data_ptr(), s_budget.data_ptr(), s_offset.data_ptr(),
                        s_rows.data_ptr(), phase_mode=phase, splat_mode=splat)
 
@@ -901,22 +907,22 @@ def time_to_error(with_boxes=False):
 
 
 def run_urban_mimo(args, rank, world, local_rank, dist):
-    """The guided urban MIMO configuration (scenes.urban_mimo_workload): 12 virtual
-    channels of one pose traced as one guided batch (PathTracer::run's doubling schedule,
-    2^22 samples per channel: 8 iterations), split-FP64 phase, up to 5 bounces; each step
-    also assembles the 128 x 256 x 12 frame on the device (zero velocity: every chirp row
-    is the first) and reads it back. Replicas under torchrun."""
+    """The guided urban MIMO configuration (scenes.urban_mimo_workload): the 3 TX x 4 RX
+    array's 12 virtual channels traced as one guided batch (PathTracer::run's doubling
+    schedule, 2^22 samples per channel: 8 iterations), split-FP64 phase, up to 5 bounces,
+    each step one hsr_simulate_frame call returning the 128 x 256 x 12 radar cube
+    [chirp][sample][channel] to the host. Replicas under torchrun."""
     import torch
 
     from hussar_gb300 import HSR_PHASE_SPLIT_FP64, PathTracer, _lib, gb300, scenes
 
     torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
     L = _lib.lib()
     w = scenes.urban_mimo_workload()
     be = gb300.Backend(w.mesh, None)
     P, N, C = len(w.tx), w.frame.samplesPerChirp, w.frame.chirpCount
-    off = np.array([replica_range(rank, int(b))[0] for b in w.budget], np.int64)
+    budget = int(w.budget[0])
+    off = replica_range(rank, budget)[0]
     res = {}
     for name, guided in (("guided", True), ("plain", False)):
         t = PathTracer()
@@ -924,11 +930,8 @@ def run_urban_mimo(args, rank, world, local_rank, dist):
         t.maxDepth = w.max_depth
 
         def step():
-            rows = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, index_offset=off,
+            return be.simulate_frame(w.rf, w.frame, t, w.tx_array, w.rx_array, budget, index_offset=off,
                                      phase_mode=HSR_PHASE_SPLIT_FP64)
-            d = torch.from_numpy(rows.view(np.float32)).to(dev).view(P, N, 2)
-            frame = d.permute(1, 0, 2).unsqueeze(0).expand(C, N, P, 2).contiguous()  # [chirp][sample][channel]
-            return frame.cpu()
 
         for _ in range(max(args.warmup, 3) if guided else 1):
             step()
@@ -954,9 +957,10 @@ def run_urban_mimo(args, rank, world, local_rank, dist):
                                "samples, guided (8 doubling iterations, 2^22 samples per channel), 5 bounces, "
                                "split FP64 phase" % (w.mesh.triangleCount(), C, N),
                    "frame_shape": [C, N, P], "l2": "inputs larger than L2 (%.0f MB scene)" % (be.footprint() / 1e6)},
-        "e2e": {"value": g["paths_per_s"], "unit": "paths/s", "h2d_bytes_per_step": int(P * (96 + 16)),
+        "e2e": {"value": g["paths_per_s"], "unit": "paths/s",
+                "h2d_bytes_per_step": int((len(w.tx_array) + len(w.rx_array)) * 48 + P * 16),
                 "d2h_bytes_per_step": int(C * N * P * 8),
-                "note": "wall clock through hsr_simulate_batch plus the frame assembly and read-back"},
+                "note": "wall clock through hsr_simulate_frame (host radar cube out, synchronous)"},
         "modes": {"plain_same_budget": res["plain"]},
         "gpu_launches": int(round(g["library_launches_per_step"] * args.steps)),
     }
@@ -1153,6 +1157,8 @@ def main():
     ap.add_argument("--workload", default="boxes",
                     choices=["boxes", "sphere", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
+    ap.add_argument("--launch-config", default=None,
+                    help="boxes workload: tile,ctas_per_sm,queue_threshold,field_on_hit instead of autotuning")
     ap.add_argument("--max-log2", type=int, default=None,
                     help="boxes workload: cap every budget at 2^k (small profiling cases only)")
     ap.add_argument("--traffic", type=float, default=None,

@@ -143,6 +143,15 @@ def lib():
         "hsr_simulate_batch_device_noalloc": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp,
                                               vp, vp, ctypes.c_int32, vp, vp],
         "hsr_scene_status": [vp, vp, P(ctypes.c_uint32)],
+        "hsr_simulate_frame": [vp, P(RFConfigC), P(FrameConfigC), P(FlagsC), ctypes.c_int32, vp, ctypes.c_int32, vp,
+                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, vp, vp],
+        "hsr_guide_create": [vp, P(vp)],
+        "hsr_guide_reset": [vp],
+        "hsr_guide_step": [vp],
+        "hsr_guide_destroy": [vp],
+        "hsr_backend_run_guided": [vp, P(RFConfigC), P(FrameConfigC), P(AntennaC), P(AntennaC), P(FlagsC),
+                                   ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_int32, vp,
+                                   ctypes.c_int32, vp, P(ctypes.c_double), vp],
         "hsr_noalloc_status": [vp, P(ctypes.c_uint32)],
         "hsr_debug_records": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), P(AntennaC), P(AntennaC),
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, vp],

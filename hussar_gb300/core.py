@@ -369,6 +369,23 @@ class _GB300:
                 int(phase_mode), int(splat_mode), _lib.ptr(out), ctypes.c_void_p(stream)))
             return out
 
+        def simulate_frame(self, rf, frame_config, integrator, tx_array, rx_array, budget, index_offset=0,
+                           phase_mode=_lib.HSR_PHASE_REFERENCE_FP32, splat_mode=_lib.HSR_SPLAT_DIRICHLET16,
+                           stream=None):
+            """hsr_simulate_frame: a MIMO radar cube [chirp][sample][channel] (complex64) of
+            len(tx_array) x len(rx_array) virtual channels (channel c = TX c // n_rx, RX
+            c % n_rx), each a run of `budget` samples, traced as one batch."""
+            T, R = len(tx_array), len(rx_array)
+            txa = (_lib.AntennaC * T)(*[a.to_c() for a in tx_array])
+            rxa = (_lib.AntennaC * R)(*[a.to_c() for a in rx_array])
+            fc = frame_config.to_c()
+            out = np.zeros((fc.chirpCount, fc.samplesPerChirp, fc.channelCount), np.complex64)
+            _lib.check(_lib.lib().hsr_simulate_frame(
+                self._scene, ctypes.byref(rf.to_c()), ctypes.byref(fc), ctypes.byref(integrator.flags_c()), T,
+                ctypes.cast(txa, ctypes.c_void_p), R, ctypes.cast(rxa, ctypes.c_void_p), int(budget), int(index_offset),
+                int(phase_mode), int(splat_mode), _lib.ptr(out), ctypes.c_void_p(stream)))
+            return out
+
         def simulate_batch_ff(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None,
                               phase_mode=_lib.HSR_PHASE_REFERENCE_FP32):
             """Far-field runs (hsr_simulate_batch_ff): tx, rx sequences of FFAntenna, one

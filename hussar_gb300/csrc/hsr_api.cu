@@ -637,6 +637,7 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
     cudaFree(s->dev.guide);
     synth_free_operand(s->dev.synth);
     cudaFree(s->dev.synth_scratch);
+    cudaFree(s->dev.frame_buf);
     if (s->dev.ev0) cudaEventDestroy(s->dev.ev0);
     if (s->dev.ev1) cudaEventDestroy(s->dev.ev1);
     delete s;
@@ -818,6 +819,126 @@ hsr_status hsr_backend_run(const hsr_scene *cs, const hsr_rf_config *rf, const h
     return HSR_OK;
 }
 
+// ---- the guiding tree of one pose, for guided backend runs -------------------------
+struct hsr_guide {
+    hsr_scene *scene = nullptr;
+    void *mem = nullptr;
+    GuideMem g;
+    int *active = nullptr;  // device int 1: the step's "this pose continues" flag
+};
+
+hsr_status hsr_guide_create(hsr_scene *s, hsr_guide **out) {
+    if (!out) return fail(HSR_ERR_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    hsr_status st = check_device();
+    if (st != HSR_OK) return st;
+    std::unique_ptr<hsr_guide> g(new hsr_guide());
+    g->scene = s;
+    std::string err;
+    if (!dev_alloc(&g->mem, guide_bytes_per_pose() + 8 * 256, err) || !dev_alloc(&g->active, 256, err)) {
+        cudaFree(g->mem);
+        return fail(HSR_ERR_OUT_OF_MEMORY, "guiding tree: " + err);
+    }
+    g->g = carve_guide(g->mem, 1);
+    const int one = 1;
+    cudaError_t e = cudaMemcpy(g->active, &one, sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess &&
+        launch_guide_reset(1, g->g.samp_child, g->g.samp_p, g->g.train_child, g->g.train_acc, g->g.train_count, 0) != 0)
+        e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaFree(g->mem);
+        cudaFree(g->active);
+        return cuda_fail(e, "guiding tree reset");
+    }
+    *out = g.release();
+    return HSR_OK;
+}
+
+hsr_status hsr_guide_reset(hsr_guide *g) {
+    if (!g) return fail(HSR_ERR_INVALID_ARGUMENT, "null guide");
+    if (launch_guide_reset(1, g->g.samp_child, g->g.samp_p, g->g.train_child, g->g.train_acc, g->g.train_count, 0) !=
+        0)
+        return cuda_fail(cudaGetLastError(), "guide reset");
+    cudaError_t e = cudaStreamSynchronize(0);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "guide reset");
+}
+
+hsr_status hsr_guide_step(hsr_guide *g) {
+    if (!g) return fail(HSR_ERR_INVALID_ARGUMENT, "null guide");
+    if (launch_guide_step(1, g->active, g->g.samp_child, g->g.samp_p, g->g.train_child, g->g.train_acc,
+                          g->g.train_count, 0) != 0)
+        return cuda_fail(cudaGetLastError(), "guide step");
+    cudaError_t e = cudaStreamSynchronize(0);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "guide step");
+}
+
+hsr_status hsr_guide_destroy(hsr_guide *g) {
+    if (!g) return HSR_OK;
+    cudaDeviceSynchronize();
+    cudaFree(g->mem);
+    cudaFree(g->active);
+    delete g;
+    return HSR_OK;
+}
+
+hsr_status hsr_backend_run_guided(hsr_scene *s, const hsr_rf_config *rf, const hsr_frame_config *frame,
+                                  const hsr_antenna *tx, const hsr_antenna *rx, const hsr_tracer_flags *fl,
+                                  int64_t budget, int64_t index_offset, float sample_weight, int32_t train,
+                                  hsr_guide *guide, int32_t phase_mode, float *frame_inout,
+                                  double *total_weight_inout, const volatile int32_t *interrupt_flag) {
+    if (!s || !frame || !tx || !rx || !guide || !frame_inout || !total_weight_inout)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    if (guide->scene != s) return fail(HSR_ERR_INVALID_ARGUMENT, "the guide belongs to another scene");
+    if (frame->chirpCount <= 0 || frame->samplesPerChirp <= 0 || frame->channelCount <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "frame dimensions must be positive");
+    hsr_status st = validate_common(rf, frame->samplesPerChirp, fl);
+    if (st != HSR_OK) return st;
+    if (budget < 0 || index_offset < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
+    if ((st = validate_phase(phase_mode, HSR_SPLAT_DIRICHLET16)) != HSR_OK) return st;
+    if (interrupt_flag && *interrupt_flag) return fail(HSR_ERR_INTERRUPTED, "interrupted before start");
+    if (budget == 0) return HSR_OK;
+    const int32_t N = frame->samplesPerChirp;
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scratch sc;
+    cudaStream_t strm = 0;
+    if ((st = ensure_scratch(s->dev, 1, N, sc, strm)) != HSR_OK) return st;
+    if ((st = upload_poses(sc, 1, tx, rx, &budget, &index_offset, cudaMemcpyHostToDevice, strm)) != HSR_OK) return st;
+    cudaError_t e;
+    const int tr = train ? 1 : 0;
+    if ((e = cudaMemcpyAsync(sc.train, &tr, sizeof(int), cudaMemcpyHostToDevice, strm)) != cudaSuccess ||
+        (e = cudaMemsetAsync(sc.acc, 0, sizeof(double) * 2 * size_t(N), strm)) != cudaSuccess)
+        return cuda_fail(e, "guided run set-up");
+    hsr_tracer_flags g = *fl;
+    g.doGuiding = 1;
+    // about four work items per resident CTA, as the guided schedule's iterations use
+    const int64_t per_item = (budget + 8 * int64_t(s->dev.sm_count) - 1) / (8 * int64_t(s->dev.sm_count));
+    int32_t tile = 256;
+    while (tile < kTile && tile < per_item) tile *= 2;
+    if ((st = enqueue_pass(s->dev, sc, rf, N, &g, 1, sample_weight, false, phase_mode, HSR_SPLAT_DIRICHLET16, strm,
+                           &guide->g, nullptr, 0, nullptr, tile)) != HSR_OK)
+        return st;
+    if (launch_finalize(sc.acc, 1, N, sc.budget, sample_weight, nullptr, 0, sc.rows, strm) != 0)
+        return cuda_fail(cudaGetLastError(), "finalize launch");
+    std::vector<float> row(2 * size_t(N));
+    if ((e = cudaMemcpyAsync(row.data(), sc.rows, sizeof(float) * 2 * N, cudaMemcpyDeviceToHost, strm)) !=
+        cudaSuccess)
+        return cuda_fail(e, "row download");
+    if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "guided backend run");
+    if ((st = read_status(sc, strm)) != HSR_OK) return st;
+    const int C = frame->channelCount;
+    for (int32_t k = 0; k < N; ++k) {
+        size_t id = size_t(k) * C;
+        frame_inout[2 * id] += row[2 * k];
+        frame_inout[2 * id + 1] += row[2 * k + 1];
+    }
+    double w = 0;
+    for (int64_t i = 0; i < budget; ++i) w += double(sample_weight);
+    *total_weight_inout += w;
+    return HSR_OK;
+}
+
 hsr_status hsr_path_tracer_run(hsr_scene *s, const hsr_rf_config *rf, const hsr_frame_config *frame,
                                const hsr_antenna *tx, const hsr_antenna *rx, const hsr_tracer_flags *fl,
                                int64_t samples, int32_t phase_mode, float *frame_out, double *total_weight_out,
@@ -922,6 +1043,57 @@ hsr_status hsr_simulate_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         cudaSuccess)
         return cuda_fail(e, "row download");
     if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "batch run");
+    return read_status(sc, strm);
+}
+
+hsr_status hsr_simulate_frame(hsr_scene *s, const hsr_rf_config *rf, const hsr_frame_config *frame,
+                              const hsr_tracer_flags *fl, int32_t tx_count, const hsr_antenna *tx, int32_t rx_count,
+                              const hsr_antenna *rx, int64_t budget, int64_t index_offset, int32_t phase_mode,
+                              int32_t splat_mode, float *frame_out, void *stream) {
+    if (!s || !frame || !tx || !rx || !frame_out || tx_count <= 0 || rx_count <= 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument or no antennas");
+    if (frame->chirpCount <= 0 || frame->samplesPerChirp <= 0 || frame->channelCount != tx_count * rx_count)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "the frame needs chirps > 0 and tx_count x rx_count channels");
+    if (budget < 0 || index_offset < 0) return fail(HSR_ERR_INVALID_ARGUMENT, "negative budget or offset");
+    const int32_t N = frame->samplesPerChirp, C = frame->channelCount;
+    hsr_status st = validate_common(rf, N, fl);
+    if (st != HSR_OK) return st;
+    if ((st = validate_phase(phase_mode, splat_mode)) != HSR_OK) return st;
+    // channel c = (TX c / rx_count, RX c % rx_count): every virtual channel a pose of one batch
+    std::vector<hsr_antenna> ctx(C), crx(C);
+    for (int32_t c = 0; c < C; ++c) {
+        ctx[c] = tx[c / rx_count];
+        crx[c] = rx[c % rx_count];
+    }
+    std::vector<int64_t> b(C, budget), o(C, index_offset);
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scratch sc;
+    cudaStream_t strm = static_cast<cudaStream_t>(stream);
+    if ((st = ensure_scratch(s->dev, C, N, sc, strm, splat_mode == HSR_SPLAT_FINE_SYNTH)) != HSR_OK) return st;
+    const size_t bytes = sizeof(float) * 2 * size_t(frame->chirpCount) * N * C;
+    if (bytes > s->dev.frame_bytes) {
+        cudaStreamSynchronize(strm);
+        cudaFree(s->dev.frame_buf);
+        s->dev.frame_buf = nullptr;
+        s->dev.frame_bytes = 0;
+        std::string err;
+        if (!dev_alloc(&s->dev.frame_buf, bytes, err)) return fail(HSR_ERR_OUT_OF_MEMORY, "frame buffer: " + err);
+        s->dev.frame_bytes = bytes;
+    }
+    if ((st = upload_poses(sc, C, ctx.data(), crx.data(), b.data(), o.data(), cudaMemcpyHostToDevice, strm)) !=
+        HSR_OK)
+        return st;
+    st = fl->doGuiding ? run_guided(s->dev, sc, rf, N, fl, C, b, o, phase_mode, splat_mode, 1, sc.rows, strm,
+                                    nullptr, nullptr)
+                       : run_plain(s->dev, sc, rf, N, fl, C, 1.f, phase_mode, splat_mode, 1, sc.rows, strm);
+    if (st != HSR_OK) return st;
+    float *d_frame = static_cast<float *>(s->dev.frame_buf);
+    if (launch_assemble_frame(sc.rows, frame->chirpCount, N, C, d_frame, strm) != 0)
+        return cuda_fail(cudaGetLastError(), "frame assembly");
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(frame_out, d_frame, bytes, cudaMemcpyDeviceToHost, strm)) != cudaSuccess)
+        return cuda_fail(e, "frame download");
+    if ((e = cudaStreamSynchronize(strm)) != cudaSuccess) return cuda_fail(e, "frame simulation");
     return read_status(sc, strm);
 }
 

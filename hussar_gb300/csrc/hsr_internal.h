@@ -58,6 +58,8 @@ struct SceneDev {
     SynthOperand synth;          // cached twiddle operand (fine-histogram synthesis)
     void *synth_scratch = nullptr;
     size_t synth_scratch_bytes = 0;
+    void *frame_buf = nullptr;  // MIMO radar cube (hsr_simulate_frame), grown as needed
+    size_t frame_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     LaunchConfig tuned;  // set by hsr_autotune_batch / hsr_set_launch_config
     float last_kernel_ms = 0.f;
@@ -181,6 +183,9 @@ int launch_tile_prefix(const int64_t *budget, int32_t pose_count, int32_t tile, 
 int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, const int64_t *budget, float sample_weight,
                     const double *total_weight, int normalise, float *out_rows, cudaStream_t st);
 int launch_clear_rows(double *acc, int32_t pose_count, int32_t samples, const int *clear, cudaStream_t st);
+// A MIMO radar cube [chirp][sample][channel] from per-channel rows (hsr_simulate_frame).
+int launch_assemble_frame(const float *rows, int32_t chirps, int32_t samples, int32_t channels, float *frame,
+                          cudaStream_t st);
 // The device Halton sampler at host-chosen indices (hsr_debug_halton).
 int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out);
 int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,

@@ -393,11 +393,35 @@ int launch_finalize(const double *acc, int32_t pose_count, int32_t samples, cons
 }
 
 namespace {
+// The radar cube of a MIMO frame (radar.h:487-494: [chirp][sample][channel], complex64)
+// from the channels' fetchFrame rows: a static scene puts everything in Doppler bin 0
+// (PIndex::setVelocity(0), path.h:130), so chirp 0 holds row c at channel c and every
+// other chirp is zero.
+__global__ void k_assemble_frame(const float2 *__restrict__ rows, int32_t chirps, int32_t samples, int32_t channels,
+                                 float2 *__restrict__ frame) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const int64_t n = int64_t(chirps) * samples * channels;
+    if (i >= n) return;
+    const int32_t c = int32_t(i % channels);
+    const int64_t cs = i / channels;
+    const int32_t k = int32_t(cs % samples), chirp = int32_t(cs / samples);
+    frame[i] = chirp == 0 ? rows[int64_t(c) * samples + k] : make_float2(0.f, 0.f);
+}
+
 __global__ void k_debug_halton(const uint64_t *index, int64_t count, int dim, float *out) {
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < count) out[i] = halton(index[i], dim);
 }
 }  // namespace
+
+int launch_assemble_frame(const float *rows, int32_t chirps, int32_t samples, int32_t channels, float *frame,
+                          cudaStream_t st) {
+    const int64_t n = int64_t(chirps) * samples * channels;
+    k_assemble_frame<<<unsigned((n + 255) / 256), 256, 0, st>>>(reinterpret_cast<const float2 *>(rows), chirps,
+                                                                 samples, channels, reinterpret_cast<float2 *>(frame));
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
 
 int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out) {
     if (count <= 0) return 0;

@@ -85,6 +85,34 @@ def dihedral_workload(poses=91, samples_per_pose=1 << 18, size=0.1, distance=1.0
     return Workload("dihedral-4tri-91poses", mesh, rf, fc, tx, rx, np.full(poses, samples_per_pose, np.int64), 2)
 
 
+def evaluation_dihedral_workload(size=0.05, angles_deg=None, samples_per_pose=1 << 19):
+    """The reference's dihedral evaluation setup (examples/src/1_dihedral.cpp:24-109):
+    two 2 mm thick plates (addBox) of edge `size` meeting at the y axis, an AWR sensor
+    with TX at (896, 67, -7) mm and RX at (896, 67, -5) mm rotated about y by
+    (angle - 45) degrees (Eigen::AngleAxisf, formed in float), facing the corner; chirp
+    77 GHz + 60 MHz/us over 60 us, 5 MHz ADC, 256 samples, 0.43 ns antenna delay. The
+    reference's evaluation data sweeps the angle over linspace(-75, 75, 601)."""
+    mesh = TriangleMesh()
+    mesh.addBox([-0.002, 0.0, 0.0], [0.0, size, size])
+    mesh.addBox([0.0, 0.0, -0.002], [size, size, 0.0])
+    rf = RFConfig(startFreq=77e9, freqSlope=60e6 / 1e-6, adcRate=5e6, idleTime=100e-6, rampTime=60e-6,
+                  antennaDelay=0.43e-9)
+    fc = FrameConfig(1, 256, 1)
+    if angles_deg is None:
+        angles_deg = np.linspace(-75.0, 75.0, 601)
+    f32 = np.float32
+    tx, rx = [], []
+    for ang in angles_deg:
+        a = (f32(ang) - f32(45)) / f32(180) * f32(np.pi)
+        c, s = np.cos(a, dtype=np.float32), np.sin(a, dtype=np.float32)
+        rot = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]], np.float32)
+        orient = (rot @ FACING).astype(np.float32)
+        tx.append(NFAntenna((rot @ np.array([0.896, 0.067, -0.007], np.float32)).astype(np.float32), orient))
+        rx.append(NFAntenna((rot @ np.array([0.896, 0.067, -0.005], np.float32)).astype(np.float32), orient))
+    return Workload("evaluation-dihedral-%dmm" % round(size * 1000), mesh, rf, fc, tx, rx,
+                    np.full(len(tx), samples_per_pose, np.int64), 10)
+
+
 def dihedral_ff_workload(poses=9, samples_per_pose=1 << 16, size=0.1, radius=0.1):
     """Monostatic far-field sweep of the dihedral: TX = RX = FFAntenna with direction
     (cos a, 0, sin a), a = 5..85 deg (the corner opens towards +x+z), H = (0, 1, 0),
@@ -316,5 +344,6 @@ def urban_mimo_workload(tris=5_000_000, seed=0xC4, samples=1 << 22, chirps=128):
     rx = [r for _ in txs for r in rxs]
     rf, _ = rf_77ghz(256)
     fc = FrameConfig(chirps, 256, len(tx))
-    return Workload("urban-%dk-mimo3x4" % (tris // 1000), mesh, rf, fc, tx, rx,
-                    np.full(len(tx), samples, np.int64), 5)
+    w = Workload("urban-%dk-mimo3x4" % (tris // 1000), mesh, rf, fc, tx, rx, np.full(len(tx), samples, np.int64), 5)
+    w.tx_array, w.rx_array = txs, rxs  # the physical array (hsr_simulate_frame's arguments)
+    return w

@@ -195,6 +195,31 @@ hsr_status hsr_backend_run(const hsr_scene *scene, const hsr_rf_config *rf,
                            int32_t phase_mode, float *frame_inout,
                            double *total_weight_inout, const volatile int32_t *interrupt_flag);
 
+/* The guiding tree of one pose (GuidingWrapper, path.h:17-131: the 10 % uniform / 90 %
+ * tree mixture over the primary sample square, split threshold 0.005, second moment,
+ * path.h:229-232) on the device, for callers that run PathTracer::run's schedule
+ * themselves (a C++ PathTracer calling its backend once per iteration): create it on
+ * the scene, reset it at the start of a schedule (GuidingWrapper::reset, path.h:47-50),
+ * run each iteration with hsr_backend_run_guided, and step it between iterations
+ * (GuidingWrapper::step, path.h:116-124: build, copy to the sampling tree, refine). The
+ * tree is this library's own (libguiding is not part of the reference sources). */
+typedef struct hsr_guide hsr_guide;
+hsr_status hsr_guide_create(hsr_scene *scene, hsr_guide **out_guide);
+hsr_status hsr_guide_reset(hsr_guide *guide);
+hsr_status hsr_guide_step(hsr_guide *guide);
+hsr_status hsr_guide_destroy(hsr_guide *guide);
+
+/* One guided iteration of PathTracer::run (path.h:186-224): as hsr_backend_run, with each
+ * sample's primary direction drawn from the guide's sampling tree (GuidingWrapper::sample,
+ * path.h:265-270) and, when `train` is non-zero (every iteration but the final one,
+ * path.h:448-450), |guidingWeight| * pdf splatted into its training tree. The flags'
+ * doGuiding is ignored (this call is guided). Synchronous. */
+hsr_status hsr_backend_run_guided(hsr_scene *scene, const hsr_rf_config *rf, const hsr_frame_config *frame,
+                                  const hsr_antenna *tx, const hsr_antenna *rx, const hsr_tracer_flags *flags,
+                                  int64_t budget, int64_t index_offset, float sample_weight, int32_t train,
+                                  hsr_guide *guide, int32_t phase_mode, float *frame_inout,
+                                  double *total_weight_inout, const volatile int32_t *interrupt_flag);
+
 /* PathTracer::run (path.h:171-224) for one pose, guided or plain: clears the frame,
  * then (doGuiding = 0) one backend run over Halton indices [0, samples), or (doGuiding =
  * 1) the doubling schedule from 16384 samples with device path guiding of the primary
@@ -242,6 +267,21 @@ hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
  * the next call on the scene. The reference throws on device errors from its synchronous
  * launch (sutil::Exception, Exception.h:91-191); this is the asynchronous counterpart. */
 hsr_status hsr_scene_status(hsr_scene *scene, void *stream, uint32_t *out_bits);
+
+/* A MIMO radar frame: tx_count x rx_count virtual channels (channel c pairs TX c / rx_count
+ * with RX c % rx_count), each the fetchFrame() of a run of `budget` samples from Halton
+ * index `index_offset` (plain, or with flags->doGuiding PathTracer::run's guided
+ * schedule), all channels traced as one batch. frame_out (HOST) receives the radar cube
+ * in the reference's layout [chirp][sample][channel], complex64 interleaved
+ * (radar.h:487-494): a static scene's energy sits in Doppler bin 0 (PIndex::setVelocity(0),
+ * path.h:130), so chirp 0 holds the channels' rows and every other chirp is zero. The
+ * reference's PathTracer writes one channel per run (path.h:291-292); this traces the
+ * array's channels together. frame->channelCount must be tx_count * rx_count.
+ * Synchronous on `stream`. */
+hsr_status hsr_simulate_frame(hsr_scene *scene, const hsr_rf_config *rf, const hsr_frame_config *frame,
+                              const hsr_tracer_flags *flags, int32_t tx_count, const hsr_antenna *tx,
+                              int32_t rx_count, const hsr_antenna *rx, int64_t budget, int64_t index_offset,
+                              int32_t phase_mode, int32_t splat_mode, float *frame_out, void *stream);
 
 /* Allocation-free form of hsr_simulate_batch_device, for callers that cannot allocate
  * device memory while they simulate (a real-time loop, work recorded into a larger

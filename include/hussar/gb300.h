@@ -18,7 +18,16 @@
  *   scene.rfConfig.{startFreq,freqSlope,adcRate,idleTime,rampTime,antennaDelay}
  *   scene.tx/rx.position().x().., scene.tx/rx.rotation()(row, col)
  *   integrator: the public flags of path.h:153-169, produceDebugImage, and (through
- *   BackendAccess) frame, totalWeight, sampleIndexOffset, currentSampleWeight.
+ *   BackendAccess) frame, totalWeight, sampleIndexOffset, currentSampleWeight and
+ *   isFinalIteration.
+ * Guiding (doGuiding = true, the reference's default, path.h:158): PathTracer::run calls
+ * run() once per iteration of its doubling schedule (path.h:186-224) and steps its own
+ * guiding tree in between. The backend keeps the device tree of the schedule
+ * (hsr_guide_*) and follows the same steps: a run that is not a final iteration and
+ * traces at most the first milestone (16384 samples, path.h:185) starts a schedule
+ * (reset), every later one steps the tree first (the reference steps after every
+ * non-final iteration), and only non-final iterations train it. The integrator's own
+ * tree (libguiding) is not used.
  * Errors: a non-OK hsr_status becomes std::runtime_error (the reference's
  * sutil::Exception derives from std::runtime_error, Exception.h:243); an interrupted
  * run returns silently like cpu::Backend (arch/cpu.h:25).
@@ -49,6 +58,7 @@ template <typename Integrator> struct BackendAccess {
     static void setTotalWeight(Integrator &it, double w) { it.totalWeight = w; }
     static long sampleIndexOffset(Integrator &it) { return long(it.sampleIndexOffset); }
     static float currentSampleWeight(Integrator &it) { return float(it.currentSampleWeight); }
+    static bool isFinalIteration(Integrator &it) { return bool(it.isFinalIteration); }
 };
 
 template <typename Vec> inline void put3(float *out, const Vec &v) {
@@ -76,7 +86,7 @@ template <typename Integrator> inline hsr_tracer_flags to_hsr_flags(const Integr
     f.maxDepth = it.maxDepth;
     f.useGeometricalOptics = it.useGeometricalOptics;
     f.poDiffraction = it.poDiffraction;
-    f.doGuiding = 0;  // the schedule is the integrator's; each backend run is plain
+    f.doGuiding = it.doGuiding;  // the schedule is the integrator's; each run is one iteration
     f.clearBeforeIteration = it.clearBeforeIteration;
     f.correctPhase = it.correctPhase;
     f.filterGuiding = it.filterGuiding;
@@ -123,9 +133,23 @@ struct Backend {
             hsr_tracer_flags fl = to_hsr_flags(integrator);
             double w = A::totalWeight(integrator);
             int32_t flag = (interruptFlag && *interruptFlag) ? 1 : 0;
-            hsr_status s = hsr_backend_run(m_scene, &sv.rf, &f, &sv.tx, &sv.rx, &fl, budget,
+            hsr_status s;
+            if (fl.doGuiding) {
+                const bool final_iteration = A::isFinalIteration(integrator);
+                if (!m_guide) check(hsr_guide_create(m_scene, &m_guide));
+                if (!final_iteration && budget <= 16384)
+                    check(hsr_guide_reset(m_guide));  // a new PathTracer::run (path.h:180-185)
+                else
+                    check(hsr_guide_step(m_guide));  // stepGuiding() after the previous iteration
+                s = hsr_backend_run_guided(m_scene, &sv.rf, &f, &sv.tx, &sv.rx, &fl, budget,
                                            A::sampleIndexOffset(integrator), A::currentSampleWeight(integrator),
-                                           HSR_PHASE_REFERENCE_FP32, buf.data(), &w, &flag);
+                                           final_iteration ? 0 : 1, m_guide, HSR_PHASE_REFERENCE_FP32, buf.data(),
+                                           &w, &flag);
+            } else {
+                s = hsr_backend_run(m_scene, &sv.rf, &f, &sv.tx, &sv.rx, &fl, budget,
+                                    A::sampleIndexOffset(integrator), A::currentSampleWeight(integrator),
+                                    HSR_PHASE_REFERENCE_FP32, buf.data(), &w, &flag);
+            }
             check(s);
             if (s == HSR_ERR_INTERRUPTED) return;
             for (size_t i = 0; i < n; ++i) {
@@ -139,7 +163,10 @@ struct Backend {
     Backend(const Backend &) = delete;
     Backend &operator=(const Backend &) = delete;
 
-    ~Backend() { hsr_scene_destroy(m_scene); }
+    ~Backend() {
+        hsr_guide_destroy(m_guide);
+        hsr_scene_destroy(m_scene);
+    }
 
     template <typename Scene> void run(const Scene &scene, long budget, bool *interruptFlag = nullptr) {
         SceneView sv{to_hsr_rf(scene.rfConfig), to_hsr(scene.tx), to_hsr(scene.rx)};
@@ -150,6 +177,7 @@ struct Backend {
 
 private:
     hsr_scene *m_scene = nullptr;
+    hsr_guide *m_guide = nullptr;  // the guided schedule's device tree (created on first use)
     std::function<void(const SceneView &, long, bool *)> m_run;
 };
 

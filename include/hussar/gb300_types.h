@@ -10,12 +10,14 @@
  *   hussar::PathTracer (flags, run, fetchFrame)         libhussar/include/hussar/integrators/path.h:133-476
  *
  * Same names, members and meaning as the reference, so example programs such as
- * examples/src/1_dihedral.cpp read the same. Only the plain (unguided) schedule is
- * available here; run() with doGuiding = true throws.
+ * examples/src/1_dihedral.cpp read the same. PathTracer::run follows path.h's schedule:
+ * one backend run, or with doGuiding = true (the default) the doubling iterations, the
+ * guiding tree living in the backend.
  */
 #ifndef HUSSAR_GB300_TYPES_H
 #define HUSSAR_GB300_TYPES_H
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -198,6 +200,9 @@ public:
 
     void configureFrame(const radar::FrameConfig &c) { frame.configure(c); }
 
+    // PathTracer::run (path.h:171-224): one backend run, or with guiding the doubling
+    // schedule from 16384 samples whose last iteration takes the remainder; the backend
+    // keeps the guiding tree and steps it between iterations
     template <typename Backend> void run(Backend &backend, const Scene &scene, long samples,
                                          bool *interruptFlag = nullptr) {
         frame.clear();
@@ -208,7 +213,29 @@ public:
             backend.run(scene, samples, interruptFlag);
             return;
         }
-        throw std::runtime_error("gb300: the guided schedule (doGuiding = true) is not available in this build");
+        isFinalIteration = false;
+        long milestone = 16384;
+        long remainingSamples = samples;
+        while (true) {
+            milestone = std::min(milestone, remainingSamples);
+            backend.run(scene, milestone, interruptFlag);
+            if (interruptFlag && *interruptFlag) return;
+            sampleIndexOffset += milestone;
+            remainingSamples -= milestone;
+            if (remainingSamples == 0) break;
+            milestone *= 2;
+            if (remainingSamples < milestone * 2) {
+                isFinalIteration = true;
+                milestone = remainingSamples;
+            }
+            if (clearBeforeIteration) {
+                frame.clear();
+                totalWeight = 0;
+                sampleIndexOffset = 0;
+            } else {
+                currentSampleWeight = 10 * currentSampleWeight;
+            }
+        }
     }
 
     radar::Frame fetchFrame() const { return frame / Float(totalWeight); }
@@ -219,6 +246,7 @@ protected:
     double totalWeight = 0;
     long sampleIndexOffset = 0;
     Float currentSampleWeight = 1.f;
+    bool isFinalIteration = false;
 };
 
 }  // namespace hussar

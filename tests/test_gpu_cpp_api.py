@@ -84,3 +84,37 @@ def test_cpp_server_matches_batch_and_oracle(serve_bin, tmp_path, oracle_lib):
         else:
             # the same Halton samples; only the FP64 summation order differs
             assert np.linalg.norm(rows[k] - batch[k]) / np.linalg.norm(batch[k]) <= 1e-5, k
+
+
+@pytest.fixture(scope="module")
+def guided_bin(product_lib, tmp_path_factory):
+    return compile_example("guided_example", tmp_path_factory.mktemp("cpp"))
+
+
+def test_cpp_guided_schedule(guided_bin, tmp_path):
+    """doGuiding = true (the reference's default) through the C++ drop-in: the mirror
+    PathTracer::run calls Backend::run per doubling iteration and the backend guides each
+    with its device tree. The frames equal the C ABI's own guided schedule
+    (hsr_path_tracer_run, the same samples and tree procedure) up to the order of the
+    float training sums, and both sit near a converged plain result (the guided and plain
+    estimators share the integrand)."""
+    poses, samples = 5, 1 << 18
+    sim = str(tmp_path / "guided.SIM")
+    subprocess.check_call([guided_bin, sim, str(poses), str(samples)])
+    frames = np.fromfile(sim, np.complex64).reshape(poses, 256).astype(np.complex128)
+    w = scenes.dihedral_workload(poses=poses, samples_per_pose=samples)
+    be = gb300.Backend(w.mesh, None)
+    t = PathTracer()
+    t.maxDepth = 2
+    t.doGuiding = True
+    guided = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, w.budget).astype(np.complex128)
+    t.doGuiding = False
+    plain = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, np.full(poses, 1 << 24, np.int64)).astype(np.complex128)
+    for k in range(poses):
+        if np.linalg.norm(plain[k]) == 0:
+            continue
+        e_abi = np.linalg.norm(frames[k] - guided[k]) / np.linalg.norm(guided[k])
+        e_conv = np.linalg.norm(frames[k] - plain[k]) / np.linalg.norm(plain[k])
+        print("pose %d: C++ guided vs C ABI guided %.3e, vs plain 2^24 %.3e" % (k, e_abi, e_conv))
+        assert e_abi <= 0.05, k
+        assert e_conv <= 0.08, k

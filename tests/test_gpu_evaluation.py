@@ -1,0 +1,54 @@
+"""Statistical comparison with the reference's own simulation outputs of its dihedral
+evaluation (evaluation/simulation/dihedral-{5,7,10,15}cm; a fixture of every 4th of the
+601 poses, range bins 8..31, made by tests/golden/make_evaluation_fixture.py). Those are
+guided Monte Carlo runs of an unrecorded length (about 500,000 samples per pose) with
+libguiding's tree, so they are compared within Monte Carlo noise: the same setup
+(examples/src/1_dihedral.cpp) traced here with guiding at 2^19 samples per pose, twice on
+disjoint Halton ranges to measure this estimator's own noise."""
+import os
+
+import numpy as np
+import pytest
+
+from hussar_gb300 import HSR_PHASE_SPLIT_FP64, PathTracer, gb300, scenes
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "dihedral_eval_ref.npz")
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.complex128) - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def runs(product_lib):
+    g = np.load(GOLD)
+    t = PathTracer()  # the reference's defaults: guided, maxDepth 10, filtering sphere
+    lo, hi = int(g["bins"][0]), int(g["bins"][-1]) + 1
+    out = {}
+    for s in g["sizes_mm"]:
+        w = scenes.evaluation_dihedral_workload(size=s / 1000.0, angles_deg=g["angles_deg"])
+        be = gb300.Backend(w.mesh, None)
+        a = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
+        b = be.simulate_batch(w.rf, 256, t, w.tx, w.rx, w.budget, index_offset=np.full(len(w.tx), 1 << 40),
+                              phase_mode=HSR_PHASE_SPLIT_FP64)
+        out[int(s)] = (a[:, lo:hi].astype(np.complex128), b[:, lo:hi].astype(np.complex128),
+                       g["size%d" % s].astype(np.complex128))
+    return g, out
+
+
+def test_range_peak_and_angular_envelope(runs):
+    g, out = runs
+    k20 = int(np.nonzero(g["bins"] == 20)[0][0])
+    for s, (a, b, ref) in out.items():
+        # the reflector's return peaks in range bin 20 in both
+        assert int(np.argmax(np.abs(ref).sum(0))) == k20, s
+        assert int(np.argmax(np.abs(a).sum(0))) == k20, s
+        # angular envelope of that bin: correlation of the magnitudes over the 151 poses
+        c = float(np.corrcoef(np.abs(a[:, k20]), np.abs(ref[:, k20]))[0, 1])
+        self_c = float(np.corrcoef(np.abs(a[:, k20]), np.abs(b[:, k20]))[0, 1])
+        e_ref, e_self = rel_l2(a, ref), rel_l2(a, b)
+        print("dihedral %d mm: envelope corr vs reference %.3f (own runs %.3f), rel L2 vs reference %.3f "
+              "(own runs %.3f), energy ratio %.3f" % (s, c, self_c, e_ref, e_self,
+                                                       np.linalg.norm(a) ** 2 / np.linalg.norm(ref) ** 2))

@@ -42,3 +42,21 @@ def test_urban_mimo_channels_match_oracle(urban):
     assert max(errs) <= 1e-4, errs
     # virtual channels half a wavelength apart see the scene with different phases
     assert rel_l2(rows[0], rows[-1]) > 0.05
+
+
+def test_urban_mimo_radar_cube(urban):
+    """hsr_simulate_frame: the 3 TX x 4 RX array's radar cube [128 chirps][256 samples][12
+    channels] in one call: channel c pairs TX c // 4 with RX c % 4 and equals that pose's
+    batch row (the same samples), the static scene's energy sits in chirp 0 (Doppler bin
+    0) and every other chirp is zero."""
+    w, be, _ = urban
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    N = w.frame.samplesPerChirp
+    cube = be.simulate_frame(w.rf, w.frame, t, w.tx_array, w.rx_array, BUDGET)
+    assert cube.shape == (128, N, 12)
+    rows = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
+    for c in range(12):
+        assert rel_l2(cube[0, :, c], rows[c]) <= 1e-5, c
+    assert np.count_nonzero(cube[1:]) == 0
