@@ -143,6 +143,8 @@ def lib():
         "hsr_simulate_batch_device_noalloc": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp,
                                               vp, vp, ctypes.c_int32, vp, vp],
         "hsr_scene_status": [vp, vp, P(ctypes.c_uint32)],
+        "hsr_read_obj": [ctypes.c_char_p, ctypes.c_int64, vp, ctypes.c_int64, vp, ctypes.c_int64,
+                         P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64)],
         "hsr_simulate_frame": [vp, P(RFConfigC), P(FrameConfigC), P(FlagsC), ctypes.c_int32, vp, ctypes.c_int32, vp,
                                ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, vp, vp],
         "hsr_guide_create": [vp, P(vp)],

@@ -32,6 +32,7 @@ UNITS = {
     "hsr_trace.cu": ["-fmad=false"],
     "hsr_wave.cu": ["-fmad=false"],
     "hsr_wave_split.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "hsr_io.cpp": [],
 }
 
 
@@ -44,7 +45,7 @@ def nvcc():
 
 def _compile(unit, extra, verbose):
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(BUILD, os.path.splitext(unit)[0] + ".o")
     cmd = [nvcc()] + ARCH + COMMON + extra + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

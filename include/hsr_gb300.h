@@ -257,6 +257,19 @@ hsr_status hsr_simulate_batch_device(hsr_scene *scene, const hsr_rf_config *rf,
                                      const int64_t *d_index_offset, int32_t phase_mode,
                                      int32_t splat_mode, float *d_out_rows, void *stream);
 
+/* WavefrontFile::read (io/wavefront.h:12-67): the vertices and triangles of an OBJ file,
+ * for hsr_scene_create. 'v x y z' lines give vertices, 'f a b c' lines triangles from the
+ * first three 1-based vertex indices (an 'a/b/c' token's vertex index is the number
+ * before the first '/'; the reference's `>> int` parse stops there and fails the rest of
+ * the file), written as 0-based indices shifted by vertex_offset (the vertices the
+ * caller's mesh already holds, wavefront.h:23, 42-48); '#' comment lines, 's' and empty
+ * lines are skipped, other commands are counted in *out_unsupported (may be NULL) and
+ * skipped. Call with vertices = indices = NULL for the counts, then with buffers of
+ * 3 * vertex count floats and 3 * triangle count ints. Host only (no device needed). */
+hsr_status hsr_read_obj(const char *path, int64_t vertex_offset, float *vertices, int64_t vertex_capacity,
+                        int32_t *indices, int64_t triangle_capacity, int64_t *out_vertex_count,
+                        int64_t *out_triangle_count, int64_t *out_unsupported);
+
 /* Device status of the last call on this scene: synchronises `stream` (the stream that
  * call ran on) and reads the status word that call's kernels set, into *out_bits (may be
  * NULL): traversal stack overflow (bit 0), a bin out of range (bit 1), a bad work item

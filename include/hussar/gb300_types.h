@@ -5,6 +5,7 @@
  *   radar::RFConfig, radar::FrameConfig, radar::Frame   libradar/include/radar/radar.h:113-701
  *   hussar::Vector3f, hussar::Matrix33f                 (the Eigen types of core/geometry.h:12-33)
  *   hussar::TriangleMesh (addQuad, addBox)              libhussar/include/hussar/core/mesh.h:14-55
+ *   hussar::WavefrontFile (OBJ input)                   libhussar/include/hussar/io/wavefront.h:12-67
  *   hussar::AWRAngularDistribution, hussar::NFAntenna   libhussar/include/hussar/core/emitter.h:109-214
  *   hussar::Scene                                       libhussar/include/hussar/core/scene.h:9-14
  *   hussar::PathTracer (flags, run, fetchFrame)         libhussar/include/hussar/integrators/path.h:133-476
@@ -22,7 +23,10 @@
 #include <complex>
 #include <cstdint>
 #include <stdexcept>
+#include <string>
 #include <vector>
+
+#include "../hsr_gb300.h"
 
 namespace radar {
 
@@ -147,6 +151,31 @@ struct TriangleMesh {
         addQuad(mx, Vector3f(0.f, 0.f, d.z()), Vector3f(0.f, d.y(), 0.f));
         addQuad(mx, Vector3f(d.x(), 0.f, 0.f), Vector3f(0.f, 0.f, d.z()));
     }
+};
+
+/* hussar::WavefrontFile (io/wavefront.h:12-67): read(mesh) appends an OBJ file's vertices
+ * and triangles to the mesh, indices shifted by the vertices it already holds; parsed by
+ * the library (hsr_read_obj). The reference logs an error and exits on a bad file; this
+ * throws std::runtime_error. */
+class WavefrontFile {
+public:
+    explicit WavefrontFile(const std::string &path) : m_path(path) {}
+
+    void read(TriangleMesh &mesh) {
+        int64_t nv = 0, nt = 0;
+        const int64_t offset = int64_t(mesh.vertexBuffer.size());
+        if (hsr_read_obj(m_path.c_str(), offset, nullptr, 0, nullptr, 0, &nv, &nt, nullptr) != HSR_OK)
+            throw std::runtime_error(std::string("WavefrontFile: ") + hsr_last_error());
+        std::vector<float> v(3 * size_t(nv));
+        std::vector<int32_t> f(3 * size_t(nt));
+        if (hsr_read_obj(m_path.c_str(), offset, v.data(), nv, f.data(), nt, &nv, &nt, nullptr) != HSR_OK)
+            throw std::runtime_error(std::string("WavefrontFile: ") + hsr_last_error());
+        for (int64_t i = 0; i < nv; ++i) mesh.vertexBuffer.push_back(Vector3f(v[3 * i], v[3 * i + 1], v[3 * i + 2]));
+        for (int64_t i = 0; i < nt; ++i) mesh.indexBuffer.push_back({f[3 * i], f[3 * i + 1], f[3 * i + 2]});
+    }
+
+private:
+    std::string m_path;
 };
 
 struct AWRAngularDistribution {};

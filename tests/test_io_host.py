@@ -83,3 +83,33 @@ def test_argmax_first_of_equal_magnitudes_and_reference_abs():
     a = complex_abs(z)
     assert a.dtype == np.float32 and a[0] == np.float32(5) and a[1] == 0 and a[3] == np.float32(2.5)
     assert np.isclose(a[2], np.float32(np.sqrt(2) * 1e-30), rtol=1e-6)
+
+
+def test_native_obj_reader_matches_python_reader(tmp_path, product_lib):
+    """hsr_read_obj (the C ABI's WavefrontFile::read, host only) gives the Python reader's
+    vertices and indices, offset by the caller's vertex count, and counts the skipped
+    commands; a short face line is an error."""
+    import ctypes
+    from hussar_gb300 import _lib
+    p = tmp_path / "quad.obj"
+    p.write_text(OBJ)
+    L = product_lib
+    nv, nt, un = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    _lib.check(L.hsr_read_obj(str(p).encode(), 4, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nt),
+                              ctypes.byref(un)))
+    assert (nv.value, nt.value, un.value) == (4, 3, 1)
+    v = np.zeros((nv.value, 3), np.float32)
+    f = np.zeros((nt.value, 3), np.int32)
+    _lib.check(L.hsr_read_obj(str(p).encode(), 4, v.ctypes.data, nv.value, f.ctypes.data, nt.value,
+                              ctypes.byref(nv), ctypes.byref(nt), None))
+    m = TriangleMesh()
+    m.addQuad([5, 5, 5], [1, 0, 0], [0, 1, 0])
+    WavefrontFile(str(p)).read(m)
+    assert np.array_equal(v, m.vertexBuffer[4:]) and np.array_equal(f, m.indexBuffer[2:])
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nf 1 1\n")
+    st = L.hsr_read_obj(str(bad).encode(), 0, None, 0, None, 0, ctypes.byref(nv), ctypes.byref(nt), None)
+    assert st == _lib.HSR_ERR_INVALID_ARGUMENT
+    st = L.hsr_read_obj(str(tmp_path / "missing.obj").encode(), 0, None, 0, None, 0, ctypes.byref(nv),
+                        ctypes.byref(nt), None)
+    assert st == _lib.HSR_ERR_INVALID_ARGUMENT
