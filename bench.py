@@ -721,7 +721,8 @@ TTE_TARGET = 1e-2  # -40 dB: relative L2 of the complex IF signal
 # (error ~ budget^-0.49 with rare grazing next-event spikes; still 10 % off at 2^32), so
 # the reference there is the guided estimator (unbiased, same integrand) at 2^33: two
 # independent 2^32 guided runs agree to 0.3-0.6 %.
-TTE_SCENES = {"sphere_ground": (True, 33, 31), "dihedral_91": (False, 28, 26), "boxes_16": (False, 26, 23)}
+TTE_SCENES = {"sphere_ground": (True, 33, 31), "dihedral_91": (False, 28, 26), "boxes_16": (False, 26, 23),
+              "urban_mimo_12": (False, 25, 22)}
 TTE_BOXES_POSES = 16  # the batched configuration's first 16 poses
 TTE_ANCHOR = 1 << 16  # budget of the FP64-oracle anchor of each scene's converged reference
 TTE_REF_OFFSET = 1_000_000_000_007
@@ -749,10 +750,11 @@ def fp64_anchor(w, be, tracer, poses):
 def time_to_error(with_boxes=False):
     """Time to -40 dB IF-signal error against the plain GPU form, on the sphere+ground pose,
     the 91-pose dihedral sweep and (with_boxes) the first 16 poses of the batched boxes
-    configuration. Each form's rows at budget 2^k (Halton indices 0 .. 2^k-1, k = 10, 11,
+    configuration and the 12 channels of the urban MIMO array. Each form's rows at budget 2^k (Halton indices 0 .. 2^k-1, k = 10, 11,
     ...) are compared with a converged run of the same estimator (split-FP64 phase, Halton
     indices from TTE_REF_OFFSET: guided at 2^33 samples per pose for the sphere, plain at
-    2^28 for the dihedral and 2^26 for the boxes; relative L2 over all poses' rows), whose
+    2^28 for the dihedral, 2^26 for the boxes and 2^25 for the urban channels; relative L2
+    over all poses' rows), whose
     own distance to the FP64 oracle on identical samples is reported (fp64_anchor); the
     smallest such budget reaching 1e-2 is then timed through the host API (wall clock,
     synchronous calls, median of 3).
@@ -768,8 +770,10 @@ def time_to_error(with_boxes=False):
                            the host; a served row is the batched split row up to summation
                            order (the same Halton samples), so it is timed at the budget the
                            batched split form needs, and its error there is reported
+      served_split_guided  the same with guided requests (each runs the doubling schedule
+                           across the server's ticks), at the batched guided form's budget
     A form that does not reach the target by the scene's largest budget (2^31 sphere,
-    2^26 dihedral, 2^23 boxes) reports the budget extrapolated
+    2^26 dihedral, 2^23 boxes, 2^22 urban) reports the budget extrapolated
     from the slope of its last six points (log error vs log budget) and the time for it
     at its measured throughput, marked "extrapolated"."""
     from hussar_gb300 import (HSR_PHASE_REFERENCE_FP32, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16,
@@ -777,9 +781,10 @@ def time_to_error(with_boxes=False):
     L = _lib.lib()
     out = {"target_rel_l2": TTE_TARGET,
            "reference": "split-FP64 phase, same splat kernel, Halton indices from %d (disjoint from the forms'); "
-                        "sphere: guided 2^%d samples per pose, dihedral: plain 2^%d, boxes: plain 2^%d"
-                        % (TTE_REF_OFFSET, TTE_SCENES["sphere_ground"][1], TTE_SCENES["dihedral_91"][1],
-                           TTE_SCENES["boxes_16"][1]),
+                        "sphere: guided 2^%d samples per pose, dihedral: plain 2^%d, boxes: plain 2^%d, "
+                        "urban: plain 2^%d" % (TTE_REF_OFFSET, TTE_SCENES["sphere_ground"][1],
+                                               TTE_SCENES["dihedral_91"][1], TTE_SCENES["boxes_16"][1],
+                                               TTE_SCENES["urban_mimo_12"][1]),
            "timing": "wall clock through hsr_simulate_batch, median of 3"}
     forms = {"plain_gpu": (1, HSR_PHASE_REFERENCE_FP32, HSR_SPLAT_DIRICHLET16, True, False),
              "batched_split": (0, HSR_PHASE_SPLIT_FP64, HSR_SPLAT_DIRICHLET16, False, False),
@@ -793,6 +798,8 @@ def time_to_error(with_boxes=False):
         wb = scenes.boxes_workload()
         wb.tx, wb.rx, wb.budget = wb.tx[:TTE_BOXES_POSES], wb.rx[:TTE_BOXES_POSES], wb.budget[:TTE_BOXES_POSES]
         todo.append(("boxes_16", wb))
+        # the urban MIMO array's 12 virtual channels (5 M triangles, 5 bounces)
+        todo.append(("urban_mimo_12", scenes.urban_mimo_workload(samples=1 << 16)))
     for name, w in todo:
         ref_guided, ref_log2, max_log2 = TTE_SCENES[name]
         plain_t, guided_t = PathTracer(), PathTracer()
@@ -891,11 +898,39 @@ def time_to_error(with_boxes=False):
         finally:
             srv.close()
 
+        # the served guided form: every pose a guided request (the doubling schedule runs
+        # across the server's ticks), at the budget the batched guided form needs
+        bg = res["batched_split_guided"]
+        g_budget = bg["samples_per_pose"] or (1 << max_log2)
+        srv = Server(flags=guided_t, phase_mode=HSR_PHASE_SPLIT_FP64, max_slots=max(P, 1), max_samples_per_chirp=N)
+        try:
+            sid = srv.add_scene(be)
+
+            def serve_guided():
+                reqs = [srv.submit(sid, w.rf, N, w.tx[k], w.rx[k], g_budget) for k in range(P)]
+                return np.stack([r.result()[0] for r in reqs]).astype(np.complex128)
+
+            rows = serve_guided()
+            ref = refs[HSR_SPLAT_DIRICHLET16]
+            entry = {"samples_per_pose": bg["samples_per_pose"], "budget_timed": g_budget,
+                     "error_at_budget": float(np.linalg.norm(rows - ref) / np.linalg.norm(ref))}
+            times = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                serve_guided()
+                times.append(time.perf_counter() - t0)
+            if bg["samples_per_pose"]:
+                entry["seconds"] = float(np.median(times))
+            entry["server"] = {k: v for k, v in srv.stats().items() if k in ("ticks", "max_batch", "device_ms")}
+            res["served_split_guided"] = entry
+        finally:
+            srv.close()
+
         def seconds(e):
             return e.get("seconds") or (e.get("extrapolated") or {}).get("seconds")
 
         plain = seconds(res["plain_gpu"])
-        for fname in list(forms) + ["served_split"]:
+        for fname in list(forms) + ["served_split", "served_split_guided"]:
             if fname != "plain_gpu" and fname in res:
                 sec = seconds(res[fname])
                 res[fname]["speedup_vs_plain_gpu"] = (plain / sec) if (plain and sec) else None
@@ -1057,7 +1092,7 @@ def run_serve(args, rank, world, local_rank, dist):
 
     torch.cuda.set_device(local_rank)
     t = PathTracer()
-    t.doGuiding = False
+    t.doGuiding = bool(args.guided)
     t.maxDepth = 4
     t0 = time.perf_counter()
     backends, posegens, tris = [], [], 0
@@ -1110,6 +1145,20 @@ def run_serve(args, rank, world, local_rank, dist):
     clk = clocks.stop()
     st = srv.stats()
     srv.close()
+    # the error the served rows reach: a sample of requests against converged runs of the
+    # same request (16x its budget, at most 2^27, on a disjoint Halton range, split phase)
+    err_sample = []
+    if rank == 0:
+        for k in np.linspace(0, n_req - 1, min(8, n_req)).astype(int):
+            row = handles[k].result()[0].astype(np.complex128)
+            rf = scenes.rf_chirp(bandwidth=float(bw[k]), samples=int(nbins[k]))
+            ref_budget = min(16 * int(budget[k]), 1 << 27)
+            ref = backends[int(sid[k])].simulate_batch(rf, int(nbins[k]), t, [poses[k]], [poses[k]], [ref_budget],
+                                                       index_offset=[TTE_REF_OFFSET],
+                                                       phase_mode=HSR_PHASE_SPLIT_FP64)[0].astype(np.complex128)
+            nr = np.linalg.norm(ref)
+            if nr > 0:
+                err_sample.append((int(budget[k]), float(np.linalg.norm(row - ref) / nr)))
     lat = np.array([i["latency_ms"] for i in infos])
     que = np.array([i["queue_ms"] for i in infos])
     paths = int(budget.sum())
@@ -1124,9 +1173,11 @@ def run_serve(args, rank, world, local_rank, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "serving: %d resident scenes (%s), %.0f req/s Poisson for %.1f s, budgets "
                                "2^16..2^24 log-uniform, bandwidth 1..4 GHz, N in {128,256,512}, 4 bounces, "
-                               "split FP64 phase" % (len(backends), ", ".join("%s-%dk" % (k, n // 1000) for k, n in
-                                                                               scenes.SERVE_SCENES),
-                                                     args.rate, args.duration),
+                               "split FP64 phase%s" % (len(backends), ", ".join("%s-%dk" % (k, n // 1000) for k, n in
+                                                                                 scenes.SERVE_SCENES),
+                                                       args.rate, args.duration,
+                                                       ", guided requests (doubling schedule across ticks)"
+                                                       if args.guided else ""),
                    "requests": n_req, "triangles": tris, "scene_bytes": st["scene_bytes"],
                    "max_slots": args.slots, "tick_ms": args.tick_ms, "setup_s": setup_s,
                    "l2": "inputs larger than L2 (%.2f GB of resident scenes)" % (st["scene_bytes"] / 1e9)},
@@ -1136,7 +1187,11 @@ def run_serve(args, rank, world, local_rank, dist):
                     "device_paths_per_s": st["samples"] / (st["device_ms"] / 1000.0) if st["device_ms"] else None,
                     "device_busy_frac": st["device_ms"] / (1000.0 * wall), "ticks": st["ticks"],
                     "max_batch": st["max_batch"], "max_resident": st["max_resident"],
-                    "admitted_while_busy": st["admitted_while_busy"], "failed": st["failed"]},
+                    "admitted_while_busy": st["admitted_while_busy"], "failed": st["failed"],
+                    "error_sample": {"requests": [{"budget": b, "rel_l2": e, "db": 20 * float(np.log10(e))}
+                                                  for b, e in err_sample],
+                                     "at_minus40db": sum(e <= TTE_TARGET for _, e in err_sample),
+                                     "reference": "16x the request's budget (at most 2^27), disjoint Halton range"}},
         "e2e": {"value": value, "unit": "paths/s",
                 "h2d_bytes_per_step": int(n_req * 152), "d2h_bytes_per_step": int(8 * nbins.sum()),
                 "note": "wall clock from the first arrival to the last row on the host, through hsr_server_*"},
@@ -1170,6 +1225,7 @@ def main():
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals")
     ap.add_argument("--slots", type=int, default=256, help="serve: requests admitted at once")
     ap.add_argument("--tick-ms", type=float, default=4.0, help="serve: target device time per tick")
+    ap.add_argument("--guided", action="store_true", help="serve: guided requests (PathTracer::run's schedule)")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     dist = init_dist(world)

@@ -169,37 +169,6 @@ static hsr_status synthesise(SceneDev &sc, const Scratch &s, int32_t P, float sa
     return HSR_OK;
 }
 
-// Guiding trees for P poses.
-struct GuideMem {
-    int *samp_child;
-    float *samp_p;
-    int *train_child;
-    float *train_acc;
-    int *train_count;
-    // the whole schedule of a guided call, iteration-major: per iteration budget and
-    // Halton offset (int64), sample weight (float), train, clear and active flags (int)
-    unsigned char *sched;
-};
-
-static GuideMem carve_guide(void *base, int P) {
-    GuideMem g;
-    char *p = static_cast<char *>(base);
-    size_t off = 0;
-    const size_t M = size_t(P) * kGuideMaxNodes;
-    auto take = [&](size_t bytes) {
-        char *r = p + off;
-        off += align256(bytes);
-        return r;
-    };
-    g.samp_child = reinterpret_cast<int *>(take(4 * M));
-    g.samp_p = reinterpret_cast<float *>(take(4 * M));
-    g.train_child = reinterpret_cast<int *>(take(4 * M));
-    g.train_acc = reinterpret_cast<float *>(take(12 * M));
-    g.train_count = reinterpret_cast<int *>(take(4 * size_t(P)));
-    g.sched = reinterpret_cast<unsigned char *>(take(size_t(kGuideMaxIters) * 32 * size_t(P)));
-    return g;
-}
-
 static hsr_status ensure_guide(SceneDev &sc, int P, GuideMem &out) {
     if (P > sc.guide_cap) {
         if (sc.guide) {
@@ -272,7 +241,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
         p.flags.doGuiding = 0;
     }
     const bool wave = g_path_kernel == 0 && fl->useGeometricalOptics && !records && !counters;
-    int per_sm = wave ? wave_blocks_per_sm(N, false) : trace_blocks_per_sm(N, splat_mode, 0);
+    int per_sm = wave ? wave_blocks_per_sm(N, false, p.do_guide != 0) : trace_blocks_per_sm(N, splat_mode, 0);
     if (wave && tuned) {
         if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);
         p.queue_threshold = sc.tuned.queue_threshold;
@@ -324,16 +293,7 @@ static hsr_status run_plain(SceneDev &sc, const Scratch &s, const hsr_rf_config 
     return HSR_OK;
 }
 
-// PathTracer::run's schedule (path.h:171-224) for one pose: per iteration the
-// backend-run budget, Halton offset, sample weight, whether the frame is cleared
-// before it, and whether it trains the guiding tree (not in the final iteration).
-struct Iter {
-    int64_t budget, offset;
-    float weight;
-    bool clear, train;
-};
-
-static std::vector<Iter> schedule(int64_t samples, bool clearBeforeIteration) {
+std::vector<Iter> schedule(int64_t samples, bool clearBeforeIteration) {
     std::vector<Iter> it;
     int64_t milestone = 16384, remaining = samples, offset = 0;
     float weight = 1.f;

@@ -14,10 +14,10 @@
 // (path.h:119-126).
 #pragma once
 #include "hsr_common.cuh"
+#include "hsr_internal.h"
 
 namespace hsr {
 
-constexpr int kGuideMaxNodes = 2048;
 constexpr int kGuideMaxDepth = 24;
 constexpr float kGuideUniformProb = 0.1f;    // path.h:229
 constexpr float kGuideSplitThreshold = 0.005f;  // path.h:230

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/hsr_gb300.h"
 
@@ -84,6 +85,17 @@ template <typename T> inline bool dev_alloc(T **p, size_t bytes, std::string &er
 
 void note_launches(int64_t n);
 const SceneDev *scene_device_state(const hsr_scene *s);
+// Guiding trees for P poses.
+// PathTracer::run's schedule (path.h:171-224) for one pose: per iteration the
+// backend-run budget, Halton offset, sample weight, whether the frame is cleared
+// before it, and whether it trains the guiding tree (not in the final iteration).
+struct Iter {
+    int64_t budget, offset;
+    float weight;
+    bool clear, train;
+};
+std::vector<Iter> schedule(int64_t samples, bool clearBeforeIteration);
+
 // The device status word's bits as a message ("device status: ...").
 std::string status_text(unsigned bits);
 // The scene's call lock (calls on one scene are serialised).
@@ -156,6 +168,9 @@ struct TraceParams {
     // uniform batch, wavefront kernel: the first double of each pose's 2N accumulators in
     // acc (a serving tick whose requests share scene, chirp and N); nullptr: pose-major rows
     const int64_t *acc_row;
+    // guided launches: the guiding-tree slot of each pose in the g_* arrays (a serving
+    // tick's requests own trees of the server's pool); nullptr: the pose index
+    const int32_t *guide_slot;
 };
 
 
@@ -166,6 +181,40 @@ int launch_guide_step(int P, const int *active, int *samp_child, float *samp_p, 
                       int *train_count, cudaStream_t st);
 // longest guided schedule (PathTracer::run iterations) a call may have
 constexpr int kGuideMaxIters = 50;
+// guiding tree nodes per pose (hsr_guide.cuh)
+constexpr int kGuideMaxNodes = 2048;
+
+// Guiding trees for P poses, carved from one allocation.
+struct GuideMem {
+    int *samp_child;
+    float *samp_p;
+    int *train_child;
+    float *train_acc;
+    int *train_count;
+    // the whole schedule of a guided call, iteration-major: per iteration budget and
+    // Halton offset (int64), sample weight (float), train, clear and active flags (int)
+    unsigned char *sched;
+};
+
+inline GuideMem carve_guide(void *base, int P) {
+    GuideMem g;
+    char *p = static_cast<char *>(base);
+    size_t off = 0;
+    const size_t M = size_t(P) * kGuideMaxNodes;
+    auto take = [&](size_t bytes) {
+        char *r = p + off;
+        off += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    g.samp_child = reinterpret_cast<int *>(take(4 * M));
+    g.samp_p = reinterpret_cast<float *>(take(4 * M));
+    g.train_child = reinterpret_cast<int *>(take(4 * M));
+    g.train_acc = reinterpret_cast<float *>(take(12 * M));
+    g.train_count = reinterpret_cast<int *>(take(4 * size_t(P)));
+    g.sched = reinterpret_cast<unsigned char *>(take(size_t(kGuideMaxIters) * 32 * size_t(P)));
+    return g;
+}
+
 
 int synth_build_operand(SynthOperand &op, int N, cudaStream_t st, std::string &err);
 void synth_free_operand(SynthOperand &op);
@@ -195,7 +244,7 @@ int trace_smem_bytes(int samples, int splat_mode, int fine_bins);
 size_t wave_smem_bytes(int samples, bool guided);
 // The split-phase instantiations of the wavefront kernel (hsr_wave_split.cu).
 void launch_wave_split(const TraceParams &p, int grid, cudaStream_t st);
-int wave_blocks_per_sm(int samples, bool mixed);
+int wave_blocks_per_sm(int samples, bool mixed, bool guided = false);
 int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st, std::string &err);
 // 0: wavefront kernel whenever the flags allow it; 1: always the one-thread-per-sample kernel
 extern int g_path_kernel;

@@ -658,7 +658,7 @@ __device__ __forceinline__ PoseCtx load_pose(const TraceParams &p, int pose) {
     c.fine_row = p.fine ? p.fine + size_t(pose) * 2 * kFineMoments * p.fine_bins : nullptr;
     c.weight = p.weights ? __ldg(&p.weights[pose]) : p.sample_weight;
     c.train = (p.do_guide && p.train) ? __ldg(&p.train[pose]) : 0;
-    const size_t g = size_t(pose) * kGuideMaxNodes;
+    const size_t g = size_t(p.guide_slot ? __ldg(&p.guide_slot[pose]) : pose) * kGuideMaxNodes;
     c.samp_child = p.do_guide ? p.g_samp_child + g : nullptr;
     c.samp_p = p.do_guide ? p.g_samp_p + g : nullptr;
     c.train_child = p.do_guide ? p.g_train_child + g : nullptr;

@@ -25,6 +25,16 @@
 //              and its CTAs take the SMs the running tick's tail frees. A tick's
 //              finalize waits for the previous tick (requests span ticks), which also
 //              keeps completions in order.
+//   guiding    (server flags with doGuiding) every request runs PathTracer::run's
+//              doubling schedule (path.h:171-224) over a guiding tree of the server's
+//              pool (one per slot, reset at admission): a request's chunks come from its
+//              current iteration (Halton offset, sample weight and training flag of that
+//              iteration); the tick that places an iteration's last chunk, once the
+//              previous tick is done too, clears the request's row when the next iteration
+//              starts a fresh frame and steps its tree (k_guide_step: build, copy,
+//              refine); the request is planned again only after that tick has finished,
+//              so the next iteration samples the stepped tree. The final iteration does
+//              not train, and its row is normalised by that iteration's total weight.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -55,19 +65,19 @@ constexpr int kEndRing = 4;      // tick-end events kept for the busy-time union
 struct FinJob {
     int64_t acc_offset;  // doubles into the arena
     int64_t out_offset;  // floats into the tick's output block
-    int64_t budget;
+    double total_weight;  // the frame's totalWeight: budget (plain), the schedule's (guided)
     int32_t samples;
     int32_t reserved;
 };
 
-// fetchFrame of finished requests: row = acc / totalWeight with totalWeight = budget
-// (sample weight 1, path.h:445,453-455), rounded as k_finalize; then clears the
-// accumulators. One CTA per request.
+// fetchFrame of finished requests: row = acc / totalWeight (path.h:445,453-455; plain:
+// budget x sample weight 1), rounded as k_finalize; then clears the accumulators. One CTA
+// per request.
 __global__ void k_serve_finalize(const FinJob *__restrict__ jobs, double *acc, float *out) {
     const FinJob j = jobs[blockIdx.x];
     double *a = acc + j.acc_offset;
     float *o = out + j.out_offset;
-    const float inv = 1.f / float(double(j.budget) * double(1.f));
+    const float inv = 1.f / float(j.total_weight);
     for (int k = threadIdx.x; k < j.samples; k += blockDim.x) {
         float re = float(a[2 * k]), im = float(a[2 * k + 1]);
         o[2 * k] = re * inv;
@@ -75,6 +85,13 @@ __global__ void k_serve_finalize(const FinJob *__restrict__ jobs, double *acc, f
         a[2 * k] = 0.0;
         a[2 * k + 1] = 0.0;
     }
+}
+
+// clearFrame between guided iterations (path.h:212-215): zero the listed rows
+__global__ void k_serve_clear(const FinJob *__restrict__ jobs, double *acc) {
+    const FinJob j = jobs[blockIdx.x];
+    double *a = acc + j.acc_offset;
+    for (int k = threadIdx.x; k < 2 * j.samples; k += blockDim.x) a[k] = 0.0;
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -126,7 +143,16 @@ struct Req {
     uint64_t ticket = 0;
     const SceneDev *scene = nullptr;
     Clock::time_point t_submit, t_admit, t_done;
-    int64_t scheduled = 0;  // samples handed to ticks
+    int64_t scheduled = 0;  // samples handed to ticks (all iterations)
+    // guided requests: the schedule, the current iteration and how much of it was handed
+    // out, the pool tree, and the tick whose end releases the next iteration
+    std::vector<Iter> sched;
+    int iter = 0;
+    int64_t iter_done = 0;
+    int guide_slot = -1;
+    bool needs_reset = false;
+    bool waiting = false;
+    int64_t wait_seq = -1;
     int64_t arena_off = -1, arena_bytes = 0;
     int32_t ticks = 0;
     int32_t in_flight = 0;  // queued ticks that contain a segment of it
@@ -139,7 +165,8 @@ using ReqPtr = std::shared_ptr<Req>;
 
 // Fixed layout of a tick's input block (host pinned and device), for `cap` segments.
 struct TickLayout {
-    size_t counters = 0, tile = 0, budget = 0, offset = 0, tx = 0, rx = 0, jobs = 0, acc_row = 0, fin = 0, bytes = 0;
+    size_t counters = 0, tile = 0, budget = 0, offset = 0, tx = 0, rx = 0, jobs = 0, acc_row = 0, fin = 0;
+    size_t weight = 0, train = 0, slot = 0, active = 0, clear = 0, bytes = 0;
     void init(int cap) {
         size_t o = 0;
         counters = o;
@@ -160,6 +187,18 @@ struct TickLayout {
         o = align256(o + sizeof(int64_t) * cap);
         fin = o;
         o = align256(o + sizeof(FinJob) * cap);
+        // guided ticks: per segment sample weight, training flag and tree slot; per pool
+        // tree the step flag; rows cleared between iterations
+        weight = o;
+        o = align256(o + sizeof(float) * cap);
+        train = o;
+        o = align256(o + sizeof(int32_t) * cap);
+        slot = o;
+        o = align256(o + sizeof(int32_t) * cap);
+        active = o;
+        o = align256(o + sizeof(int32_t) * cap);
+        clear = o;
+        o = align256(o + sizeof(FinJob) * cap);
         bytes = o;
     }
 };
@@ -173,6 +212,7 @@ struct TickSlot {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<ReqPtr> members;                         // requests with a segment in the tick
     std::vector<std::pair<ReqPtr, int64_t>> finishing;  // requests finalized by it (out offset)
+    std::vector<ReqPtr> stepping;                        // guided requests ending an iteration in it
     int64_t samples = 0;
 };
 
@@ -207,6 +247,11 @@ struct hsr_server {
     int64_t built = 0;         // ticks queued so far
     double *d_arena = nullptr;
     Arena arena;
+    // guided serving: one guiding tree per slot, and the free trees
+    bool guided = false;
+    void *d_guide = nullptr;
+    GuideMem guide{};
+    std::vector<int> free_trees;
     TickLayout layout;
     TickSlot slots[kTickSlots];
     int64_t out_floats_cap = 0;
@@ -272,6 +317,7 @@ hsr_server::~hsr_server() {
         if (t.ev1) cudaEventDestroy(t.ev1);
     }
     if (d_arena) cudaFree(d_arena);
+    if (d_guide) cudaFree(d_guide);
 }
 
 // Called with `mu` held.
@@ -283,6 +329,10 @@ void hsr_server::finish_request(const ReqPtr &q, hsr_status st, Clock::time_poin
         arena.release(q->arena_off, q->arena_bytes);
         q->arena_off = -1;
         admission_blocked = false;
+    }
+    if (q->guide_slot >= 0) {
+        free_trees.push_back(q->guide_slot);
+        q->guide_slot = -1;
     }
     active.erase(std::remove(active.begin(), active.end(), q), active.end());
     if (st == HSR_OK) {
@@ -312,19 +362,28 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             q->arena_off = off;
             q->arena_bytes = bytes;
             q->t_admit = Clock::now();
+            if (guided) {
+                // a free tree always exists: there are as many as slots
+                q->guide_slot = free_trees.back();
+                free_trees.pop_back();
+                q->needs_reset = true;
+                q->sched = schedule(q->r.budget, cfg.flags.clearBeforeIteration != 0);
+            }
             active.push_back(q);
             if (busy) ++st_while_busy;
         }
         st_max_resident = std::max(st_max_resident, int32_t(active.size()));
         st_mem_peak = std::max(st_mem_peak, arena.used());
         for (const ReqPtr &q : active)
-            if (!q->failed && !q->finalize_queued) cand.push_back(q);
+            if (!q->failed && !q->finalize_queued && !q->waiting) cand.push_back(q);
     }
     if (cand.empty()) return false;
 
     const int n = int(cand.size());
     std::vector<int64_t> remaining(n), chunk(n);
-    for (int i = 0; i < n; ++i) remaining[i] = cand[i]->r.budget - cand[i]->scheduled;
+    for (int i = 0; i < n; ++i)
+        remaining[i] = guided ? cand[i]->sched[cand[i]->iter].budget - cand[i]->iter_done
+                              : cand[i]->r.budget - cand[i]->scheduled;
     const double target = std::min(std::max(rate * double(cfg.tick_ms), double(min_tick)), double(int64_t(1) << 32));
     plan_tick(n, remaining.data(), int64_t(target), kServeTile, chunk.data());
     // work items of this tick: kServeTile samples, or larger (up to kServeMaxTile) when the
@@ -352,10 +411,18 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     PoseJob *jobs = reinterpret_cast<PoseJob *>(h + layout.jobs);
     int64_t *acc_row = reinterpret_cast<int64_t *>(h + layout.acc_row);
     FinJob *fin = reinterpret_cast<FinJob *>(h + layout.fin);
+    float *weight = reinterpret_cast<float *>(h + layout.weight);
+    int32_t *train = reinterpret_cast<int32_t *>(h + layout.train);
+    int32_t *slot = reinterpret_cast<int32_t *>(h + layout.slot);
+    int32_t *step_active = reinterpret_cast<int32_t *>(h + layout.active);
+    FinJob *clear = reinterpret_cast<FinJob *>(h + layout.clear);
+    if (guided) std::memset(step_active, 0, sizeof(int32_t) * size_t(cfg.max_slots));
+    std::vector<int> resets;
     t.members.clear();
     t.finishing.clear();
+    t.stepping.clear();
     t.samples = 0;
-    int P = 0, F = 0, maxN = 1;
+    int P = 0, F = 0, C = 0, maxN = 1;
     // the tick's GENERATE threshold: the smallest of its scenes' tuned thresholds, where a
     // scene never tuned (or tuned to 64 or less) counts as 64
     int32_t queue_threshold = kWaveMaxQueueThreshold;
@@ -366,11 +433,21 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     tile[0] = 0;
     for (int i : order) {
         const ReqPtr &q = cand[i];
+        if (q->needs_reset) {
+            resets.push_back(q->guide_slot);
+            q->needs_reset = false;
+        }
+        const Iter *it = guided ? &q->sched[q->iter] : nullptr;
         if (chunk[i] > 0) {
             tx[P] = q->r.tx;
             rx[P] = q->r.rx;
             budget[P] = chunk[i];
-            offset[P] = q->r.index_offset + q->scheduled;
+            // guided: the iteration's Halton range (each iteration restarts at the caller's
+            // offset when it clears the frame, path.h:212-215) at its sample weight
+            offset[P] = q->r.index_offset + (guided ? it->offset + q->iter_done : q->scheduled);
+            weight[P] = guided ? it->weight : 1.f;
+            train[P] = guided && it->train ? 1 : 0;
+            slot[P] = guided ? q->guide_slot : 0;
             PoseJob &j = jobs[P];
             j.nodes = q->scene->nodes;
             j.tris = q->scene->tris;
@@ -391,13 +468,36 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             if (q->scene->tuned.queue_threshold <= kWaveSmallQueue) queue_threshold = kWaveSmallQueue;
             ++P;
             q->scheduled += chunk[i];
+            q->iter_done += chunk[i];
             q->ticks += 1;
             q->in_flight += 1;
             t.members.push_back(q);
             t.samples += chunk[i];
         }
-        if (q->scheduled == q->r.budget) {
-            fin[F] = FinJob{q->arena_off / int64_t(sizeof(double)), out_off, q->r.budget, q->r.samples_per_chirp, 0};
+        if (guided && q->iter_done == it->budget && q->iter + 1 < int(q->sched.size())) {
+            // the iteration's last chunk: after this tick (and the previous one) the tree is
+            // stepped and, when the next iteration starts a fresh frame, the row cleared;
+            // the request waits for this tick before it is planned again
+            step_active[q->guide_slot] = 1;
+            if (q->sched[q->iter + 1].clear)
+                clear[C++] = FinJob{q->arena_off / int64_t(sizeof(double)), 0, 0.0, q->r.samples_per_chirp, 0};
+            q->waiting = true;
+            q->wait_seq = built;
+            t.stepping.push_back(q);
+            continue;
+        }
+        if (guided ? q->iter_done == it->budget : q->scheduled == q->r.budget) {
+            // the frame's totalWeight: the final iteration's samples at its weight when the
+            // frame was cleared before it, else the weighted sum since the start
+            double tw = double(q->r.budget);
+            if (guided) {
+                tw = 0.0;
+                for (const Iter &k : q->sched) {
+                    if (k.clear) tw = 0.0;
+                    tw += double(k.budget) * double(k.weight);
+                }
+            }
+            fin[F] = FinJob{q->arena_off / int64_t(sizeof(double)), out_off, tw, q->r.samples_per_chirp, 0};
             t.finishing.emplace_back(q, out_off);
             out_off += 2 * int64_t(q->r.samples_per_chirp);
             q->finalize_queued = true;
@@ -413,10 +513,27 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     cudaError_t e = cudaMemcpyAsync(t.d_in, t.h_in, layout.bytes, cudaMemcpyHostToDevice, stream);
     cudaEventRecord(t.ev0, stream);
     std::string err;
+    // newly admitted guided requests start from a fresh tree (GuidingWrapper::reset, path.h:180)
+    for (size_t k = 0; e == cudaSuccess && k < resets.size(); ++k) {
+        const size_t g = size_t(resets[k]) * kGuideMaxNodes;
+        if (launch_guide_reset(1, guide.samp_child + g, guide.samp_p + g, guide.train_child + g,
+                               guide.train_acc + 3 * g, guide.train_count + resets[k], stream) != 0)
+            e = cudaErrorLaunchFailure;
+    }
     if (e == cudaSuccess && P > 0) {
         TraceParams p{};
         p.flags = cfg.flags;
-        p.flags.doGuiding = 0;
+        p.flags.doGuiding = guided ? 1 : 0;
+        if (guided) {
+            p.do_guide = 1;
+            p.train = reinterpret_cast<const int *>(t.d_in + layout.train);
+            p.weights = reinterpret_cast<const float *>(t.d_in + layout.weight);
+            p.guide_slot = reinterpret_cast<const int32_t *>(t.d_in + layout.slot);
+            p.g_samp_child = guide.samp_child;
+            p.g_samp_p = guide.samp_p;
+            p.g_train_child = guide.train_child;
+            p.g_train_acc = guide.train_acc;
+        }
         p.samples = maxN;
         p.pose_count = P;
         p.tx = reinterpret_cast<const hsr_antenna *>(t.d_in + layout.tx);
@@ -448,11 +565,22 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             p.field_on_hit = q0->scene->tuned.field_on_hit;
         }
         auto it = blocks_cache.find(maxN);
-        if (it == blocks_cache.end()) it = blocks_cache.emplace(maxN, wave_blocks_per_sm(maxN, true)).first;
+        if (it == blocks_cache.end()) it = blocks_cache.emplace(maxN, wave_blocks_per_sm(maxN, true, guided)).first;
         if (launch_wave(p, cfg.phase_mode, sm_count * it->second, stream, err) != 0) e = cudaErrorLaunchFailure;
     }
     // requests span ticks: everything after this point waits for the previous tick
     if (e == cudaSuccess && built > 0) e = cudaStreamWaitEvent(stream, end_ev[(built - 1) % kEndRing], 0);
+    // guided iterations that ended here: clear the rows the next iteration starts afresh,
+    // then step the trees (every chunk of the iteration has run: this tick and the last)
+    if (e == cudaSuccess && C > 0) {
+        k_serve_clear<<<C, 256, 0, stream>>>(reinterpret_cast<const FinJob *>(t.d_in + layout.clear), d_arena);
+        note_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && !t.stepping.empty() &&
+        launch_guide_step(cfg.max_slots, reinterpret_cast<const int *>(t.d_in + layout.active), guide.samp_child,
+                          guide.samp_p, guide.train_child, guide.train_acc, guide.train_count, stream) != 0)
+        e = cudaErrorLaunchFailure;
     if (e == cudaSuccess && F > 0) {
         k_serve_finalize<<<F, 256, 0, stream>>>(reinterpret_cast<const FinJob *>(t.d_in + layout.fin), d_arena,
                                                 t.d_out);
@@ -476,6 +604,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
         for (const ReqPtr &q : t.members) q->in_flight -= 1;
         for (const ReqPtr &q : t.members) q->failed = true;
         for (auto &fo : t.finishing) fo.first->failed = true;  // includes zero-budget requests
+        for (const ReqPtr &q : t.stepping) q->failed = true;
         std::vector<ReqPtr> gone;
         for (const ReqPtr &q : active)
             if (q->failed && q->in_flight == 0 && !q->done) gone.push_back(q);
@@ -485,6 +614,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
         }
         t.members.clear();
         t.finishing.clear();
+        t.stepping.clear();
         cv_done.notify_all();
         return false;
     }
@@ -518,6 +648,14 @@ void hsr_server::complete_tick(TickSlot &t) {
         }
         for (auto &fo : t.finishing)
             if (!fo.first->done && !fo.first->failed) finish_request(fo.first, HSR_OK, now);
+        // guided requests whose iteration ended in this tick: its step has run, so the next
+        // iteration may be planned
+        for (const ReqPtr &q : t.stepping) {
+            if (status != 0) q->failed = true;
+            q->iter += 1;
+            q->iter_done = 0;
+            q->waiting = false;
+        }
         // failed requests release their accumulators once no queued tick uses them
         std::vector<ReqPtr> failed;
         for (const ReqPtr &q : active)
@@ -533,6 +671,7 @@ void hsr_server::complete_tick(TickSlot &t) {
     }
     t.members.clear();
     t.finishing.clear();
+    t.stepping.clear();
     cv_done.notify_all();
 }
 
@@ -567,7 +706,7 @@ void hsr_server::run() {
             if (int(inflight.size()) >= kTickSlots) return false;
             if (!queue.empty() && int(active.size()) < cfg.max_slots && !admission_blocked) return true;
             for (const ReqPtr &q : active)
-                if (!q->failed && !q->finalize_queued) return true;
+                if (!q->failed && !q->finalize_queued && !q->waiting) return true;
             return false;
         });
         if (stop && inflight.empty() && ticks_finished == completed) break;
@@ -632,8 +771,8 @@ hsr_status hsr_server_create(const hsr_server_config *cfg, hsr_server **out) {
     if (!(cfg->tick_ms > 0.f)) return serve_fail(HSR_ERR_INVALID_ARGUMENT, "tick_ms must be > 0");
     if (cfg->phase_mode != HSR_PHASE_REFERENCE_FP32 && cfg->phase_mode != HSR_PHASE_SPLIT_FP64)
         return serve_fail(HSR_ERR_INVALID_ARGUMENT, "unknown phase mode");
-    if (!cfg->flags.useGeometricalOptics || cfg->flags.doGuiding)
-        return serve_fail(HSR_ERR_NOT_SUPPORTED, "the server traces geometrical optics without guiding");
+    if (!cfg->flags.useGeometricalOptics)
+        return serve_fail(HSR_ERR_NOT_SUPPORTED, "the server traces geometrical optics");
     if (cfg->flags.maxDepth < 0) return serve_fail(HSR_ERR_INVALID_ARGUMENT, "maxDepth must be >= 0");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -655,9 +794,16 @@ hsr_status hsr_server_create(const hsr_server_config *cfg, hsr_server **out) {
             cudaGetLastError();
             return serve_fail(HSR_ERR_CUDA, "tick end events");
         }
+    s->guided = cfg->flags.doGuiding != 0;
     s->min_tick = int64_t(kTilesPerCta) * kServeTile * s->sm_count *
-                  wave_blocks_per_sm(cfg->max_samples_per_chirp, true);
+                  wave_blocks_per_sm(cfg->max_samples_per_chirp, true, s->guided);
     if (!dev_alloc(&s->d_arena, size_t(s->cfg.memory_bytes), err)) return serve_fail(HSR_ERR_OUT_OF_MEMORY, err);
+    if (s->guided) {
+        if (!dev_alloc(&s->d_guide, guide_bytes_per_pose() * size_t(cfg->max_slots) + 8 * 256, err))
+            return serve_fail(HSR_ERR_OUT_OF_MEMORY, "guiding trees: " + err);
+        s->guide = carve_guide(s->d_guide, cfg->max_slots);
+        for (int k = cfg->max_slots - 1; k >= 0; --k) s->free_trees.push_back(k);
+    }
     if ((e = cudaMemset(s->d_arena, 0, size_t(s->cfg.memory_bytes))) != cudaSuccess)
         return serve_fail(HSR_ERR_CUDA, std::string("arena clear: ") + cudaGetErrorString(e));
     s->arena.init(s->cfg.memory_bytes);

@@ -33,9 +33,12 @@ namespace {
 constexpr int kBM = 128;     // UMMA M
 constexpr int kBN = 256;     // UMMA N
 constexpr int kBK = 64;      // K per stage: 64 bf16 = 128 B rows (SWIZZLE_128B)
-constexpr int kStages = 4;
 constexpr int kStageA = kBM * kBK * 2;  // 16 KB
-constexpr int kStageB = kBN * kBK * 2;  // 32 KB
+constexpr int kStageB = kBN * kBK * 2;  // 32 KB per 256-column half
+// pipeline depth for a CTA computing kNH 256-column halves of its 128-row tile: the ring
+// of (A, kNH x B) stages within the 227 KB of shared memory
+template <int kNH> constexpr int umma_stages() { return kNH == 1 ? 4 : 2; }
+template <int kNH> constexpr int umma_smem() { return umma_stages<kNH>() * (kStageA + kNH * kStageB) + 1024 + 256; }
 constexpr unsigned kStatusSynthTimeout = 1u << 3;
 
 // ------------------------------------------------------------------------------------
@@ -129,15 +132,22 @@ __global__ void __launch_bounds__(256) k_sgemm_nt(const double *__restrict__ a, 
 
 // ------------------------------------------------------------------------------------
 // Tensor-core GEMM: tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM), operands
-// staged by TMA (128-byte swizzle), one 128 x 256 output tile per CTA.
+// staged by TMA (128-byte swizzle). A CTA computes a 128-row tile over kNH 256-column
+// halves (two FP32 accumulators of 256 TMEM columns each for kNH = 2), so its A tile is
+// fetched once for both halves. Its k-iterations are (k-tile, split product) pairs in
+// k-major order: the products x_i y_j of one k-tile follow each other, and the A term
+// tile a product shares with the previous one comes from L2. Split-K over grid.z; each
+// CTA writes its partial tile to its own slice of the partial buffer, which the
+// finalize sums over the slices in order (deterministic).
 // Warp 0 lane 0 issues TMA, warp 1 lane 0 issues MMA, all four warps run the epilogue.
 // ------------------------------------------------------------------------------------
 struct UmmaParams {
     int M, NC, KK;  // KK: padded reduction length of one product (multiple of 64)
-    float *c;
-    int ldc;
+    float *c;       // partial tiles [grid.z][Mpad][ldc]
+    int ldc;        // NCpad
+    int64_t slice;  // floats per split-K slice of c
     unsigned *status;
-    int chunk;      // k-iterations per CTA along grid.z (split-K); results are added into c
+    int chunk;      // k-iterations per CTA along grid.z (split-K)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -209,27 +219,29 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
                  : "memory");
 }
 
+template <int kNH>
 __global__ void __launch_bounds__(128, 1)
     k_umma_gemm(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
                 const __grid_constant__ CUtensorMap ta3, const __grid_constant__ CUtensorMap tb1,
                 const __grid_constant__ CUtensorMap tb2, const __grid_constant__ CUtensorMap tb3, UmmaParams gp) {
+    constexpr int kS = umma_stages<kNH>();
+    constexpr int kStage = kStageA + kNH * kStageB;
+    constexpr uint32_t kCols = uint32_t(kNH * kBN);  // TMEM columns: 256 or 512
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t *sa = smem;
-    uint8_t *sb = smem + kStages * kStageA;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sb + kStages * kStageB);  // full[4], empty[4], done
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kS * kStage);  // full[kS], empty[kS], done
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * kS + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * int(kCols);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                     "r"(kBN)
+                     "r"(kCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s < 2 * kStages + 1; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        for (int st = 0; st < 2 * kS + 1; ++st) mbar_init(smem_u32(&bars[st]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -249,36 +261,46 @@ __global__ void __launch_bounds__(128, 1)
         const CUtensorMap *am[3] = {&ta1, &ta2, &ta3};
         const CUtensorMap *bm[3] = {&tb1, &tb2, &tb3};
         for (int it = 0; it < total && ok; ++it) {
-            const int s = it % kStages, round = it / kStages;
-            if (it >= kStages) ok = mbar_wait(smem_u32(&bars[kStages + s]), uint32_t((round - 1) & 1), gp.status);
+            const int st = it % kS, round = it / kS;
+            if (it >= kS) ok = mbar_wait(smem_u32(&bars[kS + st]), uint32_t((round - 1) & 1), gp.status);
             if (!ok) break;
-            const uint32_t full = smem_u32(&bars[s]);
-            mbar_expect_tx(full, kStageA + kStageB);
-            const int pair = (it0 + it) / ktiles, kt = (it0 + it) % ktiles;
-            tma_load_2d(smem_u32(sa + s * kStageA), am[pa[pair]], kt * kBK, m0, full);
-            tma_load_2d(smem_u32(sb + s * kStageB), bm[pb[pair]], kt * kBK, n0, full);
+            const uint32_t full = smem_u32(&bars[st]);
+            mbar_expect_tx(full, kStage);
+            const int kt = (it0 + it) / 6, pair = (it0 + it) % 6;  // k-major: products of a k-tile adjacent
+            uint8_t *stage = smem + st * kStage;
+            tma_load_2d(smem_u32(stage), am[pa[pair]], kt * kBK, m0, full);
+#pragma unroll
+            for (int h = 0; h < kNH; ++h)
+                tma_load_2d(smem_u32(stage + kStageA + h * kStageB), bm[pb[pair]], kt * kBK, n0 + h * kBN, full);
         }
     } else if (warp == 1 && lane == 0) {
         for (int it = 0; it < total && ok; ++it) {
-            const int s = it % kStages, round = it / kStages;
-            ok = mbar_wait(smem_u32(&bars[s]), uint32_t(round & 1), gp.status);
+            const int st = it % kS, round = it / kS;
+            ok = mbar_wait(smem_u32(&bars[st]), uint32_t(round & 1), gp.status);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(sa + s * kStageA), b0 = smem_u32(sb + s * kStageB);
+            const uint32_t a0 = smem_u32(smem + st * kStage);
 #pragma unroll
-            for (int k = 0; k < kBK / 16; ++k)
-                umma(tmem, umma_desc(a0 + 32 * k), umma_desc(b0 + 32 * k), (it > 0 || k > 0) ? 1u : 0u);
-            umma_commit(smem_u32(&bars[kStages + s]));
+            for (int h = 0; h < kNH; ++h) {
+                const uint32_t b0 = a0 + kStageA + h * kStageB;
+#pragma unroll
+                for (int k = 0; k < kBK / 16; ++k)
+                    umma(tmem + uint32_t(h * kBN), umma_desc(a0 + 32 * k), umma_desc(b0 + 32 * k),
+                         (it > 0 || k > 0) ? 1u : 0u);
+            }
+            umma_commit(smem_u32(&bars[kS + st]));
         }
-        umma_commit(smem_u32(&bars[2 * kStages]));
+        umma_commit(smem_u32(&bars[2 * kS]));
     }
     __syncwarp();
-    // epilogue: each warp reads its 32 TMEM lanes (rows), 16 columns at a time
-    const bool done = mbar_wait(smem_u32(&bars[2 * kStages]), 0u, gp.status);
+    // epilogue: each warp reads its 32 TMEM lanes (rows), 16 columns at a time, into this
+    // CTA's slice of the partial buffer
+    const bool done = mbar_wait(smem_u32(&bars[2 * kS]), 0u, gp.status);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncwarp();
     const int row = m0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < kBN; c0 += 16) {
+    float *slice = gp.c + size_t(blockIdx.z) * size_t(gp.slice);
+    for (int c0 = 0; c0 < int(kCols); c0 += 16) {
         uint32_t r[16];
         const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
         asm volatile(
@@ -288,27 +310,33 @@ __global__ void __launch_bounds__(128, 1)
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (done && row < gp.M) {
-            float *dst = gp.c + size_t(row) * gp.ldc + n0 + c0;
+            float4 *dst = reinterpret_cast<float4 *>(slice + size_t(row) * gp.ldc + n0 + c0);
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-                if (n0 + c0 + j < gp.NC) atomicAdd(dst + j, __uint_as_float(r[j]));
+            for (int j = 0; j < 4; ++j)
+                dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                     __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
     }
 }
 
-// frame row m: C[p][m] + j C[p][N + m], divided by the pose's total weight
-__global__ void k_synth_finalize(const float *__restrict__ c, int P, int N, int ldc, const int64_t *__restrict__ budget,
-                                 float sample_weight, const double *__restrict__ tw, int normalise,
-                                 float *__restrict__ out) {
+// frame row m: C[p][m] + j C[p][N + m] (the sum of the split-K slices, in slice order),
+// divided by the pose's total weight
+__global__ void k_synth_finalize(const float *__restrict__ c, int slices, int64_t slice, int P, int N, int ldc,
+                                 const int64_t *__restrict__ budget, float sample_weight,
+                                 const double *__restrict__ tw, int normalise, float *__restrict__ out) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= int64_t(P) * N) return;
     const int p = int(i / N), m = int(i % N);
-    float re = c[size_t(p) * ldc + m], im = c[size_t(p) * ldc + N + m];
+    float re = 0.f, im = 0.f;
+    for (int z = 0; z < slices; ++z) {
+        re += c[size_t(z) * slice + size_t(p) * ldc + m];
+        im += c[size_t(z) * slice + size_t(p) * ldc + N + m];
+    }
     if (normalise) {
         const double w = tw ? tw[p] : double(budget[p]) * double(sample_weight);
         const float inv = 1.f / float(w);
@@ -415,9 +443,37 @@ void synth_free_operand(SynthOperand &op) {
     op = SynthOperand{};
 }
 
+namespace {
+
+// The tensor-core launch of one synthesis: 256-column halves per CTA (2 where the padded
+// output has them, within the 512 TMEM columns), CTAs along M and N, and split-K so that
+// the grid is about one CTA per SM (each CTA keeping at least 8 k-iterations).
+struct UmmaPlan {
+    int nh, mtiles, ngroups, split, chunk;
+};
+
+UmmaPlan umma_plan(const SynthOperand &op, int P) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    UmmaPlan u;
+    u.nh = op.NCpad >= 2 * kBN ? 2 : 1;
+    u.mtiles = (P + kBM - 1) / kBM;
+    u.ngroups = op.NCpad / (u.nh * kBN);
+    const int iters = 6 * (op.KKpad / kBK);
+    const int tiles = u.mtiles * u.ngroups;
+    u.split = std::max(1, std::min(sms / std::max(tiles, 1), iters / 8));
+    u.chunk = (iters + u.split - 1) / u.split;
+    u.split = (iters + u.chunk - 1) / u.chunk;  // every CTA gets at least one k-iteration
+    return u;
+}
+
+}  // namespace
+
 size_t synth_scratch_bytes(const SynthOperand &op, int P) {
     const int Mpad = (P + kBM - 1) / kBM * kBM;
-    return size_t(Mpad) * op.KKpad * 2 * 3 + size_t(P) * op.NCpad * 4 + 3 * 256;
+    const UmmaPlan u = umma_plan(op, P);
+    return size_t(Mpad) * op.KKpad * 2 * 3 + size_t(std::max(u.split, 1)) * Mpad * op.NCpad * 4 + 3 * 256;
 }
 
 // fine histograms (P x KK FP64 sums, row stride KK) -> frame rows (P x N complex64)
@@ -435,7 +491,9 @@ int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, 
     __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
     __nv_bfloat16 *a2 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
     __nv_bfloat16 *a3 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
-    float *c = reinterpret_cast<float *>(take(size_t(P) * op.NCpad * 4));
+    float *c = reinterpret_cast<float *>(p);  // the partial slices, [split][Mpad][NCpad]
+    const int64_t slice = int64_t(Mpad) * op.NCpad;
+    int slices = 1;
     if (engine == 0) {
         k_split3<<<unsigned((na + 255) / 256), 256, 0, st>>>(fine, P, op.KK, op.KK, Mpad, op.KKpad, a1, a2, a3);
         CUtensorMap ta[3], tb[3];
@@ -447,21 +505,17 @@ int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, 
                 return 2;
             }
         }
-        // split-K so that small batches still occupy the SMs: about two CTAs per SM
-        int dev = 0, sms = 148;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int tiles = (Mpad / kBM) * (op.NCpad / kBN);
-        const int iters = 6 * (op.KKpad / kBK);
-        int split = std::max(1, std::min(iters / 16, (2 * sms + tiles - 1) / tiles));
-        const int chunk = (iters + split - 1) / split;
-        split = (iters + chunk - 1) / chunk;  // every CTA gets at least one k-iteration
-        UmmaParams gp{P, 2 * op.N, op.KKpad, c, op.NCpad, status, chunk};
-        const int smem = kStages * (kStageA + kStageB) + 1024 + 256;
-        cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        cudaMemsetAsync(c, 0, size_t(P) * op.NCpad * 4, st);
-        dim3 grid(Mpad / kBM, op.NCpad / kBN, split);
-        k_umma_gemm<<<grid, 128, smem, st>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], gp);
+        const UmmaPlan u = umma_plan(op, P);
+        slices = u.split;
+        UmmaParams gp{P, 2 * op.N, op.KKpad, c, op.NCpad, slice, status, u.chunk};
+        dim3 grid(u.mtiles, u.ngroups, u.split);
+        if (u.nh == 2) {
+            cudaFuncSetAttribute(k_umma_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem<2>());
+            k_umma_gemm<2><<<grid, 128, umma_smem<2>(), st>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], gp);
+        } else {
+            cudaFuncSetAttribute(k_umma_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem<1>());
+            k_umma_gemm<1><<<grid, 128, umma_smem<1>(), st>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], gp);
+        }
         note_launches(2);
     } else {
         dim3 grid((2 * op.N + 63) / 64, (P + 63) / 64);
@@ -469,8 +523,8 @@ int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, 
         note_launches(1);
     }
     const int64_t n = int64_t(P) * op.N;
-    k_synth_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(c, P, op.N, op.NCpad, budget, sample_weight, tw,
-                                                                normalise, out_rows);
+    k_synth_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(c, slices, slice, P, op.N, op.NCpad, budget,
+                                                                sample_weight, tw, normalise, out_rows);
     note_launches(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

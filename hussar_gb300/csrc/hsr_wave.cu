@@ -6,15 +6,15 @@ namespace hsr {
 
 size_t wave_smem_bytes(int samples, bool guided) { return wave_smem_for<kWaveDefaultQueue>(samples, guided); }
 
-int wave_blocks_per_sm(int samples, bool mixed) {
+int wave_blocks_per_sm(int samples, bool mixed, bool guided) {
     int nb = 0;
     if (mixed) {
-        const size_t smem = wave_smem_for<kWaveSmallQueue>(samples, false);
+        const size_t smem = wave_smem_for<kWaveSmallQueue>(samples, guided);
         auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, true, kWaveSmallQueue>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);
     } else {
-        const size_t smem = wave_smem_bytes(samples, false);
+        const size_t smem = wave_smem_bytes(samples, guided);
         auto *k = k_wave<HSR_PHASE_REFERENCE_FP32, false, kWaveDefaultQueue>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kThreads, smem);

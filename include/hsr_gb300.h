@@ -468,7 +468,12 @@ hsr_status hsr_batch_graph_destroy(hsr_batch_graph *graph);
  * device memory for their accumulators are free. A request's result is the row
  * hsr_simulate_batch gives for the same scene, pose, chirp, budget and index offset
  * (the same Halton samples; only the summation order differs). The tracer flags and the
- * phase mode are per server; geometrical optics must be on and guiding off. A tick runs
+ * phase mode are per server; geometrical optics must be on. With flags.doGuiding every
+ * request runs PathTracer::run's guided schedule (path.h:171-224) across ticks over a
+ * guiding tree of the server (one per slot): an iteration's chunks share ticks with
+ * other requests, the tick that ends an iteration steps the request's tree, and the next
+ * iteration starts in a tick after it; the row equals hsr_simulate_batch's guided row up
+ * to the order of the float training sums. A tick runs
  * the larger path stack (GENERATE threshold 128) only when every scene in it was
  * autotuned (hsr_autotune_batch) to a threshold above 64, and larger work items when
  * its requests' chunks are large. */

@@ -184,8 +184,9 @@ private:
 /* A serving loop over resident scenes (hsr_server_*): requests from any thread, traced
  * in shared batching ticks. No counterpart in the reference, whose backends trace one
  * pose per synchronous run() (src/arch/gpu.cpp:499-532). The tracer flags come from an
- * integrator (its public flags of path.h:153-169; guiding must be off). A request's row
- * is the fetchFrame() row of a plain run of `budget` samples at index offset `offset`. */
+ * integrator (its public flags of path.h:153-169; with doGuiding every request runs the
+ * guided schedule). A request's row is the fetchFrame() row of a run of `budget`
+ * samples at index offset `offset`. */
 class Server {
 public:
     explicit Server(const hsr_server_config &config) { check(hsr_server_create(&config, &m_server)); }

@@ -109,5 +109,8 @@ def test_server_create_without_device(product_lib):
     assert cfg.flags.doGuiding == 0 and cfg.flags.useGeometricalOptics == 1 and cfg.flags.maxDepth == 10
     h = ctypes.c_void_p()
     assert product_lib.hsr_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.HSR_ERR_NO_DEVICE
+    # guided serving is supported; without geometrical optics the server refuses
     cfg.flags.doGuiding = 1
+    assert product_lib.hsr_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.HSR_ERR_NO_DEVICE
+    cfg.flags.useGeometricalOptics = 0
     assert product_lib.hsr_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.HSR_ERR_NOT_SUPPORTED
