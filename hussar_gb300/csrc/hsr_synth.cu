@@ -88,6 +88,45 @@ __global__ void k_split3(const T *__restrict__ x, int rows, int cols, int ld_in,
     o3[idx] = c3;
 }
 
+// The same split for the A operand, eight columns per thread: row r of the padded
+// output (blockIdx.y), columns 8 (blockIdx.x * blockDim.x + threadIdx.x) onwards; the
+// eight FP64 sums are read as four 16-byte loads and each term is stored as one 16-byte
+// chunk. cols_pad is a multiple of 8; every element of a chunk is either inside
+// [rows) x [cols) or padding (cols, the histogram length 64 N, is a multiple of 8).
+__global__ void k_split3_v8(const double *__restrict__ x, int rows, int cols, int ld_in, int cols_pad,
+                            __nv_bfloat16 *__restrict__ o1, __nv_bfloat16 *__restrict__ o2,
+                            __nv_bfloat16 *__restrict__ o3) {
+    const int r = blockIdx.y;
+    const int c = 8 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (c >= cols_pad) return;
+    float v[8];
+    if (r < rows && c < cols) {
+        const double2 *src = reinterpret_cast<const double2 *>(x + size_t(r) * ld_in + c);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double2 d = __ldg(src + j);
+            v[2 * j] = float(d.x);
+            v[2 * j + 1] = float(d.y);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = 0.f;
+    }
+    __align__(16) __nv_bfloat16 t1[8], t2[8], t3[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        t1[j] = __float2bfloat16_rn(v[j]);
+        const float r1 = v[j] - __bfloat162float(t1[j]);
+        t2[j] = __float2bfloat16_rn(r1);
+        const float r2 = r1 - __bfloat162float(t2[j]);
+        t3[j] = __float2bfloat16_rn(r2);
+    }
+    const size_t o = size_t(r) * cols_pad + c;
+    *reinterpret_cast<uint4 *>(o1 + o) = *reinterpret_cast<const uint4 *>(t1);
+    *reinterpret_cast<uint4 *>(o2 + o) = *reinterpret_cast<const uint4 *>(t2);
+    *reinterpret_cast<uint4 *>(o3 + o) = *reinterpret_cast<const uint4 *>(t3);
+}
+
 // ------------------------------------------------------------------------------------
 // CUDA-core FP32 GEMM (cross-check and small batches): C[M x NC] = A[M x KK] * B,
 // with B given transposed (bt[NC x KK]).
@@ -495,7 +534,8 @@ int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, 
     const int64_t slice = int64_t(Mpad) * op.NCpad;
     int slices = 1;
     if (engine == 0) {
-        k_split3<<<unsigned((na + 255) / 256), 256, 0, st>>>(fine, P, op.KK, op.KK, Mpad, op.KKpad, a1, a2, a3);
+        const dim3 sg(unsigned((op.KKpad / 8 + 255) / 256), unsigned(Mpad));
+        k_split3_v8<<<sg, 256, 0, st>>>(fine, P, op.KK, op.KK, op.KKpad, a1, a2, a3);
         CUtensorMap ta[3], tb[3];
         const void *as[3] = {a1, a2, a3};
         const void *bs[3] = {op.b1, op.b2, op.b3};
