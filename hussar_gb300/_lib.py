@@ -151,6 +151,8 @@ def lib():
         "hsr_guide_reset": [vp],
         "hsr_guide_step": [vp],
         "hsr_guide_destroy": [vp],
+        "hsr_guide_read": [vp, P(ctypes.c_int32), vp, vp, vp, vp],
+        "hsr_guide_write": [vp, ctypes.c_int32, vp, vp, vp, vp],
         "hsr_backend_run_guided": [vp, P(RFConfigC), P(FrameConfigC), P(AntennaC), P(AntennaC), P(FlagsC),
                                    ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_int32, vp,
                                    ctypes.c_int32, vp, P(ctypes.c_double), vp],

@@ -466,5 +466,67 @@ class _GB300:
             _lib.check(_lib.lib().hsr_last_kernel_ms(self._scene, ctypes.byref(out)))
             return out.value
 
+    class Guide:
+        """A device guiding tree on a backend's scene (hsr_guide_*): GuidingWrapper's
+        reset/step (path.h:47-50, 119-126) plus one guided iteration of PathTracer::run
+        (hsr_backend_run_guided) into an integrator's frame."""
+
+        MAX_NODES = 2048
+
+        def __init__(self, backend):
+            h = ctypes.c_void_p()
+            _lib.check(_lib.lib().hsr_guide_create(backend.handle, ctypes.byref(h)))
+            self._h = h
+            self._backend = backend
+
+        def close(self):
+            if self._h is not None and self._h.value:
+                _lib.lib().hsr_guide_destroy(self._h)
+                self._h = None
+
+        def __del__(self):
+            try:
+                self.close()
+            except Exception:
+                pass
+
+        def reset(self):
+            _lib.check(_lib.lib().hsr_guide_reset(self._h))
+
+        def step(self):
+            _lib.check(_lib.lib().hsr_guide_step(self._h))
+
+        def read(self):
+            """(count, samp_child, samp_p, train_child, train_acc2) as host arrays."""
+            n = self.MAX_NODES
+            sc, sp = np.zeros(n, np.int32), np.zeros(n, np.float32)
+            tc, acc = np.zeros(n, np.int32), np.zeros(n, np.float32)
+            cnt = ctypes.c_int32()
+            _lib.check(_lib.lib().hsr_guide_read(self._h, ctypes.byref(cnt), _lib.ptr(sc), _lib.ptr(sp),
+                                                 _lib.ptr(tc), _lib.ptr(acc)))
+            return cnt.value, sc, sp, tc, acc
+
+        def write(self, count, samp_child, samp_p, train_child, train_acc2):
+            arr = [np.ascontiguousarray(samp_child, np.int32), np.ascontiguousarray(samp_p, np.float32),
+                   np.ascontiguousarray(train_child, np.int32), np.ascontiguousarray(train_acc2, np.float32)]
+            if any(len(a) != self.MAX_NODES for a in arr):
+                raise ValueError("guide arrays hold %d entries" % self.MAX_NODES)
+            _lib.check(_lib.lib().hsr_guide_write(self._h, int(count), *(_lib.ptr(a) for a in arr)))
+
+        def run_iteration(self, integrator, scene, budget, train):
+            """One guided backend run: samples integrator.sampleIndexOffset + [0, budget)
+            with the integrator's sample weight, added into its frame and total weight."""
+            it = integrator
+            fc = it.frame.config()
+            buf = np.ascontiguousarray(it.frame.data.view(np.float32).reshape(-1))
+            tw = ctypes.c_double(it.totalWeight)
+            _lib.check(_lib.lib().hsr_backend_run_guided(
+                self._backend.handle, ctypes.byref(scene.rfConfig.to_c()), ctypes.byref(fc.to_c()),
+                ctypes.byref(scene.tx.to_c()), ctypes.byref(scene.rx.to_c()), ctypes.byref(it.flags_c()),
+                int(budget), int(it.sampleIndexOffset), float(it.currentSampleWeight), 1 if train else 0, self._h,
+                int(it.phaseMode), _lib.ptr(buf), ctypes.byref(tw), None))
+            it.frame.data = buf.view(np.complex64).reshape(it.frame.data.shape)
+            it.totalWeight = tw.value
+
 
 gb300 = _GB300()

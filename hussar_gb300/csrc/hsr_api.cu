@@ -834,6 +834,50 @@ hsr_status hsr_guide_step(hsr_guide *g) {
     return e == cudaSuccess ? HSR_OK : cuda_fail(e, "guide step");
 }
 
+hsr_status hsr_guide_read(hsr_guide *g, int32_t *out_count, int32_t *samp_child, float *samp_p,
+                          int32_t *train_child, float *train_acc2) {
+    if (!g || !out_count || !samp_child || !samp_p || !train_child || !train_acc2)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<float> acc(3 * size_t(kGuideMaxNodes));
+    int count = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(samp_child, g->g.samp_child, 4 * size_t(kGuideMaxNodes), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(samp_p, g->g.samp_p, 4 * size_t(kGuideMaxNodes), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(train_child, g->g.train_child, 4 * size_t(kGuideMaxNodes), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(acc.data(), g->g.train_acc, 4 * acc.size(), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&count, g->g.train_count, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "guide read");
+    for (int i = 0; i < kGuideMaxNodes; ++i) train_acc2[i] = acc[3 * size_t(i) + 2];
+    *out_count = count;
+    return HSR_OK;
+}
+
+hsr_status hsr_guide_write(hsr_guide *g, int32_t count, const int32_t *samp_child, const float *samp_p,
+                           const int32_t *train_child, const float *train_acc2) {
+    if (!g || !samp_child || !samp_p || !train_child || !train_acc2)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    if (count < 1 || count > kGuideMaxNodes)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "node count outside 1.." + std::to_string(kGuideMaxNodes));
+    // every link must name a child pair inside the array: the device descents and the
+    // step index through them
+    for (int i = 0; i < kGuideMaxNodes; ++i)
+        if (samp_child[i] < -1 || samp_child[i] + 1 >= kGuideMaxNodes || (samp_child[i] >= 0 && samp_child[i] <= i) ||
+            train_child[i] < -1 || train_child[i] + 1 >= kGuideMaxNodes ||
+            (train_child[i] >= 0 && train_child[i] <= i))
+            return fail(HSR_ERR_INVALID_ARGUMENT, "node " + std::to_string(i) + ": child link out of range");
+    std::vector<float> acc(3 * size_t(kGuideMaxNodes), 0.f);
+    for (int i = 0; i < kGuideMaxNodes; ++i) acc[3 * size_t(i) + 2] = train_acc2[i];
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(g->g.samp_child, samp_child, 4 * size_t(kGuideMaxNodes), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(g->g.samp_p, samp_p, 4 * size_t(kGuideMaxNodes), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(g->g.train_child, train_child, 4 * size_t(kGuideMaxNodes), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(g->g.train_acc, acc.data(), 4 * acc.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(g->g.train_count, &count, sizeof(int), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? HSR_OK : cuda_fail(e, "guide write");
+}
+
 hsr_status hsr_guide_destroy(hsr_guide *g) {
     if (!g) return HSR_OK;
     cudaDeviceSynchronize();

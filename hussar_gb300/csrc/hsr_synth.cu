@@ -15,7 +15,9 @@
 // As a real GEMM: C[P x 2N] = A[P x 8K] * B[8K x 2N] with A = [Re h0..h3 | Im h0..h3]
 // and B = [[Re G, Im G], [-Im G, Re G]]. On the tensor cores (tcgen05.mma kind::f16) both
 // operands are split into three BF16 terms (x = x1 + x2 + x3) and the six products
-// x1y1 + x1y2 + x2y1 + x1y3 + x2y2 + x3y1 accumulate in FP32 in tensor memory.
+// x1y1 + x1y2 + x2y1 + x1y3 + x2y2 + x3y1 accumulate in FP32 in tensor memory. B's terms
+// are built once per N and cached; A's are formed inside the GEMM from the FP64
+// histogram rows (one read of the histogram, no BF16 copy of A in memory).
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -35,10 +37,15 @@ constexpr int kBN = 256;     // UMMA N
 constexpr int kBK = 64;      // K per stage: 64 bf16 = 128 B rows (SWIZZLE_128B)
 constexpr int kStageA = kBM * kBK * 2;  // 16 KB
 constexpr int kStageB = kBN * kBK * 2;  // 32 KB per 256-column half
-// pipeline depth for a CTA computing kNH 256-column halves of its 128-row tile: the ring
-// of (A, kNH x B) stages within the 227 KB of shared memory
-template <int kNH> constexpr int umma_stages() { return kNH == 1 ? 4 : 2; }
-template <int kNH> constexpr int umma_smem() { return umma_stages<kNH>() * (kStageA + kNH * kStageB) + 1024 + 256; }
+constexpr int kConvWarps = 8;           // warps forming the A terms (and running the epilogue)
+constexpr int kUmmaThreads = 32 * (2 + kConvWarps);
+// Shared memory of a CTA computing kNH 256-column halves of its 128-row tile: the three
+// A terms of two k-tiles (double buffer, 96 KB) and a ring of B stages (one B term over
+// the kNH halves per stage) filling the rest of the 227 KB.
+template <int kNH> constexpr int umma_bstages() { return kNH == 1 ? 4 : 2; }
+template <int kNH> constexpr int umma_smem() {
+    return 2 * 3 * kStageA + umma_bstages<kNH>() * kNH * kStageB + 1024 + 256;
+}
 constexpr unsigned kStatusSynthTimeout = 1u << 3;
 
 // ------------------------------------------------------------------------------------
@@ -88,45 +95,6 @@ __global__ void k_split3(const T *__restrict__ x, int rows, int cols, int ld_in,
     o3[idx] = c3;
 }
 
-// The same split for the A operand, eight columns per thread: row r of the padded
-// output (blockIdx.y), columns 8 (blockIdx.x * blockDim.x + threadIdx.x) onwards; the
-// eight FP64 sums are read as four 16-byte loads and each term is stored as one 16-byte
-// chunk. cols_pad is a multiple of 8; every element of a chunk is either inside
-// [rows) x [cols) or padding (cols, the histogram length 64 N, is a multiple of 8).
-__global__ void k_split3_v8(const double *__restrict__ x, int rows, int cols, int ld_in, int cols_pad,
-                            __nv_bfloat16 *__restrict__ o1, __nv_bfloat16 *__restrict__ o2,
-                            __nv_bfloat16 *__restrict__ o3) {
-    const int r = blockIdx.y;
-    const int c = 8 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (c >= cols_pad) return;
-    float v[8];
-    if (r < rows && c < cols) {
-        const double2 *src = reinterpret_cast<const double2 *>(x + size_t(r) * ld_in + c);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const double2 d = __ldg(src + j);
-            v[2 * j] = float(d.x);
-            v[2 * j + 1] = float(d.y);
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) v[j] = 0.f;
-    }
-    __align__(16) __nv_bfloat16 t1[8], t2[8], t3[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        t1[j] = __float2bfloat16_rn(v[j]);
-        const float r1 = v[j] - __bfloat162float(t1[j]);
-        t2[j] = __float2bfloat16_rn(r1);
-        const float r2 = r1 - __bfloat162float(t2[j]);
-        t3[j] = __float2bfloat16_rn(r2);
-    }
-    const size_t o = size_t(r) * cols_pad + c;
-    *reinterpret_cast<uint4 *>(o1 + o) = *reinterpret_cast<const uint4 *>(t1);
-    *reinterpret_cast<uint4 *>(o2 + o) = *reinterpret_cast<const uint4 *>(t2);
-    *reinterpret_cast<uint4 *>(o3 + o) = *reinterpret_cast<const uint4 *>(t3);
-}
-
 // ------------------------------------------------------------------------------------
 // CUDA-core FP32 GEMM (cross-check and small batches): C[M x NC] = A[M x KK] * B,
 // with B given transposed (bt[NC x KK]).
@@ -170,23 +138,29 @@ __global__ void __launch_bounds__(256) k_sgemm_nt(const double *__restrict__ a, 
 }
 
 // ------------------------------------------------------------------------------------
-// Tensor-core GEMM: tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM), operands
-// staged by TMA (128-byte swizzle). A CTA computes a 128-row tile over kNH 256-column
-// halves (two FP32 accumulators of 256 TMEM columns each for kNH = 2), so its A tile is
-// fetched once for both halves. Its k-iterations are (k-tile, split product) pairs in
-// k-major order: the products x_i y_j of one k-tile follow each other, and the A term
-// tile a product shares with the previous one comes from L2. Split-K over grid.z; each
-// CTA writes its partial tile to its own slice of the partial buffer, which the
-// finalize sums over the slices in order (deterministic).
-// Warp 0 lane 0 issues TMA, warp 1 lane 0 issues MMA, all four warps run the epilogue.
+// Tensor-core GEMM: tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in TMEM). A CTA computes
+// a 128-row tile over kNH 256-column halves (two FP32 accumulators of 256 TMEM columns
+// each for kNH = 2) over a range of k-tiles (split-K over grid.z).
+//   warps 2..9 (converters): per k-tile, read the tile's FP64 histogram sums (128 rows x
+//     64 columns, one coalesced 512-byte row per warp load), split each into three BF16
+//     terms and store them in shared memory in the 128-byte-swizzled K-major layout the
+//     MMA descriptors expect (a double buffer of the three term tiles);
+//   warp 0 lane 0: TMA loads of B's terms (one term over the kNH halves per ring stage);
+//   warp 1 lane 0: per k-tile, for B term j = 1, 2, 3, the MMAs of the A terms i with
+//     i + j <= 4 (the six products), then commits that free the B stage and, after the
+//     third term, the A buffer.
+// Each CTA writes its partial tile to its own slice of the partial buffer, which the
+// finalize sums over the slices in order (deterministic). The converter warps run the
+// epilogue (TMEM lane quarter = warp % 4, two warps per quarter on half the columns each).
 // ------------------------------------------------------------------------------------
 struct UmmaParams {
-    int M, NC, KK;  // KK: padded reduction length of one product (multiple of 64)
-    float *c;       // partial tiles [grid.z][Mpad][ldc]
-    int ldc;        // NCpad
-    int64_t slice;  // floats per split-K slice of c
+    const double *a;  // fine histograms: M rows of lda FP64, reduction columns [0, K)
+    int M, lda, K;    // K: reduction length (multiple of 64)
+    float *c;         // partial tiles [grid.z][Mpad][ldc]
+    int ldc;          // NCpad
+    int64_t slice;    // floats per split-K slice of c
     unsigned *status;
-    int chunk;      // k-iterations per CTA along grid.z (split-K)
+    int chunk;        // k-tiles per CTA along grid.z (split-K)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -258,20 +232,41 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// the three BF16 terms of two FP32 values, packed in pairs (first value in the low half)
+__device__ __forceinline__ void split3_pair(double x0, double x1, uint32_t &t1, uint32_t &t2, uint32_t &t3) {
+    const float v0 = float(x0), v1 = float(x1);
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v0, v1);
+    const float r0 = v0 - __low2float(a), r1 = v1 - __high2float(a);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(r0, r1);
+    const __nv_bfloat162 c = __floats2bfloat162_rn(r0 - __low2float(b), r1 - __high2float(b));
+    t1 = *reinterpret_cast<const uint32_t *>(&a);
+    t2 = *reinterpret_cast<const uint32_t *>(&b);
+    t3 = *reinterpret_cast<const uint32_t *>(&c);
+}
+
 template <int kNH>
-__global__ void __launch_bounds__(128, 1)
-    k_umma_gemm(const __grid_constant__ CUtensorMap ta1, const __grid_constant__ CUtensorMap ta2,
-                const __grid_constant__ CUtensorMap ta3, const __grid_constant__ CUtensorMap tb1,
-                const __grid_constant__ CUtensorMap tb2, const __grid_constant__ CUtensorMap tb3, UmmaParams gp) {
-    constexpr int kS = umma_stages<kNH>();
-    constexpr int kStage = kStageA + kNH * kStageB;
+__global__ void __launch_bounds__(kUmmaThreads, 1)
+    k_umma_gemm(const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2,
+                const __grid_constant__ CUtensorMap tb3, UmmaParams gp) {
+    constexpr int kSB = umma_bstages<kNH>();
+    constexpr int kBStage = kNH * kStageB;
     constexpr uint32_t kCols = uint32_t(kNH * kBN);  // TMEM columns: 256 or 512
+    constexpr int kRowsPerWarp = kBM / kConvWarps;   // 16
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kS * kStage);  // full[kS], empty[kS], done
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(bars + 2 * kS + 1);
+    uint8_t *abuf = smem;                 // [2][3][kStageA]
+    uint8_t *bbuf = smem + 6 * kStageA;   // [kSB][kBStage]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(bbuf + kSB * kBStage);
+    uint64_t *bfull = bars, *bempty = bars + kSB, *afull = bars + 2 * kSB, *aempty = afull + 2, *done = aempty + 2;
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(done + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * int(kCols);
+    const int kt0 = blockIdx.z * gp.chunk;
+    const int nk = min(gp.K / kBK, kt0 + gp.chunk) - kt0;  // >= 1 by the host's choice of chunk
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
@@ -280,80 +275,144 @@ __global__ void __launch_bounds__(128, 1)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        for (int st = 0; st < 2 * kS + 1; ++st) mbar_init(smem_u32(&bars[st]), 1);
+        for (int s = 0; s < kSB; ++s) {
+            mbar_init(smem_u32(&bfull[s]), 1);
+            mbar_init(smem_u32(&bempty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&afull[b]), 32 * kConvWarps);
+            mbar_init(smem_u32(&aempty[b]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_holder;
-
-    const int ktiles = gp.KK / kBK;
-    const int it0 = blockIdx.z * gp.chunk;
-    const int it1 = min(6 * ktiles, it0 + gp.chunk);
-    const int total = it1 - it0;  // >= 1 by the host's choice of chunk
-    // products x_i y_j of the three-term splits: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
-    const int pa[6] = {0, 0, 1, 0, 1, 2};
-    const int pb[6] = {0, 1, 0, 2, 1, 0};
     bool ok = true;
 
-    if (warp == 0 && lane == 0) {
-        const CUtensorMap *am[3] = {&ta1, &ta2, &ta3};
-        const CUtensorMap *bm[3] = {&tb1, &tb2, &tb3};
-        for (int it = 0; it < total && ok; ++it) {
-            const int st = it % kS, round = it / kS;
-            if (it >= kS) ok = mbar_wait(smem_u32(&bars[kS + st]), uint32_t((round - 1) & 1), gp.status);
-            if (!ok) break;
-            const uint32_t full = smem_u32(&bars[st]);
-            mbar_expect_tx(full, kStage);
-            const int kt = (it0 + it) / 6, pair = (it0 + it) % 6;  // k-major: products of a k-tile adjacent
-            uint8_t *stage = smem + st * kStage;
-            tma_load_2d(smem_u32(stage), am[pa[pair]], kt * kBK, m0, full);
+    if (warp == 0) {
+        if (lane == 0) {
+            const CUtensorMap *bm[3] = {&tb1, &tb2, &tb3};
+            int n = 0;  // B stages issued
+            for (int t = 0; t < nk && ok; ++t) {
+                for (int j = 0; j < 3; ++j, ++n) {
+                    const int s = n % kSB;
+                    if (n >= kSB) ok = mbar_wait(smem_u32(&bempty[s]), uint32_t((n / kSB - 1) & 1), gp.status);
+                    if (!ok) break;
+                    const uint32_t full = smem_u32(&bfull[s]);
+                    mbar_expect_tx(full, kBStage);
 #pragma unroll
-            for (int h = 0; h < kNH; ++h)
-                tma_load_2d(smem_u32(stage + kStageA + h * kStageB), bm[pb[pair]], kt * kBK, n0 + h * kBN, full);
-        }
-    } else if (warp == 1 && lane == 0) {
-        for (int it = 0; it < total && ok; ++it) {
-            const int st = it % kS, round = it / kS;
-            ok = mbar_wait(smem_u32(&bars[st]), uint32_t(round & 1), gp.status);
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(smem + st * kStage);
-#pragma unroll
-            for (int h = 0; h < kNH; ++h) {
-                const uint32_t b0 = a0 + kStageA + h * kStageB;
-#pragma unroll
-                for (int k = 0; k < kBK / 16; ++k)
-                    umma(tmem + uint32_t(h * kBN), umma_desc(a0 + 32 * k), umma_desc(b0 + 32 * k),
-                         (it > 0 || k > 0) ? 1u : 0u);
+                    for (int h = 0; h < kNH; ++h)
+                        tma_load_2d(smem_u32(bbuf + s * kBStage + h * kStageB), bm[j], (kt0 + t) * kBK,
+                                    n0 + h * kBN, full);
+                }
             }
-            umma_commit(smem_u32(&bars[kS + st]));
+            // every load this thread issued has landed before the CTA can exit (bounded)
+            for (int s = 0; s < kSB && s < n; ++s) {
+                const int last = n - 1 - ((n - 1 - s) % kSB);
+                mbar_wait(smem_u32(&bfull[s]), uint32_t((last / kSB) & 1), gp.status);
+            }
         }
-        umma_commit(smem_u32(&bars[2 * kS]));
-    }
-    __syncwarp();
-    // epilogue: each warp reads its 32 TMEM lanes (rows), 16 columns at a time, into this
-    // CTA's slice of the partial buffer
-    const bool done = mbar_wait(smem_u32(&bars[2 * kS]), 0u, gp.status);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncwarp();
-    const int row = m0 + warp * 32 + lane;
-    float *slice = gp.c + size_t(blockIdx.z) * size_t(gp.slice);
-    for (int c0 = 0; c0 < int(kCols); c0 += 16) {
-        uint32_t r[16];
-        const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (done && row < gp.M) {
-            float4 *dst = reinterpret_cast<float4 *>(slice + size_t(row) * gp.ldc + n0 + c0);
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int n = 0;  // B stages consumed
+            for (int t = 0; t < nk && ok; ++t) {
+                const int ab = t & 1;
+                ok = mbar_wait(smem_u32(&afull[ab]), uint32_t((t >> 1) & 1), gp.status);
+                if (!ok) break;
+                for (int j = 0; j < 3; ++j, ++n) {
+                    const int s = n % kSB;
+                    ok = mbar_wait(smem_u32(&bfull[s]), uint32_t((n / kSB) & 1), gp.status);
+                    if (!ok) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t b0 = smem_u32(bbuf + s * kBStage);
+                    for (int i = 0; i + j < 3; ++i) {
+                        const uint32_t a0 = smem_u32(abuf + (ab * 3 + i) * kStageA);
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
-                                     __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+                        for (int h = 0; h < kNH; ++h) {
+#pragma unroll
+                            for (int k = 0; k < kBK / 16; ++k)
+                                umma(tmem + uint32_t(h * kBN), umma_desc(a0 + 32 * k),
+                                     umma_desc(b0 + h * kStageB + 32 * k), (t | j | i | k) ? 1u : 0u);
+                        }
+                    }
+                    umma_commit(smem_u32(&bempty[s]));
+                }
+                if (ok) umma_commit(smem_u32(&aempty[ab]));
+            }
+            umma_commit(smem_u32(done));
+        }
+    } else {
+        // converters: lane l holds columns 2l, 2l+1 of a row, i.e. 4 bytes of the row's
+        // 16-byte chunk l / 4; the chunk sits at position (l / 4) ^ (row % 8) of the
+        // 128-byte row (SWIZZLE_128B: 8-row groups 1024 B apart, tile base 1024-aligned).
+        // The loads of k-tile t + 1 are issued before k-tile t is converted, so that a
+        // whole tile of the histogram is in flight while the last one is split.
+        const int rbase = (warp - 2) * kRowsPerWarp;
+        const uint32_t lane_off = uint32_t(lane & 3) * 4;
+        double2 cur[kRowsPerWarp], nxt[kRowsPerWarp];
+        auto load_tile = [&](int t, double2 (&v)[kRowsPerWarp]) {
+            const int col = (kt0 + t) * kBK + 2 * lane;
+#pragma unroll
+            for (int u = 0; u < kRowsPerWarp; ++u) {
+                const int row = m0 + rbase + u;
+                v[u] = (row < gp.M) ? __ldg(reinterpret_cast<const double2 *>(gp.a + size_t(row) * gp.lda + col))
+                                    : make_double2(0.0, 0.0);
+            }
+        };
+        load_tile(0, cur);
+        for (int t = 0; t < nk && ok; ++t) {
+            const int ab = t & 1;
+            if (t + 1 < nk) load_tile(t + 1, nxt);
+            // the buffer is free once the MMAs of k-tile t - 2 completed
+            if (t >= 2) ok = mbar_wait(smem_u32(&aempty[ab]), uint32_t(((t >> 1) - 1) & 1), gp.status);
+            if (!ok) break;
+            uint8_t *at = abuf + ab * 3 * kStageA;
+#pragma unroll
+            for (int u = 0; u < kRowsPerWarp; ++u) {
+                const int r = rbase + u;
+                uint32_t w1, w2, w3;
+                split3_pair(cur[u].x, cur[u].y, w1, w2, w3);
+                const uint32_t off = uint32_t(r) * 128u + ((uint32_t((lane >> 2) ^ (r & 7))) << 4) + lane_off;
+                *reinterpret_cast<uint32_t *>(at + off) = w1;
+                *reinterpret_cast<uint32_t *>(at + kStageA + off) = w2;
+                *reinterpret_cast<uint32_t *>(at + 2 * kStageA + off) = w3;
+            }
+            // the generic-proxy stores become visible to the tensor cores' async proxy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_u32(&afull[ab]));
+#pragma unroll
+            for (int u = 0; u < kRowsPerWarp; ++u) cur[u] = nxt[u];
+        }
+        // epilogue: this warp's 32 TMEM lanes (rows, quarter warp % 4) over its half of the
+        // columns (two converter warps share a quarter), 16 columns at a time, into this
+        // CTA's slice of the partial buffer
+        const int quarter = warp & 3;
+        const int cbeg = ((warp - 2) / 4) * int(kCols / 2);
+        const bool fin = mbar_wait(smem_u32(done), 0u, gp.status);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        __syncwarp();
+        const int row = m0 + quarter * 32 + lane;
+        float *slice = gp.c + size_t(blockIdx.z) * size_t(gp.slice);
+        for (int c0 = cbeg; c0 < cbeg + int(kCols / 2); c0 += 16) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(c0);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (fin && row < gp.M) {
+                float4 *dst = reinterpret_cast<float4 *>(slice + size_t(row) * gp.ldc + n0 + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    dst[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
+                                         __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -485,8 +544,8 @@ void synth_free_operand(SynthOperand &op) {
 namespace {
 
 // The tensor-core launch of one synthesis: 256-column halves per CTA (2 where the padded
-// output has them, within the 512 TMEM columns), CTAs along M and N, and split-K so that
-// the grid is about one CTA per SM (each CTA keeping at least 8 k-iterations).
+// output has them, within the 512 TMEM columns), CTAs along M and N, and split-K over the
+// k-tiles so that the grid is about one CTA per SM (each CTA keeping at least 2 k-tiles).
 struct UmmaPlan {
     int nh, mtiles, ngroups, split, chunk;
 };
@@ -499,11 +558,11 @@ UmmaPlan umma_plan(const SynthOperand &op, int P) {
     u.nh = op.NCpad >= 2 * kBN ? 2 : 1;
     u.mtiles = (P + kBM - 1) / kBM;
     u.ngroups = op.NCpad / (u.nh * kBN);
-    const int iters = 6 * (op.KKpad / kBK);
+    const int ktiles = op.KKpad / kBK;
     const int tiles = u.mtiles * u.ngroups;
-    u.split = std::max(1, std::min(sms / std::max(tiles, 1), iters / 8));
-    u.chunk = (iters + u.split - 1) / u.split;
-    u.split = (iters + u.chunk - 1) / u.chunk;  // every CTA gets at least one k-iteration
+    u.split = std::max(1, std::min(sms / std::max(tiles, 1), ktiles / 2));
+    u.chunk = (ktiles + u.split - 1) / u.split;
+    u.split = (ktiles + u.chunk - 1) / u.chunk;  // every CTA gets at least one k-tile
     return u;
 }
 
@@ -512,7 +571,7 @@ UmmaPlan umma_plan(const SynthOperand &op, int P) {
 size_t synth_scratch_bytes(const SynthOperand &op, int P) {
     const int Mpad = (P + kBM - 1) / kBM * kBM;
     const UmmaPlan u = umma_plan(op, P);
-    return size_t(Mpad) * op.KKpad * 2 * 3 + size_t(std::max(u.split, 1)) * Mpad * op.NCpad * 4 + 3 * 256;
+    return size_t(std::max(u.split, 1)) * Mpad * op.NCpad * 4 + 256;
 }
 
 // fine histograms (P x KK FP64 sums, row stride KK) -> frame rows (P x N complex64)
@@ -520,43 +579,34 @@ int synth_run(const SynthOperand &op, const double *fine, int P, void *scratch, 
               float sample_weight, const double *tw, int normalise, float *out_rows, unsigned *status, cudaStream_t st,
               std::string &err) {
     const int Mpad = (P + kBM - 1) / kBM * kBM;
-    char *p = static_cast<char *>(scratch);
-    auto take = [&](size_t bytes) {
-        char *r = p;
-        p += (bytes + 255) & ~size_t(255);
-        return r;
-    };
-    const size_t na = size_t(Mpad) * op.KKpad;
-    __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
-    __nv_bfloat16 *a2 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
-    __nv_bfloat16 *a3 = reinterpret_cast<__nv_bfloat16 *>(take(na * 2));
-    float *c = reinterpret_cast<float *>(p);  // the partial slices, [split][Mpad][NCpad]
+    float *c = static_cast<float *>(scratch);  // the partial slices, [split][Mpad][NCpad]
     const int64_t slice = int64_t(Mpad) * op.NCpad;
     int slices = 1;
     if (engine == 0) {
-        const dim3 sg(unsigned((op.KKpad / 8 + 255) / 256), unsigned(Mpad));
-        k_split3_v8<<<sg, 256, 0, st>>>(fine, P, op.KK, op.KK, op.KKpad, a1, a2, a3);
-        CUtensorMap ta[3], tb[3];
-        const void *as[3] = {a1, a2, a3};
+        if (op.KK != op.KKpad || (reinterpret_cast<uintptr_t>(fine) & 15) != 0) {
+            err = "synthesis: histogram rows must be whole k-tiles on a 16-byte boundary";
+            return 1;
+        }
+        CUtensorMap tb[3];
         const void *bs[3] = {op.b1, op.b2, op.b3};
         for (int i = 0; i < 3; ++i) {
-            if (!make_map(&ta[i], as[i], Mpad, op.KKpad, kBM) || !make_map(&tb[i], bs[i], op.NCpad, op.KKpad, kBN)) {
+            if (!make_map(&tb[i], bs[i], op.NCpad, op.KKpad, kBN)) {
                 err = "cuTensorMapEncodeTiled failed";
                 return 2;
             }
         }
         const UmmaPlan u = umma_plan(op, P);
         slices = u.split;
-        UmmaParams gp{P, 2 * op.N, op.KKpad, c, op.NCpad, slice, status, u.chunk};
+        UmmaParams gp{fine, P, op.KK, op.KKpad, c, op.NCpad, slice, status, u.chunk};
         dim3 grid(u.mtiles, u.ngroups, u.split);
         if (u.nh == 2) {
             cudaFuncSetAttribute(k_umma_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem<2>());
-            k_umma_gemm<2><<<grid, 128, umma_smem<2>(), st>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], gp);
+            k_umma_gemm<2><<<grid, kUmmaThreads, umma_smem<2>(), st>>>(tb[0], tb[1], tb[2], gp);
         } else {
             cudaFuncSetAttribute(k_umma_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem<1>());
-            k_umma_gemm<1><<<grid, 128, umma_smem<1>(), st>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], gp);
+            k_umma_gemm<1><<<grid, kUmmaThreads, umma_smem<1>(), st>>>(tb[0], tb[1], tb[2], gp);
         }
-        note_launches(2);
+        note_launches(1);
     } else {
         dim3 grid((2 * op.N + 63) / 64, (P + 63) / 64);
         k_sgemm_nt<<<grid, 256, 0, st>>>(fine, op.bt, P, 2 * op.N, op.KK, op.KK, op.KKpad, c, op.NCpad);

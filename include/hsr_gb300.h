@@ -209,6 +209,19 @@ hsr_status hsr_guide_reset(hsr_guide *guide);
 hsr_status hsr_guide_step(hsr_guide *guide);
 hsr_status hsr_guide_destroy(hsr_guide *guide);
 
+/* The guide's tree as host arrays of HSR_GUIDE_MAX_NODES entries: the sampling tree
+ * (index of a node's first child, whose pair is (c, c + 1), -1 for a leaf; probability
+ * of the first child) and the training tree (child links; per node the sum of w d^2 that
+ * GuidingWrapper::splat adds, path.h:96-111). Read returns the training tree's node
+ * count; write replaces the state (links must point past their node and stay inside the
+ * arrays). For inspection, warm starts, and checks against a CPU restatement of the
+ * tree. Synchronous (they wait for the device). */
+#define HSR_GUIDE_MAX_NODES 2048
+hsr_status hsr_guide_read(hsr_guide *guide, int32_t *out_count, int32_t *samp_child, float *samp_p,
+                          int32_t *train_child, float *train_acc2);
+hsr_status hsr_guide_write(hsr_guide *guide, int32_t count, const int32_t *samp_child, const float *samp_p,
+                           const int32_t *train_child, const float *train_acc2);
+
 /* One guided iteration of PathTracer::run (path.h:186-224): as hsr_backend_run, with each
  * sample's primary direction drawn from the guide's sampling tree (GuidingWrapper::sample,
  * path.h:265-270) and, when `train` is non-zero (every iteration but the final one,

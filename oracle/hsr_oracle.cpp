@@ -1,7 +1,7 @@
 /*
  * ORACLE — TEST INFRASTRUCTURE ONLY.
  *
- * A CPU restatement of libhussar's plain (unguided) radar path tracer, used only by
+ * A CPU restatement of libhussar's radar path tracer, used only by
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker
  * and the timed CPU reference. The product (hussar_gb300/, libhsr_gb300.so) never
  * links, loads or calls anything in this directory.
@@ -14,6 +14,9 @@
  *   - Ray, Intersection                      libhussar/include/hussar/core/geometry.h:69-143,
  *                                            libhussar/include/hussar/core/intersection.h:16-57
  *   - PathTracer::sample                     libhussar/include/hussar/integrators/path.h:235-451
+ *   - PathTracer::run (guided schedule)      libhussar/include/hussar/integrators/path.h:171-224
+ *   - GuidingWrapper sample/splat/step       libhussar/include/hussar/integrators/path.h:17-131
+ *     over the product's own 2-D tree (libguiding's BTree is not in the reference sources)
  *   - Integrator::measureRay/splat/reflect   libhussar/include/hussar/core/integrator.h:107-168
  *   - Frame::PIndex::setTime/setVelocity     libradar/include/radar/radar.h:232-251
  *   - Frame::splat<16>                       libradar/include/radar/radar.h:564-626
@@ -924,6 +927,174 @@ struct Flags {
     float filteringMin, filteringMax, filteringRadius;
 };
 
+// ----------------------------------------------------------------------------------
+// Path guiding of the TX primary sample square: GuidingWrapper (path.h:17-131) with the
+// settings of PathTracer::setup (path.h:226-233: uniform mixture 0.1, split threshold
+// 0.005, second moment). The reference's distribution is libguiding's BTree (the
+// 3rdparty/libguiding submodule, github.com/iRath96/libguiding, absent from the
+// reference sources, so its own code and pinned commit are unknown here). Restated is
+// the product's tree, which follows that interface:
+//   - a 2-D binary tree over [0,1)^2; a node's region halves at its midpoint along x0 at
+//     even depths and x1 at odd ones; the children of a node are stored as a pair (first
+//     child c, second c + 1), -1 marks a leaf; at most 2048 nodes and depth 24;
+//   - sampling tree: per node the probability of its first child;
+//   - training tree: per node the sum of w d^2 (the second-moment statistic of
+//     GuidingWrapper::splat(density d, weight w), path.h:96-111, 448-450);
+//   - step (path.h:119-126): build leaf energies sqrt(sum w d^2 * area) and sums up the
+//     tree, copy into the sampling tree, refine the training tree in pre-order: a node
+//     whose energy fraction exceeds the threshold is split (an old leaf into halves of
+//     half the fraction each), anything else becomes a leaf; statistics restart at 0.
+// ----------------------------------------------------------------------------------
+constexpr int kGuideNodes = 2048;
+constexpr int kGuideDepth = 24;
+constexpr float kGuideUniform = 0.1f;     // path.h:229
+constexpr float kGuideSplit = 0.005f;     // path.h:230
+constexpr float kBelowOne = 0x1.fffffep-1f;
+
+struct GuideTree {
+    std::vector<int32_t> samp_child = std::vector<int32_t>(kGuideNodes, -1);
+    std::vector<float> samp_p = std::vector<float>(kGuideNodes, 0.5f);
+    std::vector<int32_t> train_child = std::vector<int32_t>(kGuideNodes, -1);
+    std::vector<float> acc2 = std::vector<float>(kGuideNodes, 0.f);
+    int32_t count = 1;  // nodes of the training tree
+};
+
+// descent by position: the density of the tree at x relative to uniform (with pf), or
+// the leaf holding x
+static float tree_locate(const int32_t *child, const float *pf, float x0, float x1, int32_t *leaf) {
+    float pdf = 1.f;
+    float lo[2] = {0.f, 0.f}, half[2] = {1.f, 1.f};
+    const float x[2] = {x0, x1};
+    int32_t node = 0;
+    for (int depth = 0; depth < kGuideDepth && child[node] >= 0; ++depth) {
+        const int ax = depth & 1;
+        half[ax] *= 0.5f;
+        const bool first = x[ax] < lo[ax] + half[ax];
+        if (pf) pdf *= 2.f * (first ? pf[node] : 1.f - pf[node]);
+        if (!first) lo[ax] += half[ax];
+        node = child[node] + (first ? 0 : 1);
+    }
+    if (leaf) *leaf = node;
+    return pdf;
+}
+
+// warps x through the sampling tree (each level picks a child by its probability and
+// rescales the coordinate of that level's axis); returns the tree density there
+static float tree_warp(const int32_t *child, const float *pf, float &x0, float &x1) {
+    float pdf = 1.f;
+    float lo[2] = {0.f, 0.f}, half[2] = {1.f, 1.f};
+    float x[2] = {x0, x1};
+    int32_t node = 0;
+    for (int depth = 0; depth < kGuideDepth && child[node] >= 0; ++depth) {
+        const int ax = depth & 1;
+        const float p = pf[node];
+        half[ax] *= 0.5f;
+        if (x[ax] < p) {
+            x[ax] = p > 0.f ? x[ax] / p : 0.f;
+            pdf *= 2.f * p;
+            node = child[node];
+        } else {
+            x[ax] = p < 1.f ? (x[ax] - p) / (1.f - p) : 0.f;
+            pdf *= 2.f * (1.f - p);
+            lo[ax] += half[ax];
+            node = child[node] + 1;
+        }
+        x[ax] = std::min(std::max(x[ax], 0.f), kBelowOne);
+    }
+    x0 = std::min(lo[0] + x[0] * half[0], kBelowOne);
+    x1 = std::min(lo[1] + x[1] * half[1], kBelowOne);
+    return pdf;
+}
+
+// GuidingWrapper::sample (path.h:54-82): warps (x0, x1) in place, returns the mixture pdf
+static float guide_mix_sample(const GuideTree &g, float &x0, float &x1) {
+    float pdf = 1.f - kGuideUniform;
+    if (x0 < kGuideUniform) {
+        x0 /= kGuideUniform;
+        pdf *= tree_locate(g.samp_child.data(), g.samp_p.data(), x0, x1, nullptr);
+    } else {
+        x0 -= kGuideUniform;
+        x0 /= 1.f - kGuideUniform;
+        pdf *= tree_warp(g.samp_child.data(), g.samp_p.data(), x0, x1);
+    }
+    return pdf + kGuideUniform;
+}
+
+// GuidingWrapper::splat (path.h:96-111) as PathTracer::sample calls it (path.h:448-450):
+// density |guidingWeight| * pdf, weight 1 / pdf, at the warped primary sample
+static void guide_train(GuideTree &g, Cx<float> gw, float pdf, float x0, float x1) {
+    if (!(pdf > 0.f)) return;
+    const float density = cabs(gw) * pdf;
+    if (density == 0.f) return;
+    const float weight = 1.f / pdf;
+    int32_t leaf = 0;
+    tree_locate(g.train_child.data(), nullptr, x0, x1, &leaf);
+    g.acc2[leaf] += weight * density * density;
+}
+
+// GuidingWrapper::step (path.h:119-126)
+static void guide_step(GuideTree &g) {
+    const int n = std::min(std::max(g.count, 1), kGuideNodes);
+    const int32_t *tc = g.train_child.data();
+    std::vector<int> depth(n, 0);
+    std::vector<float> e(n, 0.f);
+    for (int i = 0; i < n; ++i)  // children follow their parent
+        if (tc[i] >= 0 && tc[i] + 1 < n) depth[tc[i]] = depth[tc[i] + 1] = depth[i] + 1;
+    for (int i = n - 1; i >= 0; --i)
+        e[i] = tc[i] < 0 ? std::sqrt(std::max(g.acc2[i], 0.f) * std::ldexp(1.f, -depth[i])) : e[tc[i]] + e[tc[i] + 1];
+    for (int i = 0; i < n; ++i) {
+        g.samp_child[i] = tc[i];
+        if (tc[i] >= 0) {
+            const float s = e[tc[i]] + e[tc[i] + 1];
+            g.samp_p[i] = s > 0.f ? e[tc[i]] / s : 0.5f;
+        } else {
+            g.samp_p[i] = 0.5f;
+        }
+    }
+    int ncount = n;
+    const float total = e[0];
+    if (total > 0.f) {
+        struct Pending {
+            int old;    // node of the old training tree (-1: inside a split old leaf)
+            float f;    // energy fraction
+            int d;      // depth
+            int slot;   // node of the new tree
+        };
+        constexpr int kMaxPending = 2 * kGuideDepth + 4;
+        std::vector<int32_t> out(kGuideNodes, -1);
+        Pending stack[kMaxPending];
+        int top = 0;
+        ncount = 1;
+        stack[top++] = Pending{0, 1.f, 0, 0};
+        while (top > 0) {
+            const Pending it = stack[--top];
+            const bool split = it.f > kGuideSplit && it.d < kGuideDepth && ncount + 2 <= kGuideNodes &&
+                               top + 2 <= kMaxPending;
+            if (!split) {
+                out[it.slot] = -1;
+                continue;
+            }
+            const int c = ncount;
+            ncount += 2;
+            out[it.slot] = c;
+            if (it.old >= 0 && tc[it.old] >= 0) {
+                const int oc = tc[it.old];
+                const float eo = e[it.old];
+                const float f0 = eo > 0.f ? it.f * (e[oc] / eo) : 0.5f * it.f;
+                const float f1 = eo > 0.f ? it.f * (e[oc + 1] / eo) : 0.5f * it.f;
+                stack[top++] = Pending{oc + 1, f1, it.d + 1, c + 1};
+                stack[top++] = Pending{oc, f0, it.d + 1, c};
+            } else {
+                stack[top++] = Pending{-1, 0.5f * it.f, it.d + 1, c + 1};
+                stack[top++] = Pending{-1, 0.5f * it.f, it.d + 1, c};
+            }
+        }
+        for (int i = 0; i < ncount; ++i) g.train_child[i] = out[i];
+    }
+    std::fill(g.acc2.begin(), g.acc2.end(), 0.f);
+    g.count = ncount;
+}
+
 template <typename R> struct Tracer {
     const Scene *scene;
     Rf<R> rf;
@@ -937,6 +1108,8 @@ template <typename R> struct Tracer {
     bool floatSamples = false;
     oracle_record *records = nullptr;  // optional per-sample event log
     int maxRecords = 0;
+    GuideTree *guide = nullptr;  // doGuiding: the pose's tree (single-threaded runs)
+    bool guideTrain = false;     // splat into its training tree (not the final iteration)
 
     Cx<R> measureRay(R dt) const { return measure_ray(dt, rf.startFreq, rf.freqSlope); }
 
@@ -982,6 +1155,8 @@ template <typename R> struct Tracer {
         const R maxDist = rf.adcRate / rf.freqSlope * Consts<R>::SpeedOfLight;
         const R sampleWeight = currentSampleWeight;
         R primaryPdf = 1;
+        Cx<R> guidingWeight{R(0), R(0)};
+        float gx0 = 0.f, gx1 = 0.f;  // the primary sample after guiding (training position)
         Isect<R> isect;
         Ray<R> &ray = isect.ray;
         ray.frequency = rf.startFreq + sampler.get1D() * rf.bandwidth();
@@ -994,6 +1169,13 @@ template <typename R> struct Tracer {
             if (ray.depth == 0) {
                 R u0, u1;
                 sampler.get2D(u0, u1);
+                if (guide) {  // GuidingWrapper::sample in float (path.h:265-270)
+                    gx0 = float(u0);
+                    gx1 = float(u1);
+                    primaryPdf = R(guide_mix_sample(*guide, gx0, gx1));
+                    u0 = R(gx0);
+                    u1 = R(gx1);
+                }
                 if (farField)
                     ff_sample(ftx, u0, u1, ray);
                 else
@@ -1061,6 +1243,10 @@ template <typename R> struct Tracer {
                         if (fl.filteringSphere) {
                             if (dphase > R(fl.filteringRadius)) {
                                 if (fl.correctPhase) {
+                                    if (fl.filterGuiding) {  // path.h:363-367
+                                        const R q = dphase / R(fl.filteringRadius);
+                                        guidingWeight = cadd(guidingWeight, cdivs(v, R(double(q) * double(q) + 1.0)));
+                                    }
                                     v = {R(0), R(0)};
                                 } else {
                                     R q = dphase / R(fl.filteringRadius) - R(1);
@@ -1069,12 +1255,19 @@ template <typename R> struct Tracer {
                                 }
                             }
                         } else {
-                            if (dphase > R(fl.filteringMax)) v = {R(0), R(0)};
+                            if (dphase > R(fl.filteringMax)) {
+                                if (fl.filterGuiding) {  // path.h:378-382
+                                    const R q = dphase / R(fl.filteringMax);
+                                    guidingWeight = cadd(guidingWeight, cdivs(v, R(double(q) * double(q) + 1.0)));
+                                }
+                                v = {R(0), R(0)};
+                            }
                             if (dphase > R(fl.filteringMin))
                                 v = cscale(v, (R(fl.filteringMax) - dphase) / (R(fl.filteringMax) - R(fl.filteringMin)));
                         }
                     }
                 }
+                if (ray.depth > 0) guidingWeight = cadd(guidingWeight, v);  // path.h:389-391
                 oracle_record *rec = nullptr;
                 if (records && nrec < maxRecords) {
                     rec = &records[nrec++];
@@ -1111,6 +1304,10 @@ template <typename R> struct Tracer {
             ray.o = isect.p;
             ray.depth++;
         }
+        // path.h:448-450 (the splat's float arguments)
+        if (guide && guideTrain && primaryPdf > R(0))
+            guide_train(*guide, Cx<float>{float(guidingWeight.re), float(guidingWeight.im)}, float(primaryPdf), gx0,
+                        gx1);
     }
 };
 
@@ -1374,5 +1571,116 @@ void oracle_set_libm_trig(int on) { g_libm_trig = on ? 1 : 0; }
 void oracle_sincos_rounded(float x, float *s, float *c) { sincos_once_rounded(x, *s, *c); }
 
 int64_t oracle_bvh_nodes(void *sp) { return int64_t(static_cast<Scene *>(sp)->bvh.nodes.size()); }
+
+// ---- path guiding (GuidingWrapper, path.h:17-131; PathTracer::run, path.h:171-224) ----
+
+void *oracle_guide_create(void) { return new GuideTree(); }
+
+void oracle_guide_destroy(void *g) { delete static_cast<GuideTree *>(g); }
+
+// GuidingWrapper::reset (path.h:47-50)
+void oracle_guide_reset(void *g) { *static_cast<GuideTree *>(g) = GuideTree(); }
+
+void oracle_guide_step(void *g) { guide_step(*static_cast<GuideTree *>(g)); }
+
+// the whole state: 2048 entries per array; returns the training tree's node count
+int32_t oracle_guide_get(void *gp, int32_t *samp_child, float *samp_p, int32_t *train_child, float *acc2) {
+    const GuideTree &g = *static_cast<GuideTree *>(gp);
+    std::copy(g.samp_child.begin(), g.samp_child.end(), samp_child);
+    std::copy(g.samp_p.begin(), g.samp_p.end(), samp_p);
+    std::copy(g.train_child.begin(), g.train_child.end(), train_child);
+    std::copy(g.acc2.begin(), g.acc2.end(), acc2);
+    return g.count;
+}
+
+int oracle_guide_set(void *gp, int32_t count, const int32_t *samp_child, const float *samp_p,
+                     const int32_t *train_child, const float *acc2) {
+    if (count < 1 || count > kGuideNodes) return 1;
+    GuideTree &g = *static_cast<GuideTree *>(gp);
+    g.samp_child.assign(samp_child, samp_child + kGuideNodes);
+    g.samp_p.assign(samp_p, samp_p + kGuideNodes);
+    g.train_child.assign(train_child, train_child + kGuideNodes);
+    g.acc2.assign(acc2, acc2 + kGuideNodes);
+    g.count = count;
+    return 0;
+}
+
+// GuidingWrapper::sample on (x0, x1): the warped point and the mixture pdf
+float oracle_guide_sample(void *gp, float x0, float x1, float *y) {
+    const float pdf = guide_mix_sample(*static_cast<GuideTree *>(gp), x0, x1);
+    y[0] = x0;
+    y[1] = x1;
+    return pdf;
+}
+
+// One guided iteration (the backend run of one PathTracer::run iteration) on one thread,
+// in FP32: Halton indices offset .. offset + budget - 1, sample weight, training into
+// the tree when `train`. Adds the frame's sums to frame_out and the weight to weight_out.
+int oracle_guided_pass(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc, const hsr_antenna_o *tx,
+                       const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl, int64_t budget, int64_t offset,
+                       float sample_weight, int train, void *gp, double *frame_out, double *weight_out) {
+    if (!sp || !rf || !fc || !tx || !rx || !fl || !gp || !frame_out || !weight_out || budget < 0) return 1;
+    if (fc->chirpCount <= 0 || fc->samplesPerChirp <= 0 || fc->channelCount <= 0) return 1;
+    Tracer<float> tr;
+    setup_tracer(tr, static_cast<Scene *>(sp), rf, tx, rx, fl);
+    tr.guide = static_cast<GuideTree *>(gp);
+    tr.guideTrain = train != 0;
+    tr.currentSampleWeight = sample_weight;
+    tr.sampleIndexOffset = offset;
+    tr.frame.chirps = fc->chirpCount;
+    tr.frame.samples = fc->samplesPerChirp;
+    tr.frame.channels = fc->channelCount;
+    const size_t n = size_t(fc->chirpCount) * fc->samplesPerChirp * fc->channelCount;
+    std::vector<float> data(2 * n, 0.f);
+    tr.frame.data = data.data();
+    for (int64_t i = 0; i < budget; ++i) tr.sample(i);
+    for (size_t i = 0; i < 2 * n; ++i) frame_out[i] += double(data[i]);
+    double w = 0;
+    for (int64_t i = 0; i < budget; ++i) w += double(sample_weight);
+    *weight_out += w;
+    return 0;
+}
+
+// PathTracer::run (path.h:171-224) with doGuiding: the doubling schedule from 16384
+// samples, training on every iteration but the final one, the frame cleared between
+// iterations (clearBeforeIteration) or later samples weighted 10x, a step between
+// iterations. Overwrites frame_out / weight_out with the frame's sums and total weight;
+// the tree ends in its state after the last step.
+int oracle_path_tracer_run(void *sp, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
+                           const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
+                           int64_t samples, void *gp, double *frame_out, double *weight_out) {
+    if (!fl || !fc || !gp || !frame_out || !weight_out || samples < 0 || !fl->doGuiding) return 1;
+    const size_t n = 2 * size_t(fc->chirpCount) * fc->samplesPerChirp * fc->channelCount;
+    GuideTree &g = *static_cast<GuideTree *>(gp);
+    g = GuideTree();
+    std::fill(frame_out, frame_out + n, 0.0);
+    *weight_out = 0;
+    int64_t offset = 0, milestone = 16384, remaining = samples;
+    float weight = 1.f;
+    bool final_iteration = false;
+    while (remaining > 0) {
+        milestone = std::min(milestone, remaining);
+        const int rc = oracle_guided_pass(sp, rf, fc, tx, rx, fl, milestone, offset, weight, !final_iteration, gp,
+                                          frame_out, weight_out);
+        if (rc) return rc;
+        offset += milestone;
+        remaining -= milestone;
+        if (remaining == 0) break;
+        milestone *= 2;
+        if (remaining < milestone * 2) {
+            final_iteration = true;
+            milestone = remaining;
+        }
+        if (fl->clearBeforeIteration) {
+            std::fill(frame_out, frame_out + n, 0.0);
+            *weight_out = 0;
+            offset = 0;
+        } else {
+            weight = 10 * weight;
+        }
+        guide_step(g);
+    }
+    return 0;
+}
 
 }  // extern "C"

@@ -91,6 +91,26 @@ float oracle_set_time(float delta_t, float freqSlope, float adcRate, int samples
 void oracle_set_libm_trig(int on);
 void oracle_sincos_rounded(float x, float *s, float *c);
 
+/* Path guiding: the product's 2-D tree behind GuidingWrapper (path.h:17-131), restated.
+ * Arrays are 2048 entries (the tree's capacity); get returns the training node count. */
+void *oracle_guide_create(void);
+void oracle_guide_destroy(void *guide);
+void oracle_guide_reset(void *guide);
+void oracle_guide_step(void *guide);
+int32_t oracle_guide_get(void *guide, int32_t *samp_child, float *samp_p, int32_t *train_child, float *acc2);
+int oracle_guide_set(void *guide, int32_t count, const int32_t *samp_child, const float *samp_p,
+                     const int32_t *train_child, const float *acc2);
+float oracle_guide_sample(void *guide, float x0, float x1, float *y2);
+/* one guided iteration on one thread, FP32; adds to frame_out / weight_out */
+int oracle_guided_pass(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
+                       const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
+                       int64_t budget, int64_t offset, float sample_weight, int train, void *guide,
+                       double *frame_out, double *weight_out);
+/* PathTracer::run's guided schedule (path.h:171-224); overwrites frame_out / weight_out */
+int oracle_path_tracer_run(void *scene, const hsr_rf_config_o *rf, const hsr_frame_config_o *fc,
+                           const hsr_antenna_o *tx, const hsr_antenna_o *rx, const hsr_tracer_flags_o *fl,
+                           int64_t samples, void *guide, double *frame_out, double *weight_out);
+
 #ifdef __cplusplus
 }
 #endif

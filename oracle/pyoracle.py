@@ -81,6 +81,19 @@ def lib():
         L.oracle_awr_evaluate.argtypes = [fp, fp]
         L.oracle_uniform_sample_sphere.argtypes = [ctypes.c_float, ctypes.c_float, fp]
         L.oracle_measure_ray.argtypes = [ctypes.c_float] * 3 + [fp]
+        L.oracle_guide_create.restype = vp
+        L.oracle_guide_destroy.argtypes = [vp]
+        L.oracle_guide_reset.argtypes = [vp]
+        L.oracle_guide_step.argtypes = [vp]
+        L.oracle_guide_get.restype = ctypes.c_int32
+        L.oracle_guide_get.argtypes = [vp, vp, vp, vp, vp]
+        L.oracle_guide_set.argtypes = [vp, ctypes.c_int32, vp, vp, vp, vp]
+        L.oracle_guide_sample.restype = ctypes.c_float
+        L.oracle_guide_sample.argtypes = [vp, ctypes.c_float, ctypes.c_float, fp]
+        L.oracle_guided_pass.argtypes = [vp, P(RF), P(FC), P(ANT), P(ANT), P(FLAGS), ctypes.c_int64, ctypes.c_int64,
+                                         ctypes.c_float, ctypes.c_int, vp, vp, P(ctypes.c_double)]
+        L.oracle_path_tracer_run.argtypes = [vp, P(RF), P(FC), P(ANT), P(ANT), P(FLAGS), ctypes.c_int64, vp, vp,
+                                             P(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -199,6 +212,97 @@ class Scene:
                              ctypes.byref(ant_c(rx)), ctypes.byref(flags_c(tracer)), int(first), int(count),
                              int(offset), int(mr), _p(out))
         return out
+
+
+GUIDE_NODES = 2048
+
+
+class GuideState:
+    """The arrays of a guiding tree (sampling links and first-child probabilities,
+    training links and second-moment sums, training node count)."""
+
+    def __init__(self, count=1, samp_child=None, samp_p=None, train_child=None, acc2=None):
+        self.count = int(count)
+        self.samp_child = np.full(GUIDE_NODES, -1, np.int32) if samp_child is None else \
+            np.ascontiguousarray(samp_child, np.int32)
+        self.samp_p = np.full(GUIDE_NODES, 0.5, np.float32) if samp_p is None else \
+            np.ascontiguousarray(samp_p, np.float32)
+        self.train_child = np.full(GUIDE_NODES, -1, np.int32) if train_child is None else \
+            np.ascontiguousarray(train_child, np.int32)
+        self.acc2 = np.zeros(GUIDE_NODES, np.float32) if acc2 is None else np.ascontiguousarray(acc2, np.float32)
+
+    def reachable(self, which="samp"):
+        """Node indices reachable from the root of the sampling or training tree."""
+        child = self.samp_child if which == "samp" else self.train_child
+        out, todo = [], [0]
+        while todo:
+            n = todo.pop()
+            out.append(n)
+            if child[n] >= 0:
+                todo += [int(child[n]), int(child[n]) + 1]
+        return np.array(sorted(out), np.int64)
+
+
+class Guide:
+    """The oracle's restatement of the guiding tree (GuidingWrapper over the product's
+    2-D tree)."""
+
+    def __init__(self):
+        self.h = lib().oracle_guide_create()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_guide_destroy(self.h)
+            self.h = None
+
+    def reset(self):
+        lib().oracle_guide_reset(self.h)
+
+    def step(self):
+        lib().oracle_guide_step(self.h)
+
+    def get(self):
+        s = GuideState()
+        s.count = lib().oracle_guide_get(self.h, _p(s.samp_child), _p(s.samp_p), _p(s.train_child), _p(s.acc2))
+        return s
+
+    def set(self, s):
+        rc = lib().oracle_guide_set(self.h, int(s.count), _p(s.samp_child), _p(s.samp_p), _p(s.train_child),
+                                    _p(s.acc2))
+        if rc:
+            raise ValueError("oracle_guide_set rejected the state")
+
+    def sample(self, x0, x1):
+        y = np.zeros(2, np.float32)
+        pdf = lib().oracle_guide_sample(self.h, float(x0), float(x1), y.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        return float(y[0]), float(y[1]), float(pdf)
+
+    def run_pass(self, scene, rf, fc, tx, rx, tracer, budget, offset=0, sample_weight=1.0, train=True):
+        """One guided iteration (one thread, FP32): (raw frame sums, total weight)."""
+        n = fc.chirpCount * fc.samplesPerChirp * fc.channelCount
+        out = np.zeros(2 * n, np.float64)
+        w = ctypes.c_double(0.0)
+        rc = lib().oracle_guided_pass(scene.h, ctypes.byref(rf_c(rf)), ctypes.byref(fc_c(fc)),
+                                      ctypes.byref(ant_c(tx)), ctypes.byref(ant_c(rx)), ctypes.byref(flags_c(tracer)),
+                                      int(budget), int(offset), float(sample_weight), 1 if train else 0, self.h,
+                                      _p(out), ctypes.byref(w))
+        if rc:
+            raise RuntimeError("oracle_guided_pass failed (%d)" % rc)
+        return out.view(np.complex128).reshape(fc.chirpCount, fc.samplesPerChirp, fc.channelCount), w.value
+
+    def path_tracer_run(self, scene, rf, fc, tx, rx, tracer, samples):
+        """PathTracer::run's guided schedule: (raw frame sums, total weight); the tree
+        ends in its state after the last step."""
+        n = fc.chirpCount * fc.samplesPerChirp * fc.channelCount
+        out = np.zeros(2 * n, np.float64)
+        w = ctypes.c_double(0.0)
+        rc = lib().oracle_path_tracer_run(scene.h, ctypes.byref(rf_c(rf)), ctypes.byref(fc_c(fc)),
+                                          ctypes.byref(ant_c(tx)), ctypes.byref(ant_c(rx)),
+                                          ctypes.byref(flags_c(tracer)), int(samples), self.h, _p(out),
+                                          ctypes.byref(w))
+        if rc:
+            raise RuntimeError("oracle_path_tracer_run failed (%d)" % rc)
+        return out.view(np.complex128).reshape(fc.chirpCount, fc.samplesPerChirp, fc.channelCount), w.value
 
 
 def radical_inverse(index, dim, precision=32):
