@@ -1,6 +1,6 @@
-// Host definitions of the CUDA device intrinsics the traversal and collapse headers use,
-// so that the product's own device code (hussar_gb300/csrc/hsr_traverse.cuh,
-// hsr_wide.cuh) compiles and runs on the CPU in the tests. Semantics as in CUDA: __fmaf_rn
+// Host definitions of the CUDA device intrinsics the traversal header uses, so that the
+// product's own device code (hussar_gb300/csrc/hsr_traverse.cuh) compiles and runs on the
+// CPU in the tests. Semantics as in CUDA: __fmaf_rn
 // is a single-rounding fused multiply-add, the bit casts are exact, atomics are plain
 // read-modify-writes (the tests run one thread).
 #pragma once
