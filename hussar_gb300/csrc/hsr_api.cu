@@ -580,7 +580,7 @@ hsr_status hsr_scene_create(const float *vertices, int64_t vertex_count, const i
         cudaFree(d.tris);
         cudaFree(d.nodes);
         delete s;
-        return fail(rc == 3 ? HSR_ERR_OUT_OF_MEMORY : HSR_ERR_CUDA, err);
+        return fail(rc == 3 ? HSR_ERR_OUT_OF_MEMORY : rc == 4 ? HSR_ERR_INVALID_ARGUMENT : HSR_ERR_CUDA, err);
     }
     cudaEventCreate(&d.ev0);
     cudaEventCreate(&d.ev1);
@@ -1294,6 +1294,12 @@ hsr_status hsr_set_path_kernel(int32_t kind) {
 hsr_status hsr_set_bvh_builder(int32_t builder) {
     if (builder != 0 && builder != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "builder must be 0 or 1");
     g_bvh_builder = builder;
+    return HSR_OK;
+}
+
+hsr_status hsr_set_bvh_leaf_size(int32_t triangles) {
+    if (triangles < 1 || triangles > 8) return fail(HSR_ERR_INVALID_ARGUMENT, "leaf size must be 1..8");
+    g_bvh_leaf_max = triangles;
     return HSR_OK;
 }
 

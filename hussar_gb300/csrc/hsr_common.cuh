@@ -190,7 +190,8 @@ struct __align__(16) DTri {
 };
 
 // Binary BVH node holding both child boxes (64 bytes, four 16-byte loads).
-// child >= 0: internal node index; child < 0: leaf, triangle slot ~child.
+// child >= 0: internal node index; child < 0: a leaf of ((~child) & 7) + 1 triangles in
+// consecutive slots from (~child) >> 3.
 struct __align__(16) DNode {
     float4 a;  // c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y
     float4 b;  // c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y

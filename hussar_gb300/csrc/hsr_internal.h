@@ -250,6 +250,7 @@ int launch_wave(const TraceParams &p, int phase_mode, int grid, cudaStream_t st,
 extern int g_path_kernel;
 // BVH topology of new scenes: 0 = PLOC (default), 1 = LBVH (Karras radix tree)
 extern int g_bvh_builder;
+extern int g_bvh_leaf_max;
 int trace_blocks_per_sm(int samples, int splat_mode, int fine_bins);
 
 }  // namespace hsr

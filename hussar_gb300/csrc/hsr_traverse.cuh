@@ -165,16 +165,19 @@ __device__ __forceinline__ int closest_hit(const DNode *__restrict__ nodes, cons
                 continue;
             }
         } else {
-            int slot = ~node;
-            DTri T = load_tri(tris, slot);
-            if (kCount) cnt->tris++;
-            float t;
-            if (tri_test(T, o, d, tnear, tfar, t)) {
-                int prim = __float_as_int(T.v0.w);
-                if (t < t_best || (t == t_best && prim < prim_best)) {
-                    t_best = t;
-                    prim_best = prim;
-                    best = slot;
+            const int ref = ~node;
+            const int last = (ref >> 3) + (ref & 7);
+            for (int slot = ref >> 3; slot <= last; ++slot) {
+                DTri T = load_tri(tris, slot);
+                if (kCount) cnt->tris++;
+                float t;
+                if (tri_test(T, o, d, tnear, tfar, t)) {
+                    int prim = __float_as_int(T.v0.w);
+                    if (t < t_best || (t == t_best && prim < prim_best)) {
+                        t_best = t;
+                        prim_best = prim;
+                        best = slot;
+                    }
                 }
             }
         }
@@ -219,10 +222,14 @@ __device__ __forceinline__ bool any_hit(const DNode *__restrict__ nodes, const D
                 continue;
             }
         } else {
-            DTri T = load_tri(tris, ~node);
-            if (kCount) cnt->tris++;
-            float t;
-            if (tri_test(T, o, d, tnear, tfar, t)) return true;
+            const int ref = ~node;
+            const int last = (ref >> 3) + (ref & 7);
+            for (int slot = ref >> 3; slot <= last; ++slot) {
+                DTri T = load_tri(tris, slot);
+                if (kCount) cnt->tris++;
+                float t;
+                if (tri_test(T, o, d, tnear, tfar, t)) return true;
+            }
         }
         if (sp == 0) break;
         node = stack[--sp];

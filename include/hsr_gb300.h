@@ -437,6 +437,13 @@ hsr_status hsr_set_path_kernel(int32_t kind);
  * give bit-identical ray-query results; only the traversal cost differs. */
 hsr_status hsr_set_bvh_builder(int32_t builder);
 
+/* Largest BVH leaf (triangles, 1..8, default 4) for scenes created afterwards
+ * (process-wide): subtrees of at most this many triangles become one leaf where a
+ * surface-area cost estimate finds testing their triangles cheaper than visiting their
+ * nodes. Ray-query results do not depend on it (equal-distance hits go to the lower
+ * primitive id); only the traversal cost does. */
+hsr_status hsr_set_bvh_leaf_size(int32_t triangles);
+
 /* Engine of the fine-histogram synthesis GEMM (process-wide): 0 (default) = tensor cores
  * (tcgen05.mma, operands split into three BF16 terms, FP32 accumulation), 1 = CUDA cores
  * in FP32. Both compute the same product; tests use this to check one against the other. */

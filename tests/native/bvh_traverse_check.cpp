@@ -1,7 +1,8 @@
 // CPU check of the device traversal code, compiled from the product's own header
 // (hussar_gb300/csrc/hsr_traverse.cuh) with host definitions of the CUDA intrinsics
-// (host_shim.h): a binary tree in the kernels' DNode layout (median split, one triangle
-// per leaf, boxes padded like the device build) answers every ray through
+// (host_shim.h): a binary tree in the kernels' DNode layout (median split, leaves of up to
+// argv[2] triangles in consecutive slots, boxes padded like the device build) answers
+// every ray through
 // hsr::closest_hit / hsr::any_hit, and brute force over all triangles with the same
 // triangle test and tie rule answers it again.
 //
@@ -14,6 +15,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 using namespace hsr;
@@ -35,10 +37,17 @@ static void box_of(const std::vector<Item> &it, int a, int b, float *lo, float *
         }
 }
 
-// Median split over centroids; returns the child reference of range [a, b).
-static int build(std::vector<Item> &it, int a, int b, std::vector<DNode> &nodes, int depth, int &max_depth) {
+// Median split over centroids; returns the child reference of range [a, b). A range of at
+// most `leaf` triangles (not the root's) becomes a leaf: its records are appended to
+// `out` and referenced as ~((first slot << 3) | (count - 1)).
+static int build(std::vector<Item> &it, int a, int b, std::vector<DNode> &nodes, int depth, int &max_depth,
+                 int leaf, const std::vector<DTri> &tris, std::vector<DTri> &out) {
     max_depth = std::max(max_depth, depth);
-    if (b - a == 1) return ~it[a].slot;
+    if (b - a <= leaf && depth > 0) {
+        const int first = int(out.size());
+        for (int i = a; i < b; ++i) out.push_back(tris[it[i].slot]);
+        return ~((first << 3) | (b - a - 1));
+    }
     const int id = int(nodes.size());
     nodes.emplace_back();
     float clo[3] = {1e30f, 1e30f, 1e30f}, chi[3] = {-1e30f, -1e30f, -1e30f};
@@ -56,8 +65,8 @@ static int build(std::vector<Item> &it, int a, int b, std::vector<DNode> &nodes,
     float l0[3], h0[3], l1[3], h1[3];
     box_of(it, a, mid, l0, h0);
     box_of(it, mid, b, l1, h1);
-    const int c0 = build(it, a, mid, nodes, depth + 1, max_depth);
-    const int c1 = build(it, mid, b, nodes, depth + 1, max_depth);
+    const int c0 = build(it, a, mid, nodes, depth + 1, max_depth, leaf, tris, out);
+    const int c1 = build(it, mid, b, nodes, depth + 1, max_depth, leaf, tris, out);
     DNode &n = nodes[id];
     n.a = make_float4(l0[0], h0[0], l0[1], h0[1]);
     n.b = make_float4(l1[0], h1[0], l1[1], h1[1]);
@@ -68,6 +77,8 @@ static int build(std::vector<Item> &it, int a, int b, std::vector<DNode> &nodes,
 
 int main(int argc, char **argv) {
     if (argc < 2) return 2;
+    const int leaf = argc > 2 ? std::atoi(argv[2]) : 1;
+    if (leaf < 1 || leaf > 8) return 2;
     FILE *f = std::fopen(argv[1], "rb");
     if (!f) return 2;
     int64_t hdr[3];
@@ -100,8 +111,10 @@ int main(int argc, char **argv) {
     }
     std::vector<DNode> nodes;
     nodes.reserve(nt);
+    std::vector<DTri> leaf_tris;
+    leaf_tris.reserve(nt);
     int depth = 0;
-    build(items, 0, int(nt), nodes, 0, depth);
+    build(items, 0, int(nt), nodes, 0, depth, leaf, tris, leaf_tris);
     unsigned status = 0;
     int64_t bad_c = 0, bad_a = 0;
     TraversalCounters cnt{0u, 0u};
@@ -110,7 +123,8 @@ int main(int argc, char **argv) {
         const f3 dd = mk3(d[3 * r], d[3 * r + 1], d[3 * r + 2]);
         float tb;
         int pb;
-        const int slot = closest_hit<true>(nodes.data(), tris.data(), oo, dd, kEpsilon, INFINITY, tb, pb, &status, &cnt);
+        const int slot =
+            closest_hit<true>(nodes.data(), leaf_tris.data(), oo, dd, kEpsilon, INFINITY, tb, pb, &status, &cnt);
         float bt = INFINITY;
         int bp = 0x7fffffff;
         for (int64_t t = 0; t < nt; ++t) {
@@ -120,16 +134,18 @@ int main(int argc, char **argv) {
                 bp = int(t);
             }
         }
-        const int gp = slot < 0 ? 0x7fffffff : __float_as_int(tris[slot].v0.w);
+        const int gp = slot < 0 ? 0x7fffffff : __float_as_int(leaf_tris[slot].v0.w);
         if (gp != bp || (slot >= 0 && __float_as_uint(tb) != __float_as_uint(bt))) ++bad_c;
         bool occ = false;
         for (int64_t t = 0; t < nt && !occ; ++t) {
             float th;
             occ = tri_test(tris[t], oo, dd, kEpsilon, tf[r], th);
         }
-        if (any_hit<false>(nodes.data(), tris.data(), oo, dd, kEpsilon, tf[r], &status, nullptr) != occ) ++bad_a;
+        if (any_hit<false>(nodes.data(), leaf_tris.data(), oo, dd, kEpsilon, tf[r], &status, nullptr) != occ) ++bad_a;
     }
-    std::printf("depth %d closest_mismatch %lld any_mismatch %lld stack_status %u nodes_per_ray %.2f\n", depth,
-                (long long)bad_c, (long long)bad_a, status, double(cnt.nodes) / double(nr));
+    std::printf("depth %d closest_mismatch %lld any_mismatch %lld stack_status %u nodes_per_ray %.2f "
+                "tris_per_ray %.2f\n",
+                depth, (long long)bad_c, (long long)bad_a, status, double(cnt.nodes) / double(nr),
+                double(cnt.tris) / double(nr));
     return 0;
 }

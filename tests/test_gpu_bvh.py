@@ -1,7 +1,8 @@
 """The device BVH as built on the GPU (PLOC and LBVH topologies).
 
-Structure: a binary tree over all triangles, root 0, every internal node but the root and
-every triangle slot referenced exactly once. Conservativeness: each stored child box
+Structure: a binary tree over all triangles, root 0; the nodes reachable from the root
+are distinct and their leaves (one to eight triangles in consecutive slots) hold every
+triangle slot exactly once. Conservativeness: each stored child box
 contains the padded bounding box of every triangle beneath it, with the padding the build
 applies (max|x| * 4e-6 + 1e-6 per axis), so the FP32 slab test cannot reject a box that a
 hit lies in."""
@@ -30,49 +31,89 @@ def padded_boxes(mesh, tris):
     return mn - pad, mx + pad
 
 
+def leaf_slots(ref):
+    """Slots of a leaf reference (child < 0): ((~c) & 7) + 1 triangles from (~c) >> 3."""
+    r = ~int(ref)
+    return range(r >> 3, (r >> 3) + (r & 7) + 1)
+
+
 def check_tree(be, mesh):
     nt = mesh.triangleCount()
     nodes, tris = be.device_bvh()
     assert len(tris) == nt and len(nodes) == nt - 1
     child = nodes["child"]
-    internal = child[child >= 0]
-    leaves = ~child[child < 0]
-    assert np.array_equal(np.sort(internal), np.arange(1, nt - 1))
-    assert np.array_equal(np.sort(leaves), np.arange(nt))
     lo, hi = child_boxes(nodes)
     tlo, thi = padded_boxes(mesh, tris)
-    # post-order over the tree (explicit stack), subtree boxes bottom-up
-    order, stack = [], [0]
+    # the nodes reachable from the root (pre-order), then subtree boxes bottom-up
+    order, stack, seen_slots = [], [0], []
     while stack:
         i = stack.pop()
         order.append(i)
-        stack.extend(int(c) for c in child[i] if c >= 0)
+        for c in child[i]:
+            if c >= 0:
+                stack.append(int(c))
+            else:
+                seen_slots.extend(leaf_slots(c))
+    # every reachable internal node once, every triangle slot in exactly one leaf
+    assert len(set(order)) == len(order)
+    assert np.array_equal(np.sort(np.array(seen_slots)), np.arange(nt))
     sub_lo = np.zeros((nt - 1, 3), np.float32)
     sub_hi = np.zeros((nt - 1, 3), np.float32)
     for i in reversed(order):
         blo, bhi = [], []
         for k in range(2):
             c = int(child[i, k])
-            cl, ch = (sub_lo[c], sub_hi[c]) if c >= 0 else (tlo[~c], thi[~c])
+            if c >= 0:
+                cl, ch = sub_lo[c], sub_hi[c]
+            else:
+                sl = list(leaf_slots(c))
+                cl, ch = tlo[sl].min(0), thi[sl].max(0)
             assert (lo[i, k] <= cl).all() and (hi[i, k] >= ch).all(), (i, k)
             blo.append(cl)
             bhi.append(ch)
         sub_lo[i] = np.minimum(blo[0], blo[1])
         sub_hi[i] = np.maximum(bhi[0], bhi[1])
-    return nodes
+    leaves = [c for i in order for c in child[i] if c < 0]
+    return nodes, len(order), len(leaves)
 
 
+@pytest.mark.parametrize("leaf", [1, 4, 8])
 @pytest.mark.parametrize("builder", [0, 1], ids=["ploc", "lbvh"])
-def test_device_bvh_contains_padded_triangles(product_lib, builder):
+def test_device_bvh_contains_padded_triangles(product_lib, builder, leaf):
     product_lib.hsr_set_bvh_builder(builder)
+    product_lib.hsr_set_bvh_leaf_size(leaf)
     try:
         for mesh in (scenes.dihedral_mesh(), scenes.sphere_ground_workload(level=3).mesh,
                      scenes.boxes_mesh(seed=3, count=2000)):
             be = gb300.Backend(mesh, None)
-            check_tree(be, mesh)
-            print(mesh.triangleCount(), "triangles, depth", be.bvh_stats()["max_depth"])
+            _, inner, leaves = check_tree(be, mesh)
+            print(mesh.triangleCount(), "triangles, depth", be.bvh_stats()["max_depth"], "reachable nodes", inner,
+                  "leaves", leaves)
+            if leaf == 1:
+                assert leaves == mesh.triangleCount()
     finally:
         product_lib.hsr_set_bvh_builder(0)
+        product_lib.hsr_set_bvh_leaf_size(4)
+
+
+@pytest.mark.parametrize("leaf", [1, 8])
+def test_ray_queries_do_not_depend_on_leaf_size(product_lib, leaf):
+    """The same queries against trees with leaves of one triangle, of up to four (the
+    default) and up to eight: bit-identical answers."""
+    mesh = scenes.boxes_mesh(seed=4, count=3000)
+    rng = np.random.default_rng(7)
+    v = np.asarray(mesh.vertexBuffer, np.float32)
+    o = rng.uniform(v.min(0), v.max(0), (20000, 3)).astype(np.float32)
+    d = rng.normal(size=(20000, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    ref = gb300.Backend(mesh, None).intersect(o, d)
+    product_lib.hsr_set_bvh_leaf_size(leaf)
+    try:
+        got = gb300.Backend(mesh, None).intersect(o, d)
+    finally:
+        product_lib.hsr_set_bvh_leaf_size(4)
+    for a, b in zip(got, ref):
+        assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
 
 
 def test_single_triangle_scene(product_lib):

@@ -1,6 +1,7 @@
 """The device traversal code on the CPU: hussar_gb300/csrc/hsr_traverse.cuh compiled with
 g++ through host definitions of the CUDA intrinsics (tests/native/host_shim.h), over a
-binary tree in the kernels' node layout; every closest-hit and any-hit answer is compared
+binary tree in the kernels' node layout (leaves of one or several triangles); every
+closest-hit and any-hit answer is compared
 with brute force over all triangles (same triangle test and tie rule). Catches traversal
 logic errors without a GPU."""
 import os
@@ -28,7 +29,7 @@ def checker(tmp_path_factory):
     return exe
 
 
-def run(checker, tmp_path, mesh, rays, seed):
+def run(checker, tmp_path, mesh, rays, seed, leaf=1):
     rng = np.random.default_rng(seed)
     v = np.asarray(mesh.vertexBuffer, np.float32)
     f = np.asarray(mesh.indexBuffer, np.int32)
@@ -48,17 +49,21 @@ def run(checker, tmp_path, mesh, rays, seed):
         fh.write(np.array([len(v), len(f), rays], np.int64).tobytes())
         for a in (v, f, o, d, tf):
             fh.write(np.ascontiguousarray(a).tobytes())
-    out = subprocess.run([checker, str(path)], check=True, capture_output=True, text=True).stdout.split()
+    out = subprocess.run([checker, str(path), str(leaf)], check=True, capture_output=True,
+                         text=True).stdout.split()
     res = {out[i]: float(out[i + 1]) for i in range(0, len(out), 2)}
     print(res)
     return res
 
 
+@pytest.mark.parametrize("leaf", [1, 3, 8])
 @pytest.mark.parametrize("name", ["dihedral", "sphere", "boxes"])
-def test_traversal_matches_brute_force(checker, tmp_path, name):
+def test_traversal_matches_brute_force(checker, tmp_path, name, leaf):
+    """Leaves of one triangle and of several (consecutive slots, the leaf reference's
+    count in its low three bits)."""
     mesh = {"dihedral": lambda: scenes.dihedral_mesh(),
             "sphere": lambda: scenes.sphere_ground_workload(level=3).mesh,
             "boxes": lambda: scenes.boxes_mesh(seed=5, count=400, extent=30.0)}[name]()
-    res = run(checker, tmp_path, mesh, 3000, seed=len(name))
+    res = run(checker, tmp_path, mesh, 3000, seed=len(name), leaf=leaf)
     assert res["closest_mismatch"] == 0 and res["any_mismatch"] == 0
     assert res["stack_status"] == 0
