@@ -387,9 +387,11 @@ hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs);
 
 /* Copies the scene's device BVH to the host (tests): out_nodes receives node_count binary
  * nodes of 64 bytes each, both child boxes and child references (layout in
- * hussar_gb300/csrc/hsr_common.cuh, struct DNode; a negative reference c is triangle slot
- * ~c), out_tris triangle_count 48-byte records {v0.xyz, original id bits, v1-v0, 0,
- * v2-v0, 0} in slot order. Either pointer may be null; capacities are in records. */
+ * hussar_gb300/csrc/hsr_common.cuh, struct DNode; a negative reference c is a leaf of
+ * ((~c) & 7) + 1 triangles in consecutive slots from (~c) >> 3; nodes inside collapsed
+ * leaves stay in the array, unreachable), out_tris triangle_count 48-byte records
+ * {v0.xyz, original id bits, v1-v0, 0, v2-v0, 0} in slot order. Either pointer may be
+ * null; capacities are in records. */
 hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_capacity, void *out_tris,
                          int64_t tri_capacity);
 
