@@ -67,3 +67,47 @@ def test_traversal_matches_brute_force(checker, tmp_path, name, leaf):
     res = run(checker, tmp_path, mesh, 3000, seed=len(name), leaf=leaf)
     assert res["closest_mismatch"] == 0 and res["any_mismatch"] == 0
     assert res["stack_status"] == 0
+
+
+def far_rays(checker, tmp_path, mesh, rays, seed, distance, offset=0.0):
+    """Rays from a sphere of `distance` around the scene's centre aimed at random points of
+    the scene (the far-field disk of the RCS runs): the quantised boxes' margin and the
+    exit-distance slack must hold for origins far outside the grid."""
+    rng = np.random.default_rng(seed)
+    v = np.asarray(mesh.vertexBuffer, np.float32) + np.float32(offset)
+    m = type(mesh)()
+    m.append(v, np.asarray(mesh.indexBuffer, np.int32).reshape(-1, 3))
+    lo, hi = v.min(0), v.max(0)
+    c = 0.5 * (lo + hi)
+    u = rng.normal(size=(rays, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    o = (c + distance * u).astype(np.float32)
+    target = rng.uniform(lo, hi, (rays, 3))
+    d = target - o
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tf = np.full(rays, 2 * distance, np.float32)
+    path = tmp_path / ("far%d.bin" % seed)
+    with open(path, "wb") as fh:
+        fh.write(np.array([len(v), len(m.indexBuffer), rays], np.int64).tobytes())
+        for a in (v, np.asarray(m.indexBuffer, np.int32), o, d, tf):
+            fh.write(np.ascontiguousarray(a).tobytes())
+    out = subprocess.run([checker, str(path), "4"], check=True, capture_output=True, text=True).stdout.split()
+    return {out[i]: float(out[i + 1]) for i in range(0, len(out), 2)}
+
+
+@pytest.mark.parametrize("distance,offset", [(20.0, 0.0), (200.0, 0.0), (5.0, 1e4)])
+@pytest.mark.parametrize("name", ["dihedral", "icosphere"])
+def test_far_and_offset_rays_match_brute_force(checker, tmp_path, name, distance, offset):
+    """A 10 cm dihedral and a 10 cm icosphere of 1280 triangles seen from 20 m and 200 m
+    (200 and 2000 scene extents), and from 5 m with the scene 10 km from the coordinate
+    origin."""
+    if name == "dihedral":
+        mesh = scenes.dihedral_mesh()
+    else:
+        from hussar_gb300 import TriangleMesh
+        v, f = scenes.icosphere(3, radius=0.05)
+        mesh = TriangleMesh()
+        mesh.append(v, f)
+    res = far_rays(checker, tmp_path, mesh, 4000, 11, distance, offset)
+    print(res)
+    assert res["closest_mismatch"] == 0 and res["any_mismatch"] == 0
