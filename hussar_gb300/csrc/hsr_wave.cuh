@@ -34,6 +34,10 @@ namespace hsr {
 namespace {
 
 constexpr int kThreads = 256;
+// GENERATE hands its samples to threads grouped by the cell of their primary sample point
+// (4 x 2 cells of the unit square): a warp's primary rays leave the antenna in one part
+// of the sphere, and their hits, pushed together, come back as neighbouring stack entries
+constexpr int kPrimaryCells = 8;
 
 // A CTA's live path states: a stack of kThreads + kQueue entries, where kQueue bounds the
 // paths left when GENERATE runs (the queue threshold). Three capacities are built: 384
@@ -56,6 +60,9 @@ template <int kCap> struct WaveShared {
     long long gen, gen_end, pending_first, pending_last;
     long long since_flush;      // samples generated since the row was last flushed
     PoseJob job;                // mixed batches: the current pose's scene, chirp and row
+    int cell_count[kThreads / 32][kPrimaryCells];  // GENERATE: samples per warp and cell
+    int cell_total[kPrimaryCells];
+    short order[kThreads];      // GENERATE: stage sample offset of each thread
     FfAnt ff[2];                // far-field launches: the current pose's TX and RX
     float max_dist, bandwidth;  // mixed batches: derived from job.rf
 };
@@ -235,7 +242,39 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 S.gen = min(gen + (long long)kThreads, gen_end);
                 S.since_flush += S.gen - gen;
             }
-            const long long s = gen + tid;
+            // the stage's samples gen + [0, n), ordered by primary cell (stable, the same
+            // order in every run): thread t traces sample gen + S.order[t]
+            const int n_stage = int(min((long long)kThreads, gen_end - gen));
+            {
+                const int warp = tid >> 5, lane = tid & 31;
+                int key = kPrimaryCells;
+                if (tid < n_stage) {
+                    const uint64_t h0 = uint64_t(pc.offset + gen + tid);
+                    const float u0 = halton(h0, 1 + kGet2DFirst), u1 = halton(h0, 1 + kGet2DSecond);
+                    key = min(int(u0 * 4.f), 3) * 2 + min(int(u1 * 2.f), 1);
+                }
+                const unsigned peers = __match_any_sync(0xffffffffu, key);
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                if (lane < kPrimaryCells) S.cell_count[warp][lane] = 0;
+                __syncwarp();
+                if (rank == 0 && key < kPrimaryCells) S.cell_count[warp][key] = __popc(peers);
+                __syncthreads();
+                if (tid < kPrimaryCells) {
+                    int t = 0;
+#pragma unroll
+                    for (int w = 0; w < kThreads / 32; ++w) t += S.cell_count[w][tid];
+                    S.cell_total[tid] = t;
+                }
+                __syncthreads();
+                if (key < kPrimaryCells) {
+                    int base = rank;
+                    for (int k = 0; k < key; ++k) base += S.cell_total[k];
+                    for (int w = 0; w < warp; ++w) base += S.cell_count[w][key];
+                    S.order[base] = short(tid);  // < n_stage: the keyed samples are the stage's
+                }
+                __syncthreads();
+            }
+            const long long s = gen + (tid < n_stage ? S.order[tid] : tid);
             bool has_item = false;
             float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
             if (s < gen_end) {
