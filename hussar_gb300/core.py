@@ -305,6 +305,18 @@ class _GB300:
             it.frame.data = buf.view(np.complex64).reshape(it.frame.data.shape)
             it.totalWeight = tw.value
 
+        def refit(self, mesh):
+            """New vertex positions of the same mesh (hsr_scene_refit): the BVH keeps its
+            tree and refits its boxes."""
+            v = np.ascontiguousarray(mesh.vertexBuffer, np.float32)
+            _lib.check(_lib.lib().hsr_scene_refit(self._scene, _lib.ptr(v), len(v)))
+
+        def rebuild(self, mesh):
+            """A new mesh under this backend's scene handle (hsr_scene_rebuild)."""
+            v = np.ascontiguousarray(mesh.vertexBuffer, np.float32)
+            i = np.ascontiguousarray(mesh.indexBuffer, np.int32)
+            _lib.check(_lib.lib().hsr_scene_rebuild(self._scene, _lib.ptr(v), len(v), _lib.ptr(i), len(i)))
+
         def footprint(self):
             out = ctypes.c_int64()
             _lib.check(_lib.lib().hsr_scene_footprint(self._scene, ctypes.byref(out)))

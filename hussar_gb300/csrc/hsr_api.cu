@@ -575,10 +575,12 @@ hsr_status hsr_scene_create(const float *vertices, int64_t vertex_count, const i
     }
     int rc = bvh_build(d, dv, vertex_count, di, triangle_count, 0, err);
     cudaFree(dv);
-    cudaFree(di);
+    d.indices = di;  // kept for refits
+    d.vertex_count = vertex_count;
     if (rc != 0) {
         cudaFree(d.tris);
         cudaFree(d.nodes);
+        cudaFree(d.indices);
         delete s;
         return fail(rc == 3 ? HSR_ERR_OUT_OF_MEMORY : rc == 4 ? HSR_ERR_INVALID_ARGUMENT : HSR_ERR_CUDA, err);
     }
@@ -593,6 +595,8 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
     cudaDeviceSynchronize();
     cudaFree(s->dev.tris);
     cudaFree(s->dev.nodes);
+    cudaFree(s->dev.indices);
+    cudaFree(s->dev.refit_order);
     cudaFree(s->dev.scratch);
     cudaFree(s->dev.guide);
     synth_free_operand(s->dev.synth);
@@ -604,9 +608,69 @@ hsr_status hsr_scene_destroy(hsr_scene *s) {
     return HSR_OK;
 }
 
+hsr_status hsr_scene_refit(hsr_scene *s, const float *vertices, int64_t vertex_count) {
+    if (!s || (vertex_count > 0 && !vertices)) return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
+    if (vertex_count != s->dev.vertex_count)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "refit needs the scene's " + std::to_string(s->dev.vertex_count) +
+                                                  " vertices, got " + std::to_string(vertex_count));
+    for (int64_t i = 0; i < 3 * vertex_count; ++i)
+        if (!std::isfinite(vertices[i]))
+            return fail(HSR_ERR_INVALID_ARGUMENT, "vertex " + std::to_string(i / 3) + " is not finite");
+    hsr_status st = check_device();
+    if (st != HSR_OK) return st;
+    std::lock_guard<std::mutex> lk(s->mu);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != s->dev.device) return fail(HSR_ERR_INVALID_ARGUMENT, "the scene lives on another device");
+    float *dv = nullptr;
+    std::string err;
+    if (!dev_alloc(&dv, sizeof(float) * 3 * std::max<int64_t>(vertex_count, 1), err))
+        return fail(HSR_ERR_OUT_OF_MEMORY, err);
+    cudaError_t e = cudaDeviceSynchronize();  // no call on the scene is still reading its BVH
+    if (e == cudaSuccess && vertex_count)
+        e = cudaMemcpy(dv, vertices, sizeof(float) * 3 * vertex_count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(dv);
+        return cuda_fail(e, "vertex upload");
+    }
+    const int rc = bvh_refit(s->dev, dv, 0, err);
+    cudaFree(dv);
+    if (rc != 0) return fail(rc == 3 ? HSR_ERR_OUT_OF_MEMORY : HSR_ERR_CUDA, err);
+    return HSR_OK;
+}
+
+hsr_status hsr_scene_rebuild(hsr_scene *s, const float *vertices, int64_t vertex_count, const int32_t *indices,
+                             int64_t triangle_count) {
+    if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    // a new scene with the same handle: built aside, then swapped in under the scene lock
+    hsr_scene *fresh = nullptr;
+    hsr_status st = hsr_scene_create(vertices, vertex_count, indices, triangle_count, &fresh);
+    if (st != HSR_OK) return st;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (fresh->dev.device != s->dev.device) {
+            hsr_scene_destroy(fresh);
+            return fail(HSR_ERR_INVALID_ARGUMENT, "the scene lives on another device");
+        }
+        cudaDeviceSynchronize();  // no call on the scene is still reading its BVH
+        SceneDev &a = s->dev, &b = fresh->dev;
+        std::swap(a.tri_count, b.tri_count);
+        std::swap(a.node_count, b.node_count);
+        std::swap(a.leaf_count, b.leaf_count);
+        std::swap(a.max_depth, b.max_depth);
+        std::swap(a.tris, b.tris);
+        std::swap(a.nodes, b.nodes);
+        std::swap(a.indices, b.indices);
+        std::swap(a.vertex_count, b.vertex_count);
+        std::swap(a.refit_order, b.refit_order);
+        std::swap(a.refit_levels, b.refit_levels);
+    }
+    return hsr_scene_destroy(fresh);  // frees the old BVH, now held by `fresh`
+}
+
 hsr_status hsr_scene_footprint(const hsr_scene *s, int64_t *out_bytes) {
     if (!s || !out_bytes) return fail(HSR_ERR_INVALID_ARGUMENT, "null argument");
-    *out_bytes = int64_t(sizeof(DTri)) * std::max<int64_t>(s->dev.tri_count, 1) +
+    *out_bytes = int64_t(sizeof(DTri) + 3 * sizeof(int32_t)) * std::max<int64_t>(s->dev.tri_count, 1) +
                  int64_t(sizeof(DNode)) * s->dev.node_count + int64_t(s->dev.scratch_bytes) +
                  int64_t(guide_bytes_per_pose()) * s->dev.guide_cap;
     return HSR_OK;

@@ -756,4 +756,123 @@ int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, i
     return rc;
 }
 
+namespace {
+
+// Triangle records of new vertex positions: slot s keeps its triangle (the original id in
+// v0.w), as k_write_tris forms them.
+__global__ void k_refit_tris(int64_t nt, const float *__restrict__ v, const int32_t *__restrict__ idx,
+                             DTri *__restrict__ tris) {
+    const int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (s >= nt) return;
+    const float idbits = tris[s].v0.w;
+    const int64_t t = __float_as_int(idbits);
+    const float *p0 = v + 3 * int64_t(idx[3 * t + 0]);
+    const float *p1 = v + 3 * int64_t(idx[3 * t + 1]);
+    const float *p2 = v + 3 * int64_t(idx[3 * t + 2]);
+    DTri T;
+    T.v0 = make_float4(p0[0], p0[1], p0[2], idbits);
+    T.e1 = make_float4(p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2], 0.f);
+    T.e2 = make_float4(p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2], 0.f);
+    tris[s] = T;
+}
+
+// One level of the bottom-up refit: each node's two child boxes from its children (a
+// leaf: the padded boxes of its triangles, as k_bounds pads them; a node: the union of
+// its own two boxes, refitted one level deeper).
+__global__ void k_refit_level(int64_t count, const int32_t *__restrict__ order, DNode *nodes,
+                              const DTri *__restrict__ tris, const float *__restrict__ v,
+                              const int32_t *__restrict__ idx) {
+    const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (k >= count) return;
+    const int i = order[k];
+    const int c[2] = {nodes[i].d.x, nodes[i].d.y};
+    Box bx[2];
+    for (int w = 0; w < 2; ++w) {
+        for (int a = 0; a < 3; ++a) {
+            bx[w].lo[a] = __int_as_float(0x7f800000);
+            bx[w].hi[a] = -__int_as_float(0x7f800000);
+        }
+        if (c[w] < 0) {
+            const int ref = ~c[w];
+            for (int slot = ref >> 3; slot <= (ref >> 3) + (ref & 7); ++slot) {
+                const int64_t t = __float_as_int(tris[slot].v0.w);
+                for (int a = 0; a < 3; ++a) {
+                    const float x0 = v[3 * int64_t(idx[3 * t + 0]) + a];
+                    const float x1 = v[3 * int64_t(idx[3 * t + 1]) + a];
+                    const float x2 = v[3 * int64_t(idx[3 * t + 2]) + a];
+                    const float mn = fminf(x0, fminf(x1, x2)), mx = fmaxf(x0, fmaxf(x1, x2));
+                    const float pad = fmaxf(fabsf(mn), fabsf(mx)) * 4e-6f + 1e-6f;
+                    bx[w].lo[a] = fminf(bx[w].lo[a], mn - pad);
+                    bx[w].hi[a] = fmaxf(bx[w].hi[a], mx + pad);
+                }
+            }
+        } else {
+            const DNode cn = nodes[c[w]];
+            const Box b0 = child_box(cn, 0), b1 = child_box(cn, 1);
+            for (int a = 0; a < 3; ++a) {
+                bx[w].lo[a] = fminf(b0.lo[a], b1.lo[a]);
+                bx[w].hi[a] = fmaxf(b0.hi[a], b1.hi[a]);
+            }
+        }
+    }
+    DNode &n = nodes[i];
+    n.a = make_float4(bx[0].lo[0], bx[0].hi[0], bx[0].lo[1], bx[0].hi[1]);
+    n.b = make_float4(bx[1].lo[0], bx[1].hi[0], bx[1].lo[1], bx[1].hi[1]);
+    n.c = make_float4(bx[0].lo[2], bx[0].hi[2], bx[1].lo[2], bx[1].hi[2]);
+}
+
+}  // namespace
+
+int bvh_refit(SceneDev &s, const float *d_v, cudaStream_t st, std::string &err) {
+    const int64_t nt = s.tri_count;
+    if (nt < 2) {  // the one-node tree of 0 or 1 triangle: built again
+        cudaFree(s.tris);
+        cudaFree(s.nodes);
+        s.tris = nullptr;
+        s.nodes = nullptr;
+        return bvh_build(s, d_v, s.vertex_count, s.indices, nt, st, err);
+    }
+    if (!s.refit_order) {
+        // the reachable internal nodes, level by level from the root (host breadth-first
+        // walk over the child references)
+        std::vector<DNode> h(size_t(s.node_count));
+        if (cudaMemcpy(h.data(), s.nodes, sizeof(DNode) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            err = "refit: node download failed";
+            return 2;
+        }
+        std::vector<int32_t> order{0}, next;
+        std::vector<int64_t> levels{0};
+        size_t begin = 0;
+        while (begin < order.size()) {
+            const size_t end = order.size();
+            for (size_t k = begin; k < end; ++k)
+                for (int c : {h[order[k]].d.x, h[order[k]].d.y})
+                    if (c >= 0) order.push_back(c);
+            levels.push_back(int64_t(end));
+            begin = end;
+        }
+        if (!dev_alloc(&s.refit_order, sizeof(int32_t) * order.size(), err)) return 3;
+        if (cudaMemcpy(s.refit_order, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            err = "refit: order upload failed";
+            return 2;
+        }
+        s.refit_levels = levels;
+    }
+    const int T = 256;
+    k_refit_tris<<<blocks_for(nt, T), T, 0, st>>>(nt, d_v, s.indices, s.tris);
+    note_launches(1);
+    for (size_t l = s.refit_levels.size() - 1; l-- > 0;) {  // deepest level first
+        const int64_t b = s.refit_levels[l], e = s.refit_levels[l + 1];
+        k_refit_level<<<blocks_for(e - b, T), T, 0, st>>>(e - b, s.refit_order + b, s.nodes, s.tris, d_v, s.indices);
+        note_launches(1);
+    }
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        err = std::string("BVH refit: ") + cudaGetErrorString(e);
+        return 2;
+    }
+    return 0;
+}
+
 }  // namespace hsr

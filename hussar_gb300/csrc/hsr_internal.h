@@ -50,6 +50,13 @@ struct SceneDev {
     int max_depth = 0;
     DTri *tris = nullptr;
     DNode *nodes = nullptr;
+    // the mesh's triangle vertex indices (kept for refits) and vertex count
+    int32_t *indices = nullptr;
+    int64_t vertex_count = 0;
+    // refit order: the BVH's reachable internal nodes level by level from the root
+    // (built at the first refit), and where each level starts
+    int32_t *refit_order = nullptr;
+    std::vector<int64_t> refit_levels;
     // scratch
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -104,6 +111,9 @@ void set_last_error(const std::string &msg);
 
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
               std::string &err);
+// New vertex positions for the scene's mesh (same triangles): triangle records rewritten
+// and every node box refitted bottom-up over the existing topology. Returns 0, 2 or 3.
+int bvh_refit(SceneDev &s, const float *d_v, cudaStream_t st, std::string &err);
 
 // Per-pose scene, chirp and accumulator row of a mixed batch (the serving loop): poses
 // of one launch may trace different resident scenes with different RF configurations

@@ -906,7 +906,8 @@ hsr_status hsr_server_get_stats(hsr_server *s, hsr_server_stats *o) {
     o->admitted_while_busy = s->st_while_busy;
     o->memory_bytes_peak = s->st_mem_peak;
     for (const SceneDev *sd : s->scenes)
-        o->scene_bytes += sd->tri_count * int64_t(sizeof(DTri)) + sd->node_count * int64_t(sizeof(DNode));
+        o->scene_bytes += sd->tri_count * int64_t(sizeof(DTri) + 3 * sizeof(int32_t)) +
+                          sd->node_count * int64_t(sizeof(DNode));
     if (!s->latencies.empty()) {
         std::vector<double> v = s->latencies;
         auto pct = [&](double q) {

@@ -159,7 +159,21 @@ hsr_status hsr_scene_create(const float *vertices, int64_t vertex_count,
                             const int32_t *indices, int64_t triangle_count,
                             hsr_scene **out_scene);
 hsr_status hsr_scene_destroy(hsr_scene *scene);
-/* Device bytes held by the scene (vertices, triangles, BVH nodes). */
+
+/* Scene changes for resident scenes (the serving pool keeps scene handles): the
+ * reference builds its Embree scene or OptiX acceleration structure once per Backend
+ * (src/arch/cpu.cpp:32-47, src/arch/gpu.cpp:482-493) and has no update.
+ * hsr_scene_refit: new positions for the scene's vertices (the same count; the triangles
+ *   keep their vertex indices): the triangle records are rewritten and every BVH box is
+ *   refitted bottom-up over the existing tree (ray-query answers are exact whatever the
+ *   tree; a tree refitted after large motions only traverses more slowly).
+ * hsr_scene_rebuild: a new mesh under the same handle (a full build, then swapped in).
+ * Both wait for the device first, and must not overlap a call or a serving tick that
+ * uses the scene. */
+hsr_status hsr_scene_refit(hsr_scene *scene, const float *vertices, int64_t vertex_count);
+hsr_status hsr_scene_rebuild(hsr_scene *scene, const float *vertices, int64_t vertex_count,
+                             const int32_t *indices, int64_t triangle_count);
+/* Device bytes held by the scene (triangle records and vertex indices, BVH nodes). */
 hsr_status hsr_scene_footprint(const hsr_scene *scene, int64_t *out_bytes);
 /* BVH statistics for tests: node count, maximum depth, leaf count. */
 hsr_status hsr_scene_bvh_stats(const hsr_scene *scene, int64_t *out_nodes,
