@@ -473,6 +473,7 @@ using namespace hsr;
 struct hsr_scene {
     SceneDev dev;
     std::mutex mu;
+    std::atomic<int> graphs{0};  // live captured graphs (they hold the BVH's pointers)
 };
 
 namespace hsr {
@@ -642,6 +643,8 @@ hsr_status hsr_scene_refit(hsr_scene *s, const float *vertices, int64_t vertex_c
 hsr_status hsr_scene_rebuild(hsr_scene *s, const float *vertices, int64_t vertex_count, const int32_t *indices,
                              int64_t triangle_count) {
     if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
+    if (s->graphs.load() > 0)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "the scene has captured graphs (they hold its BVH): destroy them first");
     // a new scene with the same handle: built aside, then swapped in under the scene lock
     hsr_scene *fresh = nullptr;
     hsr_status st = hsr_scene_create(vertices, vertex_count, indices, triangle_count, &fresh);
@@ -1537,6 +1540,7 @@ hsr_status hsr_batch_graph_create(hsr_scene *s, const hsr_rf_config *rf, int32_t
             }
     }
     cudaGetLastError();
+    s->graphs.fetch_add(1);
     *out = g.release();
     return HSR_OK;
 }
@@ -1563,6 +1567,7 @@ hsr_status hsr_batch_graph_status(hsr_batch_graph *g) {
 hsr_status hsr_batch_graph_destroy(hsr_batch_graph *g) {
     if (!g) return HSR_OK;
     cudaDeviceSynchronize();
+    if (g->scene) g->scene->graphs.fetch_sub(1);
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     cudaFree(g->scratch);

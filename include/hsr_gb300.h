@@ -167,7 +167,9 @@ hsr_status hsr_scene_destroy(hsr_scene *scene);
  *   keep their vertex indices): the triangle records are rewritten and every BVH box is
  *   refitted bottom-up over the existing tree (ray-query answers are exact whatever the
  *   tree; a tree refitted after large motions only traverses more slowly).
- * hsr_scene_rebuild: a new mesh under the same handle (a full build, then swapped in).
+ * hsr_scene_rebuild: a new mesh under the same handle (a full build, then swapped in);
+ *   refused (HSR_ERR_INVALID_ARGUMENT) while batch graphs captured on the scene exist,
+ *   since they hold the old BVH's device addresses.
  * Both wait for the device first, and must not overlap a call or a serving tick that
  * uses the scene. */
 hsr_status hsr_scene_refit(hsr_scene *scene, const float *vertices, int64_t vertex_count);

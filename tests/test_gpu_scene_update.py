@@ -94,3 +94,33 @@ def test_refit_rejects_a_different_vertex_count(product_lib):
     bad = np.asarray(scenes.dihedral_mesh().vertexBuffer, np.float32).copy()
     bad[0, 0] = np.nan
     assert _lib.lib().hsr_scene_refit(be.handle, _lib.ptr(bad), len(bad)) == _lib.HSR_ERR_INVALID_ARGUMENT
+
+
+def test_rebuild_refused_while_a_graph_holds_the_scene(product_lib):
+    """A captured graph keeps the BVH's device pointers: rebuild waits for it to go."""
+    torch = pytest.importorskip("torch")
+    from hussar_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    w = scenes.dihedral_workload(poses=2)
+    be = gb300.Backend(w.mesh, None)
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    P, N = 2, 256
+    tx = (_lib.AntennaC * P)(*[a.to_c() for a in w.tx])
+    rx = (_lib.AntennaC * P)(*[a.to_c() for a in w.rx])
+    d_tx = torch.frombuffer(bytearray(bytes(tx)), dtype=torch.uint8).to(dev)
+    d_rx = torch.frombuffer(bytearray(bytes(rx)), dtype=torch.uint8).to(dev)
+    d_b = torch.full((P,), 1 << 10, dtype=torch.int64, device=dev)
+    d_o = torch.zeros(P, dtype=torch.int64, device=dev)
+    d_out = torch.zeros(2 * P * N, dtype=torch.float32, device=dev)
+    g = be.batch_graph(w.rf, N, t, P, d_tx.data_ptr(), d_rx.data_ptr(), d_b.data_ptr(), d_o.data_ptr(),
+                       d_out.data_ptr())
+    m2 = scenes.boxes_mesh(seed=9, count=50, extent=5.0)
+    v = np.ascontiguousarray(m2.vertexBuffer, np.float32)
+    i = np.ascontiguousarray(m2.indexBuffer, np.int32)
+    assert _lib.lib().hsr_scene_rebuild(be.handle, _lib.ptr(v), len(v), _lib.ptr(i), len(i)) == \
+        _lib.HSR_ERR_INVALID_ARGUMENT
+    g.close()
+    be.rebuild(m2)
+    assert be.bvh_stats()["leaves"] == m2.triangleCount()
