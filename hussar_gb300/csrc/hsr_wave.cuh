@@ -118,6 +118,34 @@ __device__ __forceinline__ void push_path(WaveShared<kCap> &S, float *gst, f3 o,
     }
 }
 
+// A stable counting sort of the stage's items by key (< kPrimaryCells; the items
+// [0, n) of the stage, thread t holding item t's key, threads t >= n holding
+// kPrimaryCells): afterwards S.order[j] is the item thread j works on, for j < n. The
+// order is the same in every run. Called by the whole CTA.
+template <int kCap> __device__ __forceinline__ void order_by_key(WaveShared<kCap> &S, int key) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (lane < kPrimaryCells) S.cell_count[warp][lane] = 0;
+    __syncwarp();
+    if (rank == 0 && key < kPrimaryCells) S.cell_count[warp][key] = __popc(peers);
+    __syncthreads();
+    if (tid < kPrimaryCells) {
+        int t = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) t += S.cell_count[w][tid];
+        S.cell_total[tid] = t;
+    }
+    __syncthreads();
+    if (key < kPrimaryCells) {
+        int base = rank;
+        for (int k = 0; k < key; ++k) base += S.cell_total[k];
+        for (int w = 0; w < warp; ++w) base += S.cell_count[w][key];
+        S.order[base] = short(tid);  // < n: the keyed items are the stage's
+    }
+    __syncthreads();
+}
+
 // Closest hit of the segment (o, d) and the bookkeeping of path.h:407-442 (GO mode).
 // Returns true (and the new state) when the path continues with a stored hit. The
 // reference's zero-field test (path.h:413, 439) is the caller's: in GO mode the field
@@ -242,37 +270,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 S.gen = min(gen + (long long)kThreads, gen_end);
                 S.since_flush += S.gen - gen;
             }
-            // the stage's samples gen + [0, n), ordered by primary cell (stable, the same
-            // order in every run): thread t traces sample gen + S.order[t]
+            // the stage's samples gen + [0, n), ordered by primary cell: thread t traces
+            // sample gen + S.order[t]
             const int n_stage = int(min((long long)kThreads, gen_end - gen));
             {
-                const int warp = tid >> 5, lane = tid & 31;
                 int key = kPrimaryCells;
                 if (tid < n_stage) {
                     const uint64_t h0 = uint64_t(pc.offset + gen + tid);
                     const float u0 = halton(h0, 1 + kGet2DFirst), u1 = halton(h0, 1 + kGet2DSecond);
                     key = min(int(u0 * 4.f), 3) * 2 + min(int(u1 * 2.f), 1);
                 }
-                const unsigned peers = __match_any_sync(0xffffffffu, key);
-                const int rank = __popc(peers & ((1u << lane) - 1u));
-                if (lane < kPrimaryCells) S.cell_count[warp][lane] = 0;
-                __syncwarp();
-                if (rank == 0 && key < kPrimaryCells) S.cell_count[warp][key] = __popc(peers);
-                __syncthreads();
-                if (tid < kPrimaryCells) {
-                    int t = 0;
-#pragma unroll
-                    for (int w = 0; w < kThreads / 32; ++w) t += S.cell_count[w][tid];
-                    S.cell_total[tid] = t;
-                }
-                __syncthreads();
-                if (key < kPrimaryCells) {
-                    int base = rank;
-                    for (int k = 0; k < key; ++k) base += S.cell_total[k];
-                    for (int w = 0; w < warp; ++w) base += S.cell_count[w][key];
-                    S.order[base] = short(tid);  // < n_stage: the keyed samples are the stage's
-                }
-                __syncthreads();
+                order_by_key(S, key);
             }
             const long long s = gen + (tid < n_stage ? S.order[tid] : tid);
             bool has_item = false;
@@ -345,8 +353,21 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             int depth = 0;
             double plen = 0.0;
             Guided g{0.f, 0.f, 1.f, cf{0.f, 0.f}};
+            // the popped paths, ordered by the octant of their reflected direction: thread t
+            // continues stack entry count - 1 - S.order[t]
+            {
+                int key = kPrimaryCells;
+                if (mine) {
+                    const int e = count - 1 - tid;
+                    const f3 di = mk3(S.dx[e], S.dy[e], S.dz[e]), nn = mk3(S.nx[e], S.ny[e], S.nz[e]);
+                    const float dn = 2.f * dot3(di, nn);
+                    key = (di.x - dn * nn.x < 0.f ? 1 : 0) | (di.y - dn * nn.y < 0.f ? 2 : 0) |
+                          (di.z - dn * nn.z < 0.f ? 4 : 0);
+                }
+                order_by_key(S, key);
+            }
             if (mine) {
-                const int slot = count - 1 - tid;
+                const int slot = count - 1 - S.order[tid];
                 if (gst)
                     g = Guided{gst[slot], gst[kCap + slot], gst[2 * kCap + slot],
                                cf{gst[3 * kCap + slot], gst[4 * kCap + slot]}};
