@@ -487,10 +487,11 @@ def run_batched(args, rank, world, local_rank, dist):
     # the product's autotuner picks the launch shape on a bounded sample of the batch (16
     # poses, budgets capped at 2^20); the graph below is captured with it
     if args.launch_config:  # a fixed shape (profiling runs reproduce the tuned one without tuning)
-        tile, ctas, thr, foh = (int(x) for x in args.launch_config.split(","))
-        be.set_launch_config(tile, ctas, thr, foh)
-        tuned = dict(tile=tile, ctas_per_sm=ctas, queue_threshold=thr, field_on_hit=foh, trace_ms=None,
-                     default_trace_ms=None)
+        vals = [int(x) for x in args.launch_config.split(",")] + [0]
+        tile, ctas, thr, foh, coh = vals[:5]
+        be.set_launch_config(tile, ctas, thr, foh, coh)
+        tuned = dict(tile=tile, ctas_per_sm=ctas, queue_threshold=thr, field_on_hit=foh, coherent_order=coh,
+                     trace_ms=None, default_trace_ms=None)
     else:
         tuned = be.autotune(w.rf, N, t, w.tx[:16], w.rx[:16], np.minimum(w.budget[:16], 1 << 20), phase_mode=phase,
                             splat_mode=splat)
@@ -627,7 +628,8 @@ def run_batched(args, rank, world, local_rank, dist):
                    "range_bins": N, "phase": "split-fp64", "splat": "fine histogram + split-BF16 tcgen05 synthesis",
                    "launch": "captured CUDA graph (hsr_batch_graph_*), one persistent trace launch per step",
                    "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas x%d" % world,
-                   "launch_config": {k: tuned[k] for k in ("tile", "ctas_per_sm", "queue_threshold", "field_on_hit")},
+                   "launch_config": {k: tuned[k] for k in ("tile", "ctas_per_sm", "queue_threshold", "field_on_hit",
+                                                           "coherent_order")},
                    "autotune_trace_ms": [tuned["default_trace_ms"], tuned["trace_ms"]]},
         "e2e": {"value": world * timed_paths / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s / args.steps,
@@ -1228,7 +1230,8 @@ def main():
                     choices=["boxes", "sphere", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--launch-config", default=None,
-                    help="boxes workload: tile,ctas_per_sm,queue_threshold,field_on_hit instead of autotuning")
+                    help="boxes workload: tile,ctas_per_sm,queue_threshold,field_on_hit[,coherent_order] instead of "
+                         "autotuning")
     ap.add_argument("--max-log2", type=int, default=None,
                     help="boxes workload: cap every budget at 2^k (small profiling cases only)")
     ap.add_argument("--traffic", type=float, default=None,

@@ -95,7 +95,8 @@ class ServerStatsC(ctypes.Structure):
 
 class LaunchConfigC(ctypes.Structure):
     _fields_ = [("tile", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("queue_threshold", ctypes.c_int32),
-                ("trace_ms", ctypes.c_float), ("default_trace_ms", ctypes.c_float), ("field_on_hit", ctypes.c_int32)]
+                ("trace_ms", ctypes.c_float), ("default_trace_ms", ctypes.c_float), ("field_on_hit", ctypes.c_int32),
+                ("coherent_order", ctypes.c_int32)]
 
 
 # PathRecord in hsr_trace.cu / hsr_debug_records

@@ -442,9 +442,11 @@ class _GB300:
                 int(phase_mode), int(splat_mode), ctypes.byref(out)))
             return {name: getattr(out, name) for name, _ in _lib.LaunchConfigC._fields_}
 
-        def set_launch_config(self, tile=0, ctas_per_sm=0, queue_threshold=0, field_on_hit=0, default=False):
+        def set_launch_config(self, tile=0, ctas_per_sm=0, queue_threshold=0, field_on_hit=0, coherent_order=0,
+                              default=False):
             """Sets the scene's launch shape (default=True: back to the default shape)."""
-            c = _lib.LaunchConfigC(int(tile), int(ctas_per_sm), int(queue_threshold), 0.0, 0.0, int(field_on_hit))
+            c = _lib.LaunchConfigC(int(tile), int(ctas_per_sm), int(queue_threshold), 0.0, 0.0, int(field_on_hit),
+                                   int(coherent_order))
             _lib.check(_lib.lib().hsr_set_launch_config(self._scene, None if default else ctypes.byref(c)))
 
         def traversal_counts(self, rf, samples_per_chirp, integrator, tx, rx, budget, index_offset=None):

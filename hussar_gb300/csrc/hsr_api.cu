@@ -246,6 +246,7 @@ static hsr_status enqueue_pass(SceneDev &sc, const Scratch &s, const hsr_rf_conf
         if (sc.tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc.tuned.ctas_per_sm);
         p.queue_threshold = sc.tuned.queue_threshold;
         p.field_on_hit = sc.tuned.field_on_hit;
+        p.coherent_order = sc.tuned.coherent_order;
     }
     int grid = sc.sm_count * per_sm;
     // timing events only outside stream capture (a captured graph must not record the
@@ -1274,6 +1275,11 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
         c.field_on_hit = 1;
         if ((st = trial(c, ms)) == HSR_OK && ms < best_ms) best_ms = ms, best = c;
     }
+    if (st == HSR_OK) {  // coherent stage order (pays where traversal dominates)
+        LaunchConfig c = best;
+        c.coherent_order = 1;
+        if ((st = trial(c, ms)) == HSR_OK && ms < best_ms) best_ms = ms, best = c;
+    }
     if (st != HSR_OK) {
         d.tuned = saved;
         return st;
@@ -1286,6 +1292,7 @@ hsr_status hsr_autotune_batch(hsr_scene *s, const hsr_rf_config *rf, int32_t N, 
     out_best->ctas_per_sm = best.ctas_per_sm;
     out_best->queue_threshold = best.queue_threshold > 0 ? best.queue_threshold : kWaveDefaultQueue;
     out_best->field_on_hit = best.field_on_hit;
+    out_best->coherent_order = best.coherent_order;
     out_best->trace_ms = best_ms;
     out_best->default_trace_ms = default_ms;
     return HSR_OK;
@@ -1297,12 +1304,13 @@ hsr_status hsr_set_launch_config(hsr_scene *s, const hsr_launch_config *c) {
     if (c) {
         if (c->tile < 0 || (c->tile > 0 && (c->tile < 32 || c->tile > (1 << 20))) || c->ctas_per_sm < 0 ||
             c->ctas_per_sm > 32 || c->queue_threshold < 0 || c->queue_threshold > kWaveMaxQueueThreshold ||
-            (c->field_on_hit != 0 && c->field_on_hit != 1))
+            (c->field_on_hit != 0 && c->field_on_hit != 1) || (c->coherent_order != 0 && c->coherent_order != 1))
             return fail(HSR_ERR_INVALID_ARGUMENT, "launch config out of range");
         l.tile = c->tile;
         l.ctas_per_sm = c->ctas_per_sm;
         l.queue_threshold = c->queue_threshold;
         l.field_on_hit = c->field_on_hit;
+        l.coherent_order = c->coherent_order;
     }
     std::lock_guard<std::mutex> lk(s->mu);
     s->dev.tuned = l;  // null: back to the default shape
@@ -1315,6 +1323,7 @@ hsr_status hsr_get_launch_config(const hsr_scene *s, hsr_launch_config *out) {
     out->ctas_per_sm = s->dev.tuned.ctas_per_sm;
     out->queue_threshold = s->dev.tuned.queue_threshold;
     out->field_on_hit = s->dev.tuned.field_on_hit;
+    out->coherent_order = s->dev.tuned.coherent_order;
     out->trace_ms = 0.f;
     out->default_trace_ms = 0.f;
     return HSR_OK;

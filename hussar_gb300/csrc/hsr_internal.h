@@ -34,6 +34,7 @@ struct LaunchConfig {
     int32_t ctas_per_sm = 0;      // persistent grid: SMs x this (<= the occupancy limit)
     int32_t queue_threshold = 0;  // see TraceParams::queue_threshold
     int32_t field_on_hit = 0;     // see TraceParams::field_on_hit
+    int32_t coherent_order = 0;   // see TraceParams::coherent_order
 };
 // wavefront path stacks: 256 + the GENERATE threshold entries; three capacities
 constexpr int kWaveMaxQueueThreshold = 256;  // thresholds above 128: the 512-entry stack
@@ -171,6 +172,9 @@ struct TraceParams {
     // wavefront kernel, indirect-only paths: form a primary ray's antenna field only once
     // it has hit something
     int32_t field_on_hit;
+    // wavefront kernel: hand each stage's samples / popped paths to threads grouped by
+    // primary sample cell / reflected-direction octant
+    int32_t coherent_order;
     // far-field runs (hsr_simulate_batch_ff): each pose's TX and RX;
     // nullptr: the near-field antennas tx/rx above
     const hsr_ff_antenna *ff_tx;

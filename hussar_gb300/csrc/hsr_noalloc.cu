@@ -170,6 +170,7 @@ extern "C" hsr_status hsr_simulate_batch_device_noalloc(hsr_scene *scene, const 
         if (sc->tuned.ctas_per_sm > 0) per_sm = std::min(per_sm, sc->tuned.ctas_per_sm);
         p.queue_threshold = sc->tuned.queue_threshold;
         p.field_on_hit = sc->tuned.field_on_hit;
+        p.coherent_order = sc->tuned.coherent_order;
     }
     const int grid = sc->sm_count * per_sm;
     const int rc = wave ? launch_wave(p, phase_mode, grid, strm, err)

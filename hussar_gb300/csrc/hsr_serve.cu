@@ -563,6 +563,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             p.samples = q0->r.samples_per_chirp;
             p.acc_row = reinterpret_cast<const int64_t *>(t.d_in + layout.acc_row);
             p.field_on_hit = q0->scene->tuned.field_on_hit;
+            p.coherent_order = q0->scene->tuned.coherent_order;
         }
         auto it = blocks_cache.find(maxN);
         if (it == blocks_cache.end()) it = blocks_cache.emplace(maxN, wave_blocks_per_sm(maxN, true, guided)).first;

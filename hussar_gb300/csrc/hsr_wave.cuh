@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             // the stage's samples gen + [0, n), ordered by primary cell: thread t traces
             // sample gen + S.order[t]
             const int n_stage = int(min((long long)kThreads, gen_end - gen));
-            {
+            if (p.coherent_order) {
                 int key = kPrimaryCells;
                 if (tid < n_stage) {
                     const uint64_t h0 = uint64_t(pc.offset + gen + tid);
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 }
                 order_by_key(S, key);
             }
-            const long long s = gen + (tid < n_stage ? S.order[tid] : tid);
+            const long long s = gen + (p.coherent_order && tid < n_stage ? S.order[tid] : tid);
             bool has_item = false;
             float4 item = make_float4(0.f, 0.f, 0.f, 0.f);
             if (s < gen_end) {
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
             Guided g{0.f, 0.f, 1.f, cf{0.f, 0.f}};
             // the popped paths, ordered by the octant of their reflected direction: thread t
             // continues stack entry count - 1 - S.order[t]
-            {
+            if (p.coherent_order) {
                 int key = kPrimaryCells;
                 if (mine) {
                     const int e = count - 1 - tid;
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_wave(TraceParams p) {
                 order_by_key(S, key);
             }
             if (mine) {
-                const int slot = count - 1 - S.order[tid];
+                const int slot = count - 1 - (p.coherent_order ? S.order[tid] : tid);
                 if (gst)
                     g = Guided{gst[slot], gst[kCap + slot], gst[2 * kCap + slot],
                                cf{gst[3 * kCap + slot], gst[4 * kCap + slot]}};

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HSR_ABI_VERSION 4
+#define HSR_ABI_VERSION 5
 
 typedef enum hsr_status {
     HSR_OK = 0,
@@ -424,8 +424,11 @@ hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, f
  * the default shape (threshold 128). field_on_hit = 1 forms a primary ray's antenna field
  * only once the ray has hit something (for indirect-only paths: the field of a ray that
  * misses is never used), which pays where most primary rays miss and costs registers
- * elsewhere. The shape changes the grouping of sums and the work done, not the samples
- * traced nor their values. */
+ * elsewhere. coherent_order = 1 hands each stage's samples and paths to threads grouped
+ * by primary sample cell and by reflected-direction octant (a counting sort per stage),
+ * which pays on traversal-heavy scenes and costs three CTA barriers per stage elsewhere.
+ * The shape changes the grouping of sums and the work done, not the samples traced nor
+ * their values. */
 typedef struct hsr_launch_config {
     int32_t tile;
     int32_t ctas_per_sm;
@@ -433,6 +436,7 @@ typedef struct hsr_launch_config {
     float trace_ms;          /* hsr_autotune_batch: the chosen shape's trace-kernel time */
     float default_trace_ms;  /* and the default shape's, on the same batch */
     int32_t field_on_hit;
+    int32_t coherent_order;
 } hsr_launch_config;
 
 /* Runs the given batch (host arrays, as hsr_simulate_batch; plain GO mode) under

@@ -1,6 +1,6 @@
 """The launch-shape autotuner (hsr_autotune_batch): it times the caller's batch under
-candidate shapes (work-item tile, CTAs per SM, queue threshold: 32, 64, 128, 256) and
-keeps the fastest.
+candidate shapes (work-item tile, CTAs per SM, queue threshold: 32, 64, 128, 256, the
+primary field formed on a hit, the coherent stage order) and keeps the fastest.
 A shape changes only the grouping of sums, so rows agree with the default shape up to
 summation order (1e-5 relative L2)."""
 import numpy as np
@@ -34,17 +34,18 @@ def test_autotune_picks_a_valid_shape_and_keeps_results(product_lib):
     assert rel_l2(tuned, ref) <= 1e-5
     # explicit shapes at each path-stack capacity (320, 384 and 512 entries) give the same
     # rows too, in both phase modes, and the default can be restored
-    for tile, ctas, q, lazy in ((1024, 2, 32, 0), (2048, 3, 100, 0), (1024, 4, 256, 0), (4096, 4, 200, 0),
-                                (1024, 4, 64, 1), (2048, 4, 128, 1), (1024, 4, 256, 1)):
-        be.set_launch_config(tile=tile, ctas_per_sm=ctas, queue_threshold=q, field_on_hit=lazy)
-        assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5, (tile, ctas, q, lazy)
+    for tile, ctas, q, lazy, coh in ((1024, 2, 32, 0, 0), (2048, 3, 100, 0, 1), (1024, 4, 256, 0, 0),
+                                     (4096, 4, 200, 0, 1), (1024, 4, 64, 1, 0), (2048, 4, 128, 1, 1),
+                                     (1024, 4, 256, 1, 1), (1024, 4, 32, 0, 1)):
+        be.set_launch_config(tile=tile, ctas_per_sm=ctas, queue_threshold=q, field_on_hit=lazy, coherent_order=coh)
+        assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5, (tile, ctas, q, lazy, coh)
     from hussar_gb300 import HSR_PHASE_SPLIT_FP64
     be.set_launch_config(default=True)
     ref_split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
-    for lazy in (0, 1):
-        be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=256, field_on_hit=lazy)
+    for lazy, coh in ((0, 0), (1, 0), (0, 1)):
+        be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=256, field_on_hit=lazy, coherent_order=coh)
         split = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget, phase_mode=HSR_PHASE_SPLIT_FP64)
-        assert rel_l2(split, ref_split) <= 1e-5, lazy
+        assert rel_l2(split, ref_split) <= 1e-5, (lazy, coh)
     be.set_launch_config(default=True)
     assert rel_l2(be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget), ref) <= 1e-5
 
@@ -71,3 +72,23 @@ def test_field_on_hit_keeps_rows_where_primaries_miss(product_lib):
         for k in range(len(w.tx)):
             assert rel_l2(got[k], ref[k]) <= 1e-5, (only_indirect, k)
     be.set_launch_config(default=True)
+
+
+def test_coherent_order_matches_the_oracle_on_boxes(product_lib):
+    """The coherent stage order (samples and popped paths grouped by direction) on the
+    batched boxes configuration, against the oracle at 1e-4 as the default order is."""
+    from oracle import pyoracle
+    w = scenes.boxes_workload(poses=6)
+    w.budget = np.minimum(w.budget, 1 << 14)
+    t = PathTracer()
+    t.doGuiding = False
+    t.maxDepth = w.max_depth
+    be = gb300.Backend(w.mesh, None)
+    N = w.frame.samplesPerChirp
+    be.set_launch_config(tile=1024, ctas_per_sm=4, queue_threshold=64, coherent_order=1)
+    rows = be.simulate_batch(w.rf, N, t, w.tx, w.rx, w.budget)
+    be.set_launch_config(default=True)
+    ora = pyoracle.Scene(w.mesh)
+    for k in range(len(w.tx)):
+        ref = ora.fetch_row(w.rf, N, w.tx[k], w.rx[k], t, int(w.budget[k]))
+        assert rel_l2(rows[k], ref) <= 1e-4, k

@@ -68,7 +68,7 @@ int main(void) {
     F(hsr_server_stats, admitted_while_busy); F(hsr_server_stats, scene_bytes);
     S(hsr_tracer_flags); S(hsr_antenna); S(hsr_rf_config);
     S(hsr_launch_config); F(hsr_launch_config, queue_threshold); F(hsr_launch_config, default_trace_ms);
-    F(hsr_launch_config, field_on_hit);
+    F(hsr_launch_config, field_on_hit); F(hsr_launch_config, coherent_order);
     S(hsr_ff_antenna); F(hsr_ff_antenna, polarization); F(hsr_ff_antenna, scene_center); F(hsr_ff_antenna, radius);
     return 0;
 }
