@@ -426,6 +426,8 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
     // the tick's GENERATE threshold: the smallest of its scenes' tuned thresholds, where a
     // scene never tuned (or tuned to 64 or less) counts as 64
     int32_t queue_threshold = kWaveMaxQueueThreshold;
+    // the coherent stage order when every scene in the tick was tuned to it
+    bool coherent = true;
     // a tick whose requests share one scene, chirp and N runs the uniform kernel
     bool uniform = true;
     const ReqPtr *first = nullptr;
@@ -466,6 +468,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
             maxN = std::max(maxN, q->r.samples_per_chirp);
             queue_threshold = std::min(queue_threshold, std::max(q->scene->tuned.queue_threshold, kWaveSmallQueue));
             if (q->scene->tuned.queue_threshold <= kWaveSmallQueue) queue_threshold = kWaveSmallQueue;
+            coherent = coherent && q->scene->tuned.coherent_order != 0;
             ++P;
             q->scheduled += chunk[i];
             q->iter_done += chunk[i];
@@ -552,6 +555,7 @@ bool hsr_server::build_tick(TickSlot &t, bool busy, int64_t &ticks_launched) {
         // otherwise, and for scenes never tuned, the small stack (the faster one on dense
         // scenes, where it leaves more of the L1 to the BVH)
         p.queue_threshold = queue_threshold;
+        p.coherent_order = coherent ? 1 : 0;
         if (uniform) {
             // one scene, chirp and N: the uniform kernel (no per-pose job loads, fewer
             // registers), writing each request's rows through acc_row
