@@ -322,7 +322,13 @@ def run_gb300(args, rank, world, local_rank, dist):
     # the product's own autotuner picks the launch shape on a bounded sample of this batch
     # (at most 16 poses, budgets capped at 2^20); later plain runs on the scene use it
     sub = min(P, 16)
-    tuned = be.autotune(w.rf, N, t, w.tx[:sub], w.rx[:sub], np.minimum(w.budget[:sub], 1 << 20))
+    if args.launch_config:  # a fixed shape (profiling runs reproduce the tuned one without tuning)
+        vals = [int(x) for x in args.launch_config.split(",")] + [0]
+        be.set_launch_config(*vals[:5])
+        tuned = dict(zip(("tile", "ctas_per_sm", "queue_threshold", "field_on_hit", "coherent_order"), vals[:5]),
+                     trace_ms=None, default_trace_ms=None)
+    else:
+        tuned = be.autotune(w.rf, N, t, w.tx[:sub], w.rx[:sub], np.minimum(w.budget[:sub], 1 << 20))
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -1230,8 +1236,8 @@ def main():
                     choices=["boxes", "sphere", "serve", "tte", "urban_mimo", "synth"])
     ap.add_argument("--poses", type=int, default=None, help="boxes workload: trace the first P poses")
     ap.add_argument("--launch-config", default=None,
-                    help="boxes workload: tile,ctas_per_sm,queue_threshold,field_on_hit[,coherent_order] instead of "
-                         "autotuning")
+                    help="boxes and sphere workloads: tile,ctas_per_sm,queue_threshold,field_on_hit[,coherent_order] "
+                         "instead of autotuning")
     ap.add_argument("--max-log2", type=int, default=None,
                     help="boxes workload: cap every budget at 2^k (small profiling cases only)")
     ap.add_argument("--traffic", type=float, default=None,
