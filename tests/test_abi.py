@@ -70,3 +70,13 @@ def test_invalid_indices_rejected_before_device(product_lib):
     st = product_lib.hsr_scene_create(_lib.ptr(v), 3, _lib.ptr(i), 1, ctypes.byref(h))
     assert st == _lib.HSR_ERR_INVALID_ARGUMENT
     assert b"outside" in product_lib.hsr_last_error()
+
+
+def test_build_setters_validate_without_device(product_lib):
+    """The process-wide BVH settings check their range before anything else."""
+    from hussar_gb300 import _lib
+    for bad in (0, 9, -1):
+        assert product_lib.hsr_set_bvh_leaf_size(bad) == _lib.HSR_ERR_INVALID_ARGUMENT
+    assert product_lib.hsr_set_bvh_builder(2) == _lib.HSR_ERR_INVALID_ARGUMENT
+    for good in (1, 8, 4):  # ends at the default
+        assert product_lib.hsr_set_bvh_leaf_size(good) == _lib.HSR_OK
