@@ -1,5 +1,5 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle on identical Halton
-samples. The bar is the benchmark spec's tolerance: relative L2 of the complex IF signal
+samples. The bar is the parity tolerance: relative L2 of the complex IF signal
 <= 1e-4 (the IF signal is the inverse DFT of the frame row, which is unitary, so the
 relative L2 is the same in either domain). Integer/index results (hit primitive,
 visibility, record structure) must agree exactly."""
