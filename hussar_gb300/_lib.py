@@ -104,6 +104,7 @@ RECORD_DTYPE = [("depth", "<i4"), ("splatted", "<i4"), ("time", "<f4"), ("v_re",
                 ("dphase", "<f4"), ("bin", "<f4"), ("value_re", "<f4"), ("value_im", "<f4")]
 
 _lib = None
+ABI_VERSION = 5  # HSR_ABI_VERSION of include/hsr_gb300.h that these ctypes mirrors follow
 
 
 def lib():
@@ -118,6 +119,9 @@ def lib():
     P = ctypes.POINTER
     vp = ctypes.c_void_p
     L.hsr_abi_version.restype = ctypes.c_int32
+    if L.hsr_abi_version() != ABI_VERSION:  # a stale build: the struct mirrors would not match
+        raise RuntimeError("libhsr_gb300.so has ABI %d, this package expects %d: rebuild it"
+                           % (L.hsr_abi_version(), ABI_VERSION))
     L.hsr_last_error.restype = ctypes.c_char_p
     L.hsr_launch_count.restype = ctypes.c_int64
     L.hsr_debug_alloc_count.restype = ctypes.c_int64

@@ -80,3 +80,11 @@ def test_build_setters_validate_without_device(product_lib):
     assert product_lib.hsr_set_bvh_builder(2) == _lib.HSR_ERR_INVALID_ARGUMENT
     for good in (1, 8, 4):  # ends at the default
         assert product_lib.hsr_set_bvh_leaf_size(good) == _lib.HSR_OK
+
+
+def test_abi_version_matches_the_mirrors(product_lib):
+    """The header's HSR_ABI_VERSION, the library's and the ctypes mirrors' agree."""
+    from hussar_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "hsr_gb300.h")).read()
+    m = re.search(r"#define HSR_ABI_VERSION (\d+)", src)
+    assert m and int(m.group(1)) == _lib.ABI_VERSION == product_lib.hsr_abi_version()
