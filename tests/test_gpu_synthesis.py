@@ -118,3 +118,26 @@ def test_fine_synth_guided(dihedral):
     g = be.simulate_batch(w.rf, 256, tracer(w, True), [w.tx[k]], [w.rx[k]], [1 << 18],
                           splat_mode=HSR_SPLAT_FINE_SYNTH)[0]
     assert rel_l2(g, ref) < 0.05
+
+
+@pytest.mark.parametrize("N", [64, 128, 512, 1000])
+def test_fine_synth_column_tilings(product_lib, oracle_lib, engine, N):
+    """Every column tiling of the tensor-core GEMM: N <= 128 (one 256-column half per
+    CTA), 512 and 1000 (two and four groups of two halves), with a partial row tile (3
+    poses): against the FP64 exact oracle, and the two engines against each other."""
+    rf, _ = scenes.rf_77ghz(N)
+    w = scenes.dihedral_workload(poses=5)
+    be = gb300.Backend(w.mesh, None)
+    ora = oracle_lib.Scene(w.mesh)
+    t = tracer(w)
+    sel = [1, 2, 3]
+    engine(0)
+    rows = be.simulate_batch(rf, N, t, [w.tx[k] for k in sel], [w.rx[k] for k in sel], [1 << 16] * 3,
+                             splat_mode=HSR_SPLAT_FINE_SYNTH)
+    engine(1)
+    rows_cc = be.simulate_batch(rf, N, t, [w.tx[k] for k in sel], [w.rx[k] for k in sel], [1 << 16] * 3,
+                                splat_mode=HSR_SPLAT_FINE_SYNTH)
+    for i, k in enumerate(sel):
+        ref = ora.fetch_row(rf, N, w.tx[k], w.rx[k], t, 1 << 16, precision=65, exact=True)
+        assert rel_l2(rows[i], ref) <= 2e-3, (N, k)
+        assert rel_l2(rows[i], rows_cc[i]) <= 1e-5, (N, k)
