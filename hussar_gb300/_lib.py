@@ -183,6 +183,7 @@ def lib():
         "hsr_debug_plan_tick": [ctypes.c_int32, vp, ctypes.c_int64, ctypes.c_int32, vp],
         "hsr_debug_bvh": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
         "hsr_debug_halton": [vp, ctypes.c_int64, ctypes.c_int32, vp],
+        "hsr_debug_sincos_sweep": [ctypes.c_float, ctypes.c_float, vp, vp, vp],
         "hsr_simulate_batch_ff": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,
                                   ctypes.c_int32, vp],
         "hsr_autotune_batch": [vp, P(RFConfigC), ctypes.c_int32, P(FlagsC), ctypes.c_int32, vp, vp, vp, vp,

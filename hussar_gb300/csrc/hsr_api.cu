@@ -709,6 +709,30 @@ hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, f
     return e == cudaSuccess ? HSR_OK : cuda_fail(e, "halton");
 }
 
+hsr_status hsr_debug_sincos_sweep(float lo, float hi, int64_t *out_checked, int64_t *out_mismatches,
+                                  int64_t *out_slow) {
+    if (!(lo >= 0.f) || !(hi >= lo) || !(hi <= 3.0e38f) || !out_checked || !out_mismatches || !out_slow)
+        return fail(HSR_ERR_INVALID_ARGUMENT, "bad arguments");
+    hsr_status r = check_device();
+    if (r != HSR_OK) return r;
+    unsigned long long *d_counts = nullptr;
+    std::string err;
+    if (!dev_alloc(&d_counts, 3 * sizeof(unsigned long long), err)) return fail(HSR_ERR_OUT_OF_MEMORY, err);
+    unsigned lo_bits, hi_bits;
+    memcpy(&lo_bits, &lo, 4);
+    memcpy(&hi_bits, &hi, 4);
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemset(d_counts, 0, sizeof(h));
+    if (e == cudaSuccess && launch_debug_sincos_sweep(lo_bits, hi_bits, d_counts) != 0) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d_counts, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d_counts);
+    if (e != cudaSuccess) return cuda_fail(e, "sincos sweep");
+    *out_checked = int64_t(h[0]);
+    *out_mismatches = int64_t(h[1]);
+    *out_slow = int64_t(h[2]);
+    return HSR_OK;
+}
+
 hsr_status hsr_scene_bvh_stats(const hsr_scene *s, int64_t *out_nodes, int32_t *out_max_depth, int64_t *out_leaves) {
     if (!s) return fail(HSR_ERR_INVALID_ARGUMENT, "null scene");
     if (out_nodes) *out_nodes = s->dev.node_count;

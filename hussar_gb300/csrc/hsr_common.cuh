@@ -5,7 +5,9 @@
 // exactly like the CPU restatement, so hit/miss decisions agree bit-for-bit.
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace hsr {
 
@@ -60,6 +62,169 @@ __host__ __device__ inline void sincos_rounded(float x, float *s, float *c) {
     const double cv = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
     *s = static_cast<float>(sv);
     *c = static_cast<float>(cv);
+}
+
+// Single-precision operations with one rounding each and no contraction, the same on
+// the device (the _rn intrinsics) and on the host (host code compiles with
+// -ffp-contract=off).
+__host__ __device__ __forceinline__ float rn_add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float rn_mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ float rn_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+__host__ __device__ __forceinline__ unsigned f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    unsigned u;
+    memcpy(&u, &x, 4);
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ float f32_from_bits(unsigned u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float x;
+    memcpy(&x, &u, 4);
+    return x;
+#endif
+}
+
+// Double-float values h + l (|l| <= ulp(h) / 2 after a normalising sum) and the
+// error-free transformations they are built from (Knuth's TwoSum, Dekker's Fast2Sum,
+// the FMA form of Dekker's TwoProduct).
+struct dfloat {
+    float h, l;
+};
+__host__ __device__ __forceinline__ dfloat two_sum(float a, float b) {
+    const float s = rn_add(a, b);
+    const float bb = rn_add(s, -a);
+    return dfloat{s, rn_add(rn_add(a, -rn_add(s, -bb)), rn_add(b, -bb))};
+}
+__host__ __device__ __forceinline__ dfloat fast_two_sum(float a, float b) {  // |a| >= |b|, or a == 0
+    const float s = rn_add(a, b);
+    return dfloat{s, rn_add(b, -rn_add(s, -a))};
+}
+__host__ __device__ __forceinline__ dfloat two_prod(float a, float b) {
+    const float p = rn_mul(a, b);
+    return dfloat{p, rn_fma(a, b, -p)};
+}
+// (a.h + a.l)(b.h + b.l) without the a.l b.l term
+__host__ __device__ __forceinline__ dfloat mul_df(dfloat a, dfloat b) {
+    dfloat p = two_prod(a.h, b.h);
+    p.l = rn_add(p.l, rn_fma(a.h, b.l, rn_mul(a.l, b.h)));
+    return p;
+}
+
+// Ziv's rounding test for a normalised double-float v whose exact value lies within
+// |v.h| 2^-37 of v.h + v.l: true when every such value rounds to v.h (nearest, ties to
+// even), i.e. v.h is the correctly rounded float of the exact value. Values whose
+// magnitude is below 2^-100 are never certified.
+__host__ __device__ __forceinline__ bool rounds_to_high(dfloat v) {
+    const unsigned bits = f32_bits(v.h) & 0x7fffffffu;
+    const int e = int(bits >> 23);
+    if (e < 27 || e > 253) return false;
+    const float a = f32_from_bits(bits);
+    const float ulp = f32_from_bits(unsigned(e - 23) << 23);
+    const float err = rn_mul(a, 0x1p-37f);
+    const float l = v.h < 0.f ? -v.l : v.l;  // > 0: away from zero
+    // the half-gaps to the neighbouring floats, shortened by 1e-5 ulp to cover the
+    // rounding of l + err; below a power of two the gap is half as wide
+    const float up = rn_mul(ulp, 0.49999f);
+    const float down = (bits & 0x7fffffu) == 0u ? rn_mul(ulp, 0.249995f) : up;
+    return l >= 0.f ? rn_add(l, err) < up : rn_add(-l, err) < down;
+}
+
+// sin x and cos x as double-floats for 2^-14 <= |x| <= 8 (sincos_cr's fast path; no
+// intermediate value is subnormal there).
+// Method: Cody-Waite reduction x = k pi/2 + r with pi/2 = C1 + C2 + C3 (C1 has 21
+// significant bits, so k C1 and x - k C1 are exact for |k| <= 5), r as a double-float;
+// the Taylor series sin r = r (1 - z/3! + z^2/5! - ...) and cos r = 1 - z/2! + z^2/4! -
+// ... in z = r^2 (|r| <= pi/4 + 1e-7), the terms up to z^3 in double-float arithmetic and
+// the rest, below 4e-6, in float (where its rounding, a few float ulps of the rest, sets
+// the error). Relative error below 2^-38.8; the largest over every float in [2^-14, 8],
+// against long double: 2^-40.2.
+__host__ __device__ __forceinline__ void sincos_df(float x, dfloat &sv, dfloat &cv) {
+    const float k = rintf(rn_mul(x, 0x1.45f306p-1f));                 // x 2/pi
+    const float r1 = rn_fma(-k, 0x1.921fb0p+0f, x);                    // exact
+    const dfloat kc2 = two_prod(k, 0x1.5110b4p-22f);
+    const dfloat s1 = two_sum(r1, -kc2.h);
+    const dfloat r = fast_two_sum(s1.h, rn_add(rn_add(s1.l, -kc2.l), -rn_mul(k, 0x1.84698ap-48f)));
+    dfloat z = two_prod(r.h, r.h);
+    z.l = rn_fma(rn_add(r.h, r.h), r.l, z.l);
+    const dfloat z2 = mul_df(z, z);
+    const dfloat z3 = mul_df(z2, z);
+    const float z4 = rn_fma(z2.h, z2.h, rn_mul(rn_add(z2.h, z2.h), z2.l));
+    // sin r / r = 1 - z/3! + z^2/5! - z^3/7! + z^4 (1/9! - z/11! + z^2/13!)
+    const dfloat a1 = mul_df(z, dfloat{-0x1.555556p-3f, 0x1.555556p-28f});
+    const dfloat a2 = mul_df(z2, dfloat{0x1.111112p-7f, -0x1.dddddep-32f});
+    const dfloat a3 = mul_df(z3, dfloat{-0x1.a01a02p-13f, 0x1.7f97fap-39f});
+    float ts = rn_fma(z.h, 0x1.612462p-33f, -0x1.ae6456p-26f);
+    ts = rn_fma(ts, z.h, 0x1.71de3ap-19f);
+    dfloat sr = fast_two_sum(1.f, a1.h);
+    float sl = sr.l;
+    sr = fast_two_sum(sr.h, a2.h);
+    sl = rn_add(sl, sr.l);
+    sr = fast_two_sum(sr.h, a3.h);
+    sl = rn_add(rn_add(rn_add(sl, sr.l), rn_add(rn_add(a1.l, a2.l), a3.l)), rn_mul(z4, ts));
+    sr = mul_df(r, dfloat{sr.h, sl});
+    sr = fast_two_sum(sr.h, sr.l);
+    // cos r = 1 - z/2! + z^2/4! - z^3/6! + z^4 (1/8! - z/10! + z^2/12! - z^3/14!)
+    const dfloat b2 = mul_df(z2, dfloat{0x1.555556p-5f, -0x1.555556p-30f});
+    const dfloat b3 = mul_df(z3, dfloat{-0x1.6c16c2p-10f, 0x1.27d27ep-35f});
+    float tc = rn_fma(z.h, -0x1.93974ap-37f, 0x1.1eed8ep-29f);
+    tc = rn_fma(tc, z.h, -0x1.27e4fcp-22f);
+    tc = rn_fma(tc, z.h, 0x1.a01a02p-16f);
+    dfloat cr = fast_two_sum(1.f, rn_mul(z.h, -0.5f));
+    float cl = rn_add(cr.l, rn_mul(z.l, -0.5f));
+    cr = fast_two_sum(cr.h, b2.h);
+    cl = rn_add(cl, cr.l);
+    cr = fast_two_sum(cr.h, b3.h);
+    cl = rn_add(rn_add(rn_add(cl, cr.l), rn_add(b2.l, b3.l)), rn_mul(z4, tc));
+    cr = fast_two_sum(cr.h, cl);
+    // quadrant
+    const int q = int(k) & 3;
+    const dfloat ns = dfloat{-sr.h, -sr.l}, nc = dfloat{-cr.h, -cr.l};
+    sv = q == 0 ? sr : q == 1 ? cr : q == 2 ? ns : nc;
+    cv = q == 0 ? cr : q == 1 ? ns : q == 2 ? nc : sr;
+}
+
+// sincos_rounded's results (the same bits for every float x) at a fraction of its
+// double-precision operations: for 2^-14 <= |x| <= 8 the double-floats of sincos_df are
+// returned when the rounding test certifies both, which holds for all but about 0.05 %
+// of arguments (1.4 % of warps of uniformly distributed angles); those, and every x outside that range, take sincos_rounded. Checked
+// against sincos_rounded for every float in [-8, 8] (the rounding test is what makes the
+// two agree: sincos_rounded is correctly rounded except within 2^-50 of a midpoint, and
+// a certified value is further than 2^-37 from one).
+__host__ __device__ __forceinline__ void sincos_cr(float x, float *s, float *c) {
+    const float ax = fabsf(x);
+    if (ax >= 0x1p-14f && ax <= 8.f) {
+        dfloat sv, cv;
+        sincos_df(x, sv, cv);
+        if (rounds_to_high(sv) && rounds_to_high(cv)) {
+            *s = sv.h;
+            *c = cv.h;
+            return;
+        }
+    }
+    sincos_rounded(x, s, c);
 }
 
 struct f3 {

@@ -251,6 +251,7 @@ int launch_assemble_frame(const float *rows, int32_t chirps, int32_t samples, in
                           cudaStream_t st);
 // The device Halton sampler at host-chosen indices (hsr_debug_halton).
 int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out);
+int launch_debug_sincos_sweep(unsigned lo_bits, unsigned hi_bits, unsigned long long *d_counts);
 int launch_ray_queries(const DNode *nodes, const DTri *tris, int64_t count, const float *o, const float *d,
                        const float *tfar, float *t, float *p, float *n, int32_t *prim, int32_t *vis, unsigned *status,
                        cudaStream_t st);

@@ -153,7 +153,8 @@ __device__ __forceinline__ Ant load_ant(const hsr_antenna *a) {
 
 // UniformSampleSphere (libhussar/include/hussar/core/sampling.h:38-43). kExact (the
 // reference-phase parity instantiations): sin and cos of phi correctly rounded
-// (sincos_rounded), bit for bit what the CPU restatement computes; the reference's
+// (sincos_cr: sincos_rounded's bits, mostly without its double-precision operations),
+// bit for bit what the CPU restatement computes; the reference's
 // std::sin/std::cos of a float resolve to the platform's sinf/cosf, which are not
 // correctly rounded everywhere (glibc 2.39: one ulp off on 1.3 % of uniformly
 // distributed angles), and CUDA's sincosf differs from both by up to two ulps. A one-ulp
@@ -166,7 +167,7 @@ template <bool kExact = true> __device__ __forceinline__ f3 uniform_sample_spher
     float r = sqrtf(fmaxf(0.f, 1.f - y * y));
     float s, c;
     if (kExact)
-        sincos_rounded(phi, &s, &c);
+        sincos_cr(phi, &s, &c);
     else
         sincosf(phi, &s, &c);
     return mk3(-r * s, y, -r * c);

@@ -412,6 +412,32 @@ __global__ void k_debug_halton(const uint64_t *index, int64_t count, int dim, fl
     const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < count) out[i] = halton(index[i], dim);
 }
+
+// Every float x with |x| bits in [lo_bits, hi_bits], both signs: sincos_cr against
+// sincos_rounded. counts: [0] arguments checked, [1] mismatches, [2] arguments where
+// sincos_cr took sincos_rounded (outside the fast range or not certified).
+__global__ void k_debug_sincos_sweep(unsigned lo_bits, unsigned hi_bits, unsigned long long *counts) {
+    unsigned long long checked = 0, bad = 0, slow = 0;
+    const unsigned stride = gridDim.x * blockDim.x;
+    for (unsigned u = lo_bits + blockIdx.x * blockDim.x + threadIdx.x; u <= hi_bits && u >= lo_bits; u += stride) {
+        for (unsigned sign = 0; sign < 2; ++sign) {
+            const float x = __uint_as_float(u | (sign << 31));
+            float s0, c0, s1, c1;
+            sincos_rounded(x, &s0, &c0);
+            sincos_cr(x, &s1, &c1);
+            bad += (__float_as_uint(s0) != __float_as_uint(s1)) || (__float_as_uint(c0) != __float_as_uint(c1));
+            dfloat sv, cv;
+            sincos_df(x, sv, cv);
+            const float ax = fabsf(x);
+            slow += !(ax >= 0x1p-14f && ax <= 8.f && rounds_to_high(sv) && rounds_to_high(cv));
+            ++checked;
+        }
+        if (u > hi_bits - stride) break;  // the next u would wrap past 2^32
+    }
+    atomicAdd(&counts[0], checked);
+    if (bad) atomicAdd(&counts[1], bad);
+    if (slow) atomicAdd(&counts[2], slow);
+}
 }  // namespace
 
 int launch_assemble_frame(const float *rows, int32_t chirps, int32_t samples, int32_t channels, float *frame,
@@ -426,6 +452,12 @@ int launch_assemble_frame(const float *rows, int32_t chirps, int32_t samples, in
 int launch_debug_halton(const uint64_t *d_index, int64_t count, int dim, float *d_out) {
     if (count <= 0) return 0;
     k_debug_halton<<<unsigned((count + 255) / 256), 256>>>(d_index, count, dim, d_out);
+    note_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_debug_sincos_sweep(unsigned lo_bits, unsigned hi_bits, unsigned long long *d_counts) {
+    k_debug_sincos_sweep<<<152 * 16, 256>>>(lo_bits, hi_bits, d_counts);
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

@@ -416,6 +416,15 @@ hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_c
  * into out[count] (host). For tests: the trace kernels call the same device function. */
 hsr_status hsr_debug_halton(const uint64_t *index, int64_t count, int32_t dim, float *out);
 
+/* The primary direction's sine and cosine on the device (UniformSampleSphere,
+ * sampling.h:38-43, in the reference-phase kernels): for every float x with lo <= |x| <= hi
+ * (0 <= lo <= hi), both signs, the fast certified evaluation the kernels call against the
+ * double-precision one it stands for. out_checked: arguments; out_mismatches: arguments
+ * where the two differ in any bit (0 is the requirement); out_slow: arguments the fast
+ * evaluation passed to the double-precision one. For tests. Synchronous. */
+hsr_status hsr_debug_sincos_sweep(float lo, float hi, int64_t *out_checked, int64_t *out_mismatches,
+                                  int64_t *out_slow);
+
 /* ---- Autotuning of the plain wavefront launch ---------------------------------------
  * No counterpart in the reference. The launch shape of a plain batch: samples per work
  * item (tile), persistent CTAs per SM, and the queue threshold (GENERATE runs while a CTA

@@ -82,6 +82,14 @@ def test_build_setters_validate_without_device(product_lib):
         assert product_lib.hsr_set_bvh_leaf_size(good) == _lib.HSR_OK
 
 
+def test_sincos_sweep_validates_without_device(product_lib):
+    from hussar_gb300 import _lib
+    n = ctypes.c_int64()
+    for lo, hi in ((1.0, 0.5), (-1.0, 1.0), (0.0, float("inf")), (float("nan"), 1.0)):
+        assert product_lib.hsr_debug_sincos_sweep(lo, hi, ctypes.byref(n), ctypes.byref(n),
+                                                  ctypes.byref(n)) == _lib.HSR_ERR_INVALID_ARGUMENT
+
+
 def test_abi_version_matches_the_mirrors(product_lib):
     """The header's HSR_ABI_VERSION, the library's and the ctypes mirrors' agree."""
     from hussar_gb300 import _lib
