@@ -170,6 +170,7 @@ def lib():
         "hsr_set_synth_engine": [ctypes.c_int32],
         "hsr_set_bvh_builder": [ctypes.c_int32],
         "hsr_set_bvh_leaf_size": [ctypes.c_int32],
+        "hsr_set_bvh_optimize": [ctypes.c_int32],
         "hsr_scene_refit": [vp, vp, ctypes.c_int64],
         "hsr_scene_rebuild": [vp, vp, ctypes.c_int64, vp, ctypes.c_int64],
         "hsr_last_kernel_ms": [vp, P(ctypes.c_float)],

@@ -1403,6 +1403,12 @@ hsr_status hsr_set_bvh_leaf_size(int32_t triangles) {
     return HSR_OK;
 }
 
+hsr_status hsr_set_bvh_optimize(int32_t passes) {
+    if (passes < 0 || passes > 64) return fail(HSR_ERR_INVALID_ARGUMENT, "passes must be 0..64");
+    g_bvh_optimize = passes;
+    return HSR_OK;
+}
+
 hsr_status hsr_set_synth_engine(int32_t engine) {
     if (engine != 0 && engine != 1) return fail(HSR_ERR_INVALID_ARGUMENT, "engine must be 0 or 1");
     g_synth_engine = engine;

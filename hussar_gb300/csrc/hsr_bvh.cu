@@ -449,10 +449,382 @@ __global__ void k_relink(int64_t n_nodes, DNode *nodes, const int32_t *__restric
     nodes[i].d.y = c[1];
 }
 
+// ---------------- insertion-based optimisation ----------------
+// Bittner, Hapala and Havran (2013): take a subtree out and insert it as the sibling of
+// the node where the tree's surface-area cost grows least. Every node searches in
+// parallel on a snapshot of the tree (Meister and Bittner 2018); the moves that lower the
+// cost claim the six nodes they rewire (the subtree N, its parent P and sibling S, its
+// grandparent G, the target X and X's parent) with 64-bit priority locks (gain, node); a
+// winner whose target lies inside another winner's subtree withdraws, so no move closes a
+// cycle; the winners are applied and the boxes refitted. Index space: internal nodes
+// [0, M), triangle slot t at M + t. The root stays node 0 (never moved, never a target,
+// never removed). The build's DNodes are written back only when the result passes its
+// checks (every node's parent chain ends at node 0; leaves at most 60 deep).
+constexpr int kReinsPath = 128;      // deepest parent chain a search handles
+constexpr int kReinsHeap = 384;      // search frontier (a fuller frontier drops entries)
+constexpr int kReinsPops = 4096;
+constexpr int kReinsMaxDepth = 60;   // the traversal stack holds 64 entries
+
+__device__ __forceinline__ Box box_union(const Box &a, const Box &b) {
+    Box u;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        u.lo[k] = fminf(a.lo[k], b.lo[k]);
+        u.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+    }
+    return u;
+}
+
+__global__ void k_reins_init(int m, const DNode *__restrict__ nodes, const int32_t *__restrict__ par_i, int *rpar,
+                             int2 *rkid, Box *rbox) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const DNode nd = nodes[i];
+    const int c[2] = {nd.d.x, nd.d.y};
+    int k[2];
+    for (int w = 0; w < 2; ++w) {
+        k[w] = c[w] >= 0 ? c[w] : m + ~c[w];
+        if (c[w] < 0) {
+            rbox[k[w]] = child_box(nd, w);
+            rpar[k[w]] = i;
+        }
+    }
+    rkid[i] = make_int2(k[0], k[1]);
+    rpar[i] = par_i[i];
+    rbox[i] = box_union(child_box(nd, 0), child_box(nd, 1));
+}
+
+// Depth of every node (the root 0) and the deepest leaf; bad: a parent chain that does not
+// end at node 0 within the bound.
+__global__ void k_reins_depth(int total, int m, const int *__restrict__ rpar, int *depth, int *max_depth,
+                              int *bad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int d = 0, x = i;
+    while (rpar[x] >= 0 && d < 1024) {
+        x = rpar[x];
+        ++d;
+    }
+    depth[i] = d;
+    if (x != 0 || d >= 1024) atomicOr(bad, 1);
+    if (i >= m) atomicMax(max_depth, d);
+}
+
+// The best place for subtree n: mv_x[n] (-1: none lowers the cost by min_gain) and the
+// cost it saves, mv_gain[n].
+__global__ void __launch_bounds__(128) k_reins_search(int total, int m, const int *__restrict__ rpar,
+                                                      const int2 *__restrict__ rkid, const Box *__restrict__ rbox,
+                                                      const int *__restrict__ depth, float min_gain, int *mv_x,
+                                                      float *mv_gain) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= total) return;
+    mv_x[n] = -1;
+    const int P = rpar[n];
+    if (P < 0) return;
+    const int G = rpar[P];
+    if (G < 0) return;
+    const int dp = depth[P];
+    if (dp >= kReinsPath) return;
+    const int2 pk = rkid[P];
+    const int S = pk.x == n ? pk.y : pk.x;
+    // the tree with n taken out: P disappears, S takes its place, P's ancestors shrink
+    int pnode[kReinsPath];
+    Box pbox[kReinsPath];
+    float drem = -box_area(rbox[P]);
+    Box cur = rbox[S];
+    int child = P;
+    for (int y = G, steps = 0; y >= 0; child = y, y = rpar[y], ++steps) {
+        const int dy = depth[y];
+        if (steps >= kReinsPath || dy < 0 || dy >= dp) return;  // an inconsistent snapshot: no move
+        const int2 yk = rkid[y];
+        const Box nb = box_union(cur, rbox[yk.x == child ? yk.y : yk.x]);
+        drem += box_area(nb) - box_area(rbox[y]);
+        pnode[dy] = y;
+        pbox[dy] = nb;
+        cur = nb;
+    }
+    const Box bn = rbox[n];
+    const float an = box_area(bn);
+    // best-first branch and bound over the detached tree; a node's key is the area its
+    // ancestors grow by when n goes below them (the induced cost)
+    float hk[kReinsHeap];
+    int hv[kReinsHeap];
+    int hs = 1;
+    hk[0] = 0.f;
+    hv[0] = 0;
+    float best = __int_as_float(0x7f800000);
+    int bx = -1;
+    for (int pops = 0; hs > 0 && pops < kReinsPops; ++pops) {
+        const float ic0 = hk[0];
+        int x = hv[0];
+        --hs;
+        if (hs > 0) {  // sift the last entry down from the top
+            const float k = hk[hs];
+            const int v = hv[hs];
+            int i = 0;
+            while (true) {
+                int c = 2 * i + 1;
+                if (c >= hs) break;
+                if (c + 1 < hs && hk[c + 1] < hk[c]) ++c;
+                if (hk[c] >= k) break;
+                hk[i] = hk[c];
+                hv[i] = hv[c];
+                i = c;
+            }
+            hk[i] = k;
+            hv[i] = v;
+        }
+        if (ic0 + an >= best) break;
+        if (x == P) x = S;
+        const int dx = depth[x];
+        const Box bxx = (dx < dp && pnode[dx] == x) ? pbox[dx] : rbox[x];
+        const float au = box_area(box_union(bxx, bn));
+        if (x != S && x != 0 && ic0 + au < best) {
+            best = ic0 + au;
+            bx = x;
+        }
+        const float ic = ic0 + au - box_area(bxx);
+        if (x < m && ic + an < best) {
+            const int2 xk = rkid[x];
+            for (int w = 0; w < 2; ++w) {
+                if (hs >= kReinsHeap) break;
+                int i = hs++;
+                while (i > 0 && hk[(i - 1) / 2] > ic) {
+                    hk[i] = hk[(i - 1) / 2];
+                    hv[i] = hv[(i - 1) / 2];
+                    i = (i - 1) / 2;
+                }
+                hk[i] = ic;
+                hv[i] = w ? xk.y : xk.x;
+            }
+        }
+    }
+    const float gain = -(drem + best);
+    if (bx >= 0 && gain > min_gain) {
+        mv_x[n] = bx;
+        mv_gain[n] = gain;
+    }
+}
+
+// The nodes a move rewires: n, P, S, G, X, X's parent.
+__device__ __forceinline__ void reins_touched(int n, int x, const int *rpar, const int2 *rkid, int *t) {
+    const int P = rpar[n];
+    const int2 pk = rkid[P];
+    t[0] = n;
+    t[1] = P;
+    t[2] = pk.x == n ? pk.y : pk.x;
+    t[3] = rpar[P];
+    t[4] = x;
+    t[5] = rpar[x];
+}
+
+__global__ void k_reins_lock(int total, const int *__restrict__ rpar, const int2 *__restrict__ rkid,
+                             const int *__restrict__ mv_x, const float *__restrict__ mv_gain,
+                             unsigned long long *lock) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= total || mv_x[n] < 0) return;
+    int t[6];
+    reins_touched(n, mv_x[n], rpar, rkid, t);
+    for (int k = 0; k < 6; ++k)
+        if (t[k] < 0 || t[k] >= total) return;
+    const unsigned long long key = (static_cast<unsigned long long>(__float_as_uint(mv_gain[n])) << 32) | unsigned(n);
+    for (int k = 0; k < 6; ++k) atomicMax(&lock[t[k]], key);
+}
+
+__global__ void k_reins_claim(int total, const int *__restrict__ rpar, const int2 *__restrict__ rkid,
+                              const int *__restrict__ mv_x, const float *__restrict__ mv_gain,
+                              const unsigned long long *__restrict__ lock, char *moving) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= total) return;
+    moving[n] = 0;
+    if (mv_x[n] < 0) return;
+    int t[6];
+    reins_touched(n, mv_x[n], rpar, rkid, t);
+    const unsigned long long key = (static_cast<unsigned long long>(__float_as_uint(mv_gain[n])) << 32) | unsigned(n);
+    for (int k = 0; k < 6; ++k)
+        if (t[k] < 0 || t[k] >= total || lock[t[k]] != key) return;
+    moving[n] = 1;
+}
+
+// A winner stays unless its target is inside another winner's subtree.
+__global__ void k_reins_keep(int total, const int *__restrict__ rpar, const int *__restrict__ mv_x,
+                             const char *__restrict__ moving, char *keep) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= total) return;
+    keep[n] = 0;
+    if (!moving[n]) return;
+    int x = mv_x[n];
+    for (int steps = 0; x >= 0; x = rpar[x], ++steps)
+        if (steps >= 1024 || (x != n && moving[x])) return;
+    keep[n] = 1;
+}
+
+__global__ void k_reins_apply(int total, int *rpar, int2 *rkid, const int *__restrict__ mv_x,
+                              const char *__restrict__ keep, int *applied) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= total || !keep[n]) return;
+    const int X = mv_x[n];
+    const int P = rpar[n], G = rpar[P];
+    const int2 pk = rkid[P];
+    const int S = pk.x == n ? pk.y : pk.x;
+    // take n out: S replaces P below G
+    int2 gk = rkid[G];
+    if (gk.x == P) gk.x = S; else gk.y = S;
+    rkid[G] = gk;
+    rpar[S] = G;
+    // P becomes the parent of X and n, in X's place
+    const int XP = rpar[X];
+    int2 xk = rkid[XP];
+    if (xk.x == X) xk.x = P; else xk.y = P;
+    rkid[XP] = xk;
+    rpar[P] = XP;
+    rkid[P] = make_int2(X, n);
+    rpar[X] = P;
+    rpar[n] = P;
+    atomicAdd(applied, 1);
+}
+
+// Boxes from the leaves up: a leaf's thread climbs while it is the second child to arrive.
+__global__ void k_reins_refit(int total, int m, const int *__restrict__ rpar, const int2 *__restrict__ rkid,
+                              Box *rbox, int *counters, int *bad) {
+    const int leaf = m + blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= total) return;
+    int p = rpar[leaf];
+    for (int steps = 0; p >= 0; p = rpar[p], ++steps) {
+        if (steps >= 1024) {
+            atomicOr(bad, 1);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(&counters[p], 1) == 0) return;
+        __threadfence();
+        const int2 k = rkid[p];
+        const volatile Box *vb = rbox;
+        Box a, b;
+        for (int j = 0; j < 3; ++j) {
+            a.lo[j] = vb[k.x].lo[j];
+            a.hi[j] = vb[k.x].hi[j];
+            b.lo[j] = vb[k.y].lo[j];
+            b.hi[j] = vb[k.y].hi[j];
+        }
+        rbox[p] = box_union(a, b);
+    }
+}
+
+// Back to the build's layout: DNodes with child boxes and references (leaf: ~slot),
+// internal and leaf parent links.
+__global__ void k_reins_write(int m, const int *__restrict__ rpar, const int2 *__restrict__ rkid,
+                              const Box *__restrict__ rbox, DNode *nodes, int32_t *par_i, int32_t *par_l) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int2 k = rkid[i];
+    const Box l = rbox[k.x], r = rbox[k.y];
+    DNode nd;
+    nd.a = make_float4(l.lo[0], l.hi[0], l.lo[1], l.hi[1]);
+    nd.b = make_float4(r.lo[0], r.hi[0], r.lo[1], r.hi[1]);
+    nd.c = make_float4(l.lo[2], l.hi[2], r.lo[2], r.hi[2]);
+    nd.d = make_int4(k.x < m ? k.x : ~(k.x - m), k.y < m ? k.y : ~(k.y - m), 0, 0);
+    nodes[i] = nd;
+    par_i[i] = rpar[i];
+    if (k.x >= m) par_l[k.x - m] = i;
+    if (k.y >= m) par_l[k.y - m] = i;
+}
+
 }  // namespace
 
 int g_bvh_builder = 0;  // 0: PLOC, 1: LBVH (Karras)
 int g_bvh_leaf_max = 4;  // triangles per leaf (1..8)
+int g_bvh_optimize = 32;  // largest number of insertion passes after the build (0: none)
+
+// Insertion passes over the binary tree of a build (par_i/par_l and the DNodes, leaves
+// referenced as ~slot); stops when a pass moves fewer than 1 in 20,000 nodes. Returns 0
+// (also when the result failed its checks and the build's tree was kept), 2 or 3.
+static int optimize_tree(SceneDev &s, int64_t nt, int32_t *par_i, int32_t *par_l, cudaStream_t st,
+                         std::string &err) {
+    if (g_bvh_optimize <= 0 || nt < 4 || nt >= (int64_t(1) << 30)) return 0;
+    const int m = int(nt - 1), total = int(2 * nt - 1);
+    int *rpar = nullptr, *depth = nullptr, *mv_x = nullptr, *counters = nullptr, *scal = nullptr;
+    int2 *rkid = nullptr;
+    Box *rbox = nullptr;
+    float *mv_gain = nullptr;
+    unsigned long long *lock = nullptr;
+    char *moving = nullptr, *keep = nullptr;
+    int rc = 0;
+    do {
+        if (!dev_alloc(&rpar, sizeof(int) * total, err) || !dev_alloc(&depth, sizeof(int) * total, err) ||
+            !dev_alloc(&mv_x, sizeof(int) * total, err) || !dev_alloc(&counters, sizeof(int) * m, err) ||
+            !dev_alloc(&scal, sizeof(int) * 4, err) || !dev_alloc(&rkid, sizeof(int2) * m, err) ||
+            !dev_alloc(&rbox, sizeof(Box) * total, err) || !dev_alloc(&mv_gain, sizeof(float) * total, err) ||
+            !dev_alloc(&lock, sizeof(unsigned long long) * total, err) || !dev_alloc(&moving, size_t(total), err) ||
+            !dev_alloc(&keep, size_t(total), err)) {
+            rc = 3;
+            break;
+        }
+        const int T = 256;
+        k_reins_init<<<blocks_for(m, T), T, 0, st>>>(m, s.nodes, par_i, rpar, rkid, rbox);
+        note_launches(1);
+        Box root;
+        if (cudaMemcpyAsync(&root, rbox, sizeof(Box), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            err = "BVH optimisation: reading the root box failed";
+            rc = 2;
+            break;
+        }
+        const float dx = root.hi[0] - root.lo[0], dy = root.hi[1] - root.lo[1], dz = root.hi[2] - root.lo[2];
+        const float min_gain = 1e-6f * (dx * dy + dy * dz + dz * dx);
+        int h[4] = {0, 0, 0, 0};
+        for (int pass = 0; pass < g_bvh_optimize; ++pass) {
+            cudaMemsetAsync(scal, 0, sizeof(int) * 4, st);
+            cudaMemsetAsync(lock, 0, sizeof(unsigned long long) * total, st);
+            cudaMemsetAsync(counters, 0, sizeof(int) * m, st);
+            k_reins_depth<<<blocks_for(total, T), T, 0, st>>>(total, m, rpar, depth, scal + 2, scal + 1);
+            k_reins_search<<<blocks_for(total, 128), 128, 0, st>>>(total, m, rpar, rkid, rbox, depth, min_gain, mv_x,
+                                                                   mv_gain);
+            k_reins_lock<<<blocks_for(total, T), T, 0, st>>>(total, rpar, rkid, mv_x, mv_gain, lock);
+            k_reins_claim<<<blocks_for(total, T), T, 0, st>>>(total, rpar, rkid, mv_x, mv_gain, lock, moving);
+            k_reins_keep<<<blocks_for(total, T), T, 0, st>>>(total, rpar, mv_x, moving, keep);
+            k_reins_apply<<<blocks_for(total, T), T, 0, st>>>(total, rpar, rkid, mv_x, keep, scal);
+            k_reins_refit<<<blocks_for(nt, T), T, 0, st>>>(total, m, rpar, rkid, rbox, counters, scal + 1);
+            note_launches(7);
+            if (cudaMemcpyAsync(h, scal, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) {
+                err = "BVH optimisation pass failed";
+                rc = 2;
+                break;
+            }
+            if (h[1] || h[0] < std::max(1, total / 20000)) break;
+        }
+        if (rc || h[1]) break;  // a failed check keeps the build's own tree
+        cudaMemsetAsync(scal, 0, sizeof(int) * 4, st);
+        k_reins_depth<<<blocks_for(total, T), T, 0, st>>>(total, m, rpar, depth, scal + 2, scal + 1);
+        note_launches(1);
+        if (cudaMemcpyAsync(h, scal, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            err = "BVH optimisation check failed";
+            rc = 2;
+            break;
+        }
+        if (h[1] || h[2] > kReinsMaxDepth) break;
+        k_reins_write<<<blocks_for(m, T), T, 0, st>>>(m, rpar, rkid, rbox, s.nodes, par_i, par_l);
+        note_launches(1);
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            err = "BVH optimisation write-back failed";
+            rc = 2;
+        }
+    } while (false);
+    cudaFree(rpar);
+    cudaFree(depth);
+    cudaFree(mv_x);
+    cudaFree(counters);
+    cudaFree(scal);
+    cudaFree(rkid);
+    cudaFree(rbox);
+    cudaFree(mv_gain);
+    cudaFree(lock);
+    cudaFree(moving);
+    cudaFree(keep);
+    return rc;
+}
 
 // Leaves of several triangles over a built binary topology (parent links of the build).
 static int collapse_leaves(SceneDev &s, int64_t nt, const int32_t *par_i, const int32_t *par_l, int *counters,
@@ -730,6 +1102,16 @@ int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, i
             err = std::string("BVH build: ") + cudaGetErrorString(e);
             fail(2);
             break;
+        }
+        const int orc = optimize_tree(s, nt, par_i, par_l, st, err);
+        if (orc) {
+            fail(orc);
+            break;
+        }
+        if (g_bvh_optimize > 0) {  // the depth of the tree as it now is
+            cudaMemsetAsync(depth + 1, 0, sizeof(int), st);
+            k_leaf_depth<<<blocks_for(nt, T), T, 0, st>>>(nt, par_i, par_l, depth + 1);
+            note_launches(1);
         }
         const int lrc = collapse_leaves(s, nt, par_i, par_l, counters, st, err);
         if (lrc) {

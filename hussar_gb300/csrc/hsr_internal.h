@@ -266,6 +266,7 @@ extern int g_path_kernel;
 // BVH topology of new scenes: 0 = PLOC (default), 1 = LBVH (Karras radix tree)
 extern int g_bvh_builder;
 extern int g_bvh_leaf_max;
+extern int g_bvh_optimize;
 int trace_blocks_per_sm(int samples, int splat_mode, int fine_bins);
 
 }  // namespace hsr

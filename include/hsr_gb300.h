@@ -475,6 +475,15 @@ hsr_status hsr_set_bvh_builder(int32_t builder);
  * primitive id); only the traversal cost does. */
 hsr_status hsr_set_bvh_leaf_size(int32_t triangles);
 
+/* Insertion passes over the BVH after its build (0..64, default 32; 0 = none) for scenes
+ * created afterwards (process-wide). A pass takes every subtree out and re-inserts it
+ * where the tree's surface-area cost grows least, in parallel with conflicting moves
+ * resolved by priority; passes stop early once they move fewer than 1 in 20,000 nodes.
+ * Fewer node visits per ray (on the 1 M-triangle boxes scene about a quarter fewer); the
+ * ray-query results do not depend on it. The build keeps its own tree if the result is
+ * deeper than 60 levels. */
+hsr_status hsr_set_bvh_optimize(int32_t passes);
+
 /* Engine of the fine-histogram synthesis GEMM (process-wide): 0 (default) = tensor cores
  * (tcgen05.mma, operands split into three BF16 terms, FP32 accumulation), 1 = CUDA cores
  * in FP32. Both compute the same product; tests use this to check one against the other. */

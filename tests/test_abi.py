@@ -78,6 +78,9 @@ def test_build_setters_validate_without_device(product_lib):
     for bad in (0, 9, -1):
         assert product_lib.hsr_set_bvh_leaf_size(bad) == _lib.HSR_ERR_INVALID_ARGUMENT
     assert product_lib.hsr_set_bvh_builder(2) == _lib.HSR_ERR_INVALID_ARGUMENT
+    for bad in (-1, 65):
+        assert product_lib.hsr_set_bvh_optimize(bad) == _lib.HSR_ERR_INVALID_ARGUMENT
+    assert product_lib.hsr_set_bvh_optimize(32) == _lib.HSR_OK
     for good in (1, 8, 4):  # ends at the default
         assert product_lib.hsr_set_bvh_leaf_size(good) == _lib.HSR_OK
 

@@ -87,25 +87,35 @@ def test_batch_fine_synthesis(boxes, product_lib):
     assert max(rel_l2(a[i], b[i]) for i in np.nonzero(nz)[0]) <= 2e-5
 
 
-def test_bvh_builders_agree_and_ploc_visits_fewer_nodes(product_lib):
-    """PLOC and LBVH topologies give bit-identical ray queries; on the dense boxes scene the
-    surface-area-driven PLOC tree visits far fewer nodes per ray."""
+def test_bvh_builders_and_insertion_passes_agree_and_cost_less(product_lib):
+    """PLOC and LBVH topologies, each with and without the insertion passes, give
+    bit-identical ray queries; on the dense boxes scene the surface-area-driven PLOC tree
+    visits far fewer nodes per ray than LBVH, and the insertion passes cut both further."""
     w = scenes.boxes_workload(poses=8, min_log2=12, max_log2=12)
     t = tracer(w)
     res = {}
-    for builder in (0, 1):
-        product_lib.hsr_set_bvh_builder(builder)
-        be = gb300.Backend(w.mesh, None)
-        rng = np.random.default_rng(9)
-        o = np.concatenate([np.array([a.position() for a in w.tx]), rng.uniform([-50, 0.1, -50], [50, 3, 50], (4000, 3))])
-        d = rng.normal(size=(len(o), 3))
-        d /= np.linalg.norm(d, axis=1, keepdims=True)
-        res[builder] = (be.intersect(o.astype(np.float32), d.astype(np.float32)),
-                        be.traversal_counts(w.rf, 256, t, w.tx, w.rx, w.budget))
-    product_lib.hsr_set_bvh_builder(0)
-    (t0, p0, n0, pr0), c0 = res[0]
-    (t1, p1, n1, pr1), c1 = res[1]
-    assert np.array_equal(pr0, pr1) and np.array_equal(t0.view(np.uint32), t1.view(np.uint32))
-    print("nodes per ray: PLOC %.1f LBVH %.1f" % (c0["nodes"] / c0["rays"], c1["nodes"] / c1["rays"]))
-    assert c0["rays"] == c1["rays"]
-    assert c0["nodes"] < 0.7 * c1["nodes"]
+    try:
+        for builder in (0, 1):
+            for passes in (0, 32):
+                product_lib.hsr_set_bvh_builder(builder)
+                product_lib.hsr_set_bvh_optimize(passes)
+                be = gb300.Backend(w.mesh, None)
+                rng = np.random.default_rng(9)
+                o = np.concatenate([np.array([a.position() for a in w.tx]),
+                                    rng.uniform([-50, 0.1, -50], [50, 3, 50], (4000, 3))])
+                d = rng.normal(size=(len(o), 3))
+                d /= np.linalg.norm(d, axis=1, keepdims=True)
+                res[builder, passes] = (be.intersect(o.astype(np.float32), d.astype(np.float32)),
+                                        be.traversal_counts(w.rf, 256, t, w.tx, w.rx, w.budget))
+    finally:
+        product_lib.hsr_set_bvh_builder(0)
+        product_lib.hsr_set_bvh_optimize(32)
+    (t0, p0, n0, pr0), c0 = res[0, 0]
+    for key, ((tk, pk, nk, prk), ck) in res.items():
+        assert np.array_equal(pr0, prk) and np.array_equal(t0.view(np.uint32), tk.view(np.uint32)), key
+        assert ck["rays"] == c0["rays"]
+    nodes = {k: v[1]["nodes"] / v[1]["rays"] for k, v in res.items()}
+    print("nodes per ray:", nodes)
+    assert nodes[0, 0] < 0.7 * nodes[1, 0]
+    assert nodes[0, 32] < 0.8 * nodes[0, 0]
+    assert nodes[1, 32] < 0.8 * nodes[1, 0]

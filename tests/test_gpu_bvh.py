@@ -1,4 +1,5 @@
-"""The device BVH as built on the GPU (PLOC and LBVH topologies).
+"""The device BVH as built on the GPU (PLOC and LBVH topologies, with and without the
+insertion passes that follow the build).
 
 Structure: a binary tree over all triangles, root 0; the nodes reachable from the root
 are distinct and their leaves (one to eight triangles in consecutive slots) hold every
@@ -77,11 +78,14 @@ def check_tree(be, mesh):
     return nodes, len(order), len(leaves)
 
 
+@pytest.mark.parametrize("passes", [0, 32], ids=["built", "reinserted"])
 @pytest.mark.parametrize("leaf", [1, 4, 8])
 @pytest.mark.parametrize("builder", [0, 1], ids=["ploc", "lbvh"])
-def test_device_bvh_contains_padded_triangles(product_lib, builder, leaf):
+def test_device_bvh_contains_padded_triangles(product_lib, builder, leaf, passes):
+    """Each topology as built and after the insertion passes (hsr_set_bvh_optimize)."""
     product_lib.hsr_set_bvh_builder(builder)
     product_lib.hsr_set_bvh_leaf_size(leaf)
+    product_lib.hsr_set_bvh_optimize(passes)
     try:
         for mesh in (scenes.dihedral_mesh(), scenes.sphere_ground_workload(level=3).mesh,
                      scenes.boxes_mesh(seed=3, count=2000)):
@@ -94,6 +98,7 @@ def test_device_bvh_contains_padded_triangles(product_lib, builder, leaf):
     finally:
         product_lib.hsr_set_bvh_builder(0)
         product_lib.hsr_set_bvh_leaf_size(4)
+        product_lib.hsr_set_bvh_optimize(32)
 
 
 @pytest.mark.parametrize("leaf", [1, 8])
