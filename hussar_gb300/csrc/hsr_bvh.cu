@@ -25,6 +25,7 @@
 #include <cub/device/device_select.cuh>
 
 #include <limits>
+#include <vector>
 
 #include "hsr_common.cuh"
 #include "hsr_internal.h"
@@ -977,6 +978,54 @@ static int build_ploc(SceneDev &s, int64_t nt, const int32_t *ids2, const float 
     return rc;
 }
 
+// The reachable nodes renumbered in depth-first order from the root (each node's first
+// child follows it in memory, so a descent reads neighbouring nodes), the nodes inside
+// collapsed leaves dropped: the node array shrinks to the reachable nodes. On the host:
+// one download and one upload of the node array.
+static int renumber_depth_first(SceneDev &s, cudaStream_t st, std::string &err) {
+    const int64_t n = s.node_count;
+    if (n < 2) return 0;
+    std::vector<DNode> h(static_cast<size_t>(n));
+    if (cudaMemcpyAsync(h.data(), s.nodes, sizeof(DNode) * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        err = "BVH layout: node download failed";
+        return 2;
+    }
+    std::vector<int32_t> newid(static_cast<size_t>(n), -1), order, stack{0};
+    order.reserve(size_t(n));
+    while (!stack.empty()) {
+        const int32_t i = stack.back();
+        stack.pop_back();
+        if (i >= n || newid[i] >= 0 || int64_t(order.size()) >= n) {
+            err = "BVH layout: the tree is not a tree";
+            return 2;
+        }
+        newid[i] = int32_t(order.size());
+        order.push_back(i);
+        if (h[i].d.y >= 0) stack.push_back(h[i].d.y);
+        if (h[i].d.x >= 0) stack.push_back(h[i].d.x);
+    }
+    std::vector<DNode> out(order.size());
+    for (size_t k = 0; k < order.size(); ++k) {
+        DNode d = h[order[k]];
+        if (d.d.x >= 0) d.d.x = newid[d.d.x];
+        if (d.d.y >= 0) d.d.y = newid[d.d.y];
+        out[k] = d;
+    }
+    DNode *compact = nullptr;  // the array shrinks to the reachable nodes
+    if (!dev_alloc(&compact, sizeof(DNode) * out.size(), err)) return 3;
+    if (cudaMemcpyAsync(compact, out.data(), sizeof(DNode) * out.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaFree(compact);
+        err = "BVH layout: node upload failed";
+        return 2;
+    }
+    cudaFree(s.nodes);
+    s.nodes = compact;
+    s.node_count = int64_t(out.size());
+    return 0;
+}
+
 // Builds tris/nodes for `scene` from device vertex/index arrays. Returns 0, 2 (CUDA
 // error), 3 (out of memory) or 4 (too many triangles).
 int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, int64_t nt, cudaStream_t st,
@@ -1116,6 +1165,11 @@ int bvh_build(SceneDev &s, const float *d_v, int64_t nv, const int32_t *d_idx, i
         const int lrc = collapse_leaves(s, nt, par_i, par_l, counters, st, err);
         if (lrc) {
             fail(lrc);
+            break;
+        }
+        const int drc = renumber_depth_first(s, st, err);
+        if (drc) {
+            fail(drc);
             break;
         }
         int hd[2];

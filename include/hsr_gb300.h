@@ -177,7 +177,7 @@ hsr_status hsr_scene_rebuild(hsr_scene *scene, const float *vertices, int64_t ve
                              const int32_t *indices, int64_t triangle_count);
 /* Device bytes held by the scene (triangle records and vertex indices, BVH nodes). */
 hsr_status hsr_scene_footprint(const hsr_scene *scene, int64_t *out_bytes);
-/* BVH statistics for tests: node count, maximum depth, leaf count. */
+/* BVH statistics for tests: internal node count, maximum depth, triangle count. */
 hsr_status hsr_scene_bvh_stats(const hsr_scene *scene, int64_t *out_nodes,
                                int32_t *out_max_depth, int64_t *out_leaves);
 
@@ -404,8 +404,9 @@ hsr_status hsr_measure_l2_read(int64_t bytes, int32_t sweeps, double *out_gbs);
 /* Copies the scene's device BVH to the host (tests): out_nodes receives node_count binary
  * nodes of 64 bytes each, both child boxes and child references (layout in
  * hussar_gb300/csrc/hsr_common.cuh, struct DNode; a negative reference c is a leaf of
- * ((~c) & 7) + 1 triangles in consecutive slots from (~c) >> 3; nodes inside collapsed
- * leaves stay in the array, unreachable), out_tris triangle_count 48-byte records
+ * ((~c) & 7) + 1 triangles in consecutive slots from (~c) >> 3; the nodes are stored depth
+ * first from the root, node 0, so a node's first child, when internal, is the next node),
+ * out_tris triangle_count 48-byte records
  * {v0.xyz, original id bits, v1-v0, 0, v2-v0, 0} in slot order. Either pointer may be
  * null; capacities are in records. */
 hsr_status hsr_debug_bvh(const hsr_scene *scene, void *out_nodes, int64_t node_capacity, void *out_tris,

@@ -1,9 +1,9 @@
 """The device BVH as built on the GPU (PLOC and LBVH topologies, with and without the
 insertion passes that follow the build).
 
-Structure: a binary tree over all triangles, root 0; the nodes reachable from the root
-are distinct and their leaves (one to eight triangles in consecutive slots) hold every
-triangle slot exactly once. Conservativeness: each stored child box
+Structure: a binary tree over all triangles, root 0, stored depth first; every stored
+node is reachable from the root exactly once and the leaves (one to eight triangles in
+consecutive slots) hold every triangle slot exactly once. Conservativeness: each stored child box
 contains the padded bounding box of every triangle beneath it, with the padding the build
 applies (max|x| * 4e-6 + 1e-6 per axis), so the FP32 slab test cannot reject a box that a
 hit lies in."""
@@ -41,7 +41,7 @@ def leaf_slots(ref):
 def check_tree(be, mesh):
     nt = mesh.triangleCount()
     nodes, tris = be.device_bvh()
-    assert len(tris) == nt and len(nodes) == nt - 1
+    assert len(tris) == nt and 1 <= len(nodes) <= nt - 1
     child = nodes["child"]
     lo, hi = child_boxes(nodes)
     tlo, thi = padded_boxes(mesh, tris)
@@ -55,8 +55,11 @@ def check_tree(be, mesh):
                 stack.append(int(c))
             else:
                 seen_slots.extend(leaf_slots(c))
-    # every reachable internal node once, every triangle slot in exactly one leaf
-    assert len(set(order)) == len(order)
+    # every stored node reachable once (depth-first layout: a node's first child, when
+    # internal, is the next node), every triangle slot in exactly one leaf
+    assert len(set(order)) == len(order) == len(nodes)
+    first = child[:, 0]
+    assert np.array_equal(first[first >= 0], np.nonzero(first >= 0)[0] + 1)
     assert np.array_equal(np.sort(np.array(seen_slots)), np.arange(nt))
     sub_lo = np.zeros((nt - 1, 3), np.float32)
     sub_hi = np.zeros((nt - 1, 3), np.float32)
