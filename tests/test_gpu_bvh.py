@@ -132,3 +132,34 @@ def test_single_triangle_scene(product_lib):
     assert st["leaves"] == 1 and st["nodes"] == 1
     t, p, n, prim = be.intersect(np.array([[0.2, 0.2, 1.0]], np.float32), np.array([[0, 0, -1.0]], np.float32))
     assert prim[0] == 0 and t[0] == np.float32(1.0)
+
+
+@pytest.mark.parametrize("nt", [4, 5, 9, 33])
+def test_insertion_passes_on_small_and_degenerate_scenes(product_lib, nt):
+    """Trees of a handful of triangles, and a scene of repeated, zero-area and far-away
+    triangles: after the insertion passes the tree is complete and conservative, and ray
+    queries answer as on the tree as built."""
+    rng = np.random.default_rng(nt)
+    if nt == 33:
+        tri = np.repeat(rng.uniform(-1, 1, (1, 3, 3)), 12, axis=0)            # 12 copies of one triangle
+        flat = rng.uniform(-1, 1, (12, 1, 3)) * np.array([[[1.0], [0.5], [0.25]]])  # collinear: zero area
+        far = rng.uniform(-1, 1, (9, 3, 3)) + np.array([1e4, 0, -3e3])         # far from the rest
+        tri = np.concatenate([tri, flat, far]).astype(np.float32)
+    else:
+        tri = rng.uniform(-1, 1, (nt, 3, 3)).astype(np.float32)
+    mesh = TriangleMesh()
+    mesh.append(tri.reshape(-1, 3), np.arange(3 * nt, dtype=np.int32).reshape(-1, 3))
+    o = rng.uniform(-2, 2, (4000, 3)).astype(np.float32)
+    d = rng.normal(size=(4000, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    res = {}
+    try:
+        for passes in (0, 32):
+            product_lib.hsr_set_bvh_optimize(passes)
+            be = gb300.Backend(mesh, None)
+            check_tree(be, mesh)
+            res[passes] = be.intersect(o, d)
+    finally:
+        product_lib.hsr_set_bvh_optimize(32)
+    for a, b in zip(res[0], res[32]):
+        assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
