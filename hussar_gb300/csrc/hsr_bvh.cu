@@ -547,13 +547,15 @@ __global__ void __launch_bounds__(128) k_reins_search(int total, int m, const in
     const Box bn = rbox[n];
     const float an = box_area(bn);
     // best-first branch and bound over the detached tree; a node's key is the area its
-    // ancestors grow by when n goes below them (the induced cost)
+    // ancestors grow by when n goes below them (the induced cost). Only a place whose
+    // insertion cost is below -drem - min_gain saves more than min_gain: that is the
+    // starting bound, so a subtree already well placed ends its search at once.
     float hk[kReinsHeap];
     int hv[kReinsHeap];
     int hs = 1;
     hk[0] = 0.f;
     hv[0] = 0;
-    float best = __int_as_float(0x7f800000);
+    float best = -drem - min_gain;
     int bx = -1;
     for (int pops = 0; hs > 0 && pops < kReinsPops; ++pops) {
         const float ic0 = hk[0];
@@ -601,7 +603,7 @@ __global__ void __launch_bounds__(128) k_reins_search(int total, int m, const in
         }
     }
     const float gain = -(drem + best);
-    if (bx >= 0 && gain > min_gain) {
+    if (bx >= 0 && gain > min_gain) {  // bx >= 0 already means gain > min_gain, up to rounding
         mv_x[n] = bx;
         mv_gain[n] = gain;
     }
