@@ -13,14 +13,17 @@
 //        Surface-area-driven like an SAH build, robust to large overlapping triangles.
 //      LBVH: binary radix tree from the sorted codes (Karras 2012, k_karras) and a
 //        bottom-up box refit (k_refit).
-//   6. leaves: a bottom-up surface-area cost pass turns subtrees of at most the leaf size
+//   6. insertion passes (up to 32, hsr_set_bvh_optimize): every subtree is re-placed in
+//      parallel where the surface-area cost falls most (k_reins_*, below)
+//   7. leaves: a bottom-up surface-area cost pass turns subtrees of at most the leaf size
 //      (default 4, hsr_set_bvh_leaf_size) into leaves when testing their triangles is
 //      cheaper than visiting their nodes (k_leaf_cost); the triangle records are reordered so that every
 //      leaf's triangles are contiguous (k_leaf_group, radix sort, k_permute_tris) and
 //      the links of the remaining nodes rewritten (k_relink).
+//   8. the reachable nodes renumbered depth first and the array shrunk to them (host).
 // Node i stores the boxes of both its children; node 0 is the root. A child reference
 // c >= 0 is an internal node; c < 0 a leaf of ((~c) & 7) + 1 triangles from slot
-// (~c) >> 3. Nodes inside a collapsed subtree stay in the array, unreachable.
+// (~c) >> 3. A node's first child, when internal, is node i + 1.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_select.cuh>
 
