@@ -36,9 +36,10 @@
  *   - 3-term reductions (dot, squaredNorm, 3x3 mat-vec rows) are x0 + (x1 + x2)
  *   - v.normalized() is v / sqrt(squaredNorm)
  *   - cross() of complex vectors conjugates the result
- * Embree (absent) is replaced by a binned-SAH BVH with a Moller-Trumbore triangle
+ * Embree (absent) is replaced by a BVH of its own (PLOC clustering, leaves of up to 4
+ * triangles; a binned-SAH build as the fallback) with a Moller-Trumbore triangle
  * test; hits are accepted for tnear < t <= tfar, equal-t ties go to the lower
- * primitive id. Parity with Embree/OptiX/Eigen themselves is unpinned.
+ * primitive id, so the answers do not depend on the tree. Parity with Embree/OptiX/Eigen themselves is unpinned.
  *
  * Build: oracle/Makefile (g++ -O3 -ffp-contract=off, no -march: the same bits on
  * x86-64 and aarch64).
@@ -488,6 +489,11 @@ struct Scene {
     Bvh bvh;
 };
 
+static bool build_bvh_ploc(Scene &s, const std::vector<float> &lo, const std::vector<float> &hi,
+                           const std::vector<float> &cen);
+static void build_bvh_sah(Scene &s, const std::vector<float> &lo, const std::vector<float> &hi,
+                          const std::vector<float> &cen);
+
 static void build_bvh(Scene &s) {
     const int64_t nt = s.mesh.nt;
     std::vector<float> lo(3 * nt), hi(3 * nt), cen(3 * nt);
@@ -509,6 +515,22 @@ static void build_bvh(Scene &s) {
     s.bvh.prims.resize(nt);
     for (int64_t i = 0; i < nt; ++i) s.bvh.prims[i] = int32_t(i);
     s.bvh.nodes.clear();
+    if (!build_bvh_ploc(s, lo, hi, cen)) {
+        s.bvh.nodes.clear();
+        for (int64_t i = 0; i < nt; ++i) s.bvh.prims[i] = int32_t(i);
+        build_bvh_sah(s, lo, hi, cen);
+    }
+    s.bvh.tv.resize(size_t(9) * nt);
+    for (int64_t i = 0; i < nt; ++i)
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) s.bvh.tv[9 * i + 3 * k + a] = s.mesh.v[3 * s.mesh.f[3 * s.bvh.prims[i] + k] + a];
+}
+
+// Top-down binned SAH (32 bins on the axis of largest centroid extent, the median where
+// no split separates): the fallback of build_bvh_ploc.
+static void build_bvh_sah(Scene &s, const std::vector<float> &lo, const std::vector<float> &hi,
+                          const std::vector<float> &cen) {
+    const int64_t nt = s.mesh.nt;
     s.bvh.nodes.reserve(2 * std::max<int64_t>(nt, 1));
     struct Task {
         int32_t node, first, count;
@@ -646,10 +668,174 @@ static void build_bvh(Scene &s) {
         stack.push_back({l, tk.first, mid - tk.first});
         stack.push_back({l + 1, mid, tk.first + tk.count - mid});
     }
-    s.bvh.tv.resize(size_t(9) * nt);
-    for (int64_t i = 0; i < nt; ++i)
-        for (int k = 0; k < 3; ++k)
-            for (int a = 0; a < 3; ++a) s.bvh.tv[9 * i + 3 * k + a] = s.mesh.v[3 * s.mesh.f[3 * s.bvh.prims[i] + k] + a];
+}
+
+// Parallel locally-ordered clustering (Meister and Bittner 2018) over the Morton order of
+// the centroids (21 bits per axis): each cluster finds, within 64 positions, the one whose
+// merged box has the smallest surface area (ties: the lower position), mutual pairs
+// merge, repeat; the searches run on all host threads. Subtrees of at most 4 triangles
+// then become leaves, in the node layout the traversal reads (children at left and
+// left + 1). A tree deeper than 100 levels (the traversal stack holds 128 entries) or a
+// pass that merges nothing returns false, and build_bvh falls back to build_bvh_sah.
+static bool build_bvh_ploc(Scene &s, const std::vector<float> &lo, const std::vector<float> &hi,
+                           const std::vector<float> &cen) {
+    const int64_t nt = s.mesh.nt;
+    if (nt < 8 || nt >= (int64_t(1) << 30)) return false;
+    float cl[3], ch[3];
+    for (int a = 0; a < 3; ++a) {
+        cl[a] = std::numeric_limits<float>::infinity();
+        ch[a] = -cl[a];
+    }
+    for (int64_t t = 0; t < nt; ++t)
+        for (int a = 0; a < 3; ++a) {
+            cl[a] = std::min(cl[a], cen[3 * t + a]);
+            ch[a] = std::max(ch[a], cen[3 * t + a]);
+        }
+    std::vector<std::pair<uint64_t, int32_t>> key(static_cast<size_t>(nt));
+    for (int64_t t = 0; t < nt; ++t) {
+        uint64_t code = 0;
+        for (int a = 0; a < 3; ++a) {
+            const float ext = ch[a] - cl[a];
+            float u = ext > 0.f ? (cen[3 * t + a] - cl[a]) / ext : 0.5f;
+            u = std::min(std::max(u, 0.f), 1.f);
+            const uint64_t q = uint64_t(std::min(u * 2097152.f, 2097151.f));
+            for (int b = 0; b < 21; ++b) code |= ((q >> b) & 1u) << (3 * b + a);
+        }
+        key[size_t(t)] = {code, int32_t(t)};
+    }
+    std::sort(key.begin(), key.end());
+    struct PNode {  // a merge: children (>= 0 merge index, < 0 ~triangle), box, triangles
+        int32_t c[2];
+        float lo[3], hi[3];
+        int32_t count;
+    };
+    std::vector<PNode> pn;
+    pn.reserve(size_t(nt));
+    std::vector<int32_t> id(static_cast<size_t>(nt));
+    std::vector<float> box(static_cast<size_t>(6 * nt));
+    for (int64_t i = 0; i < nt; ++i) {
+        const int32_t t = key[size_t(i)].second;
+        id[size_t(i)] = ~t;
+        for (int a = 0; a < 3; ++a) {
+            box[6 * i + a] = lo[3 * size_t(t) + a];
+            box[6 * i + 3 + a] = hi[3 * size_t(t) + a];
+        }
+    }
+    auto merged_area = [&](const float *a, const float *b) {
+        const float dx = std::max(a[3], b[3]) - std::min(a[0], b[0]);
+        const float dy = std::max(a[4], b[4]) - std::min(a[1], b[1]);
+        const float dz = std::max(a[5], b[5]) - std::min(a[2], b[2]);
+        return dx * dy + dy * dz + dz * dx;
+    };
+    const int R = 64;
+    const int threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<int32_t> nearest;
+    while (id.size() > 1) {
+        const int64_t n = int64_t(id.size());
+        nearest.assign(size_t(n), -1);
+        std::vector<std::thread> pool;
+        for (int w = 0; w < threads; ++w)
+            pool.emplace_back([&, w] {
+                const int64_t a = n * w / threads, b = n * (w + 1) / threads;
+                for (int64_t i = a; i < b; ++i) {
+                    float best = std::numeric_limits<float>::infinity();
+                    int64_t bj = -1;
+                    for (int64_t j = std::max<int64_t>(0, i - R); j <= std::min<int64_t>(n - 1, i + R); ++j) {
+                        if (j == i) continue;
+                        const float ar = merged_area(&box[6 * i], &box[6 * j]);
+                        if (ar < best) {
+                            best = ar;
+                            bj = j;
+                        }
+                    }
+                    nearest[size_t(i)] = int32_t(bj);
+                }
+            });
+        for (auto &th : pool) th.join();
+        std::vector<int32_t> nid;
+        std::vector<float> nbox;
+        nid.reserve(size_t(n));
+        nbox.reserve(size_t(6) * n);
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t j = nearest[size_t(i)];
+            const bool mutual = j >= 0 && nearest[size_t(j)] == i;
+            if (mutual && i > j) continue;  // merged by j
+            if (mutual) {
+                PNode m;
+                m.c[0] = id[size_t(i)];
+                m.c[1] = id[size_t(j)];
+                m.count = (m.c[0] < 0 ? 1 : pn[size_t(m.c[0])].count) + (m.c[1] < 0 ? 1 : pn[size_t(m.c[1])].count);
+                for (int a = 0; a < 3; ++a) {
+                    m.lo[a] = std::min(box[6 * i + a], box[6 * j + a]);
+                    m.hi[a] = std::max(box[6 * i + 3 + a], box[6 * j + 3 + a]);
+                }
+                pn.push_back(m);
+                nid.push_back(int32_t(pn.size() - 1));
+                for (int a = 0; a < 3; ++a) nbox.push_back(m.lo[a]);
+                for (int a = 0; a < 3; ++a) nbox.push_back(m.hi[a]);
+            } else {
+                nid.push_back(id[size_t(i)]);
+                for (int a = 0; a < 6; ++a) nbox.push_back(box[6 * i + a]);
+            }
+        }
+        if (int64_t(nid.size()) == n) return false;
+        id.swap(nid);
+        box.swap(nbox);
+    }
+    // the node layout: a subtree of at most 4 triangles is a leaf, its triangles gathered
+    // in order; otherwise two consecutive nodes for the children
+    struct Task {
+        int32_t ref, node, depth;
+    };
+    std::vector<Task> stack{{id[0], 0, 0}};
+    s.bvh.nodes.assign(1, BNode{});
+    int32_t filled = 0;
+    std::vector<int32_t> gather;
+    while (!stack.empty()) {
+        const Task tk = stack.back();
+        stack.pop_back();
+        if (tk.depth > 100) return false;
+        BNode nd;
+        const int32_t cnt = tk.ref < 0 ? 1 : pn[size_t(tk.ref)].count;
+        if (tk.ref < 0) {
+            const int32_t t = ~tk.ref;
+            for (int a = 0; a < 3; ++a) {
+                nd.lo[a] = lo[3 * size_t(t) + a];
+                nd.hi[a] = hi[3 * size_t(t) + a];
+            }
+        } else {
+            for (int a = 0; a < 3; ++a) {
+                nd.lo[a] = pn[size_t(tk.ref)].lo[a];
+                nd.hi[a] = pn[size_t(tk.ref)].hi[a];
+            }
+        }
+        if (cnt <= 4) {
+            gather.assign(1, tk.ref);
+            nd.left = filled;
+            nd.count = cnt;
+            while (!gather.empty()) {
+                const int32_t r = gather.back();
+                gather.pop_back();
+                if (r < 0) {
+                    s.bvh.prims[size_t(filled++)] = ~r;
+                } else {
+                    gather.push_back(pn[size_t(r)].c[1]);
+                    gather.push_back(pn[size_t(r)].c[0]);
+                }
+            }
+            s.bvh.nodes[size_t(tk.node)] = nd;
+            continue;
+        }
+        const int32_t l = int32_t(s.bvh.nodes.size());
+        s.bvh.nodes.push_back(BNode{});
+        s.bvh.nodes.push_back(BNode{});
+        nd.left = l;
+        nd.count = 0;
+        s.bvh.nodes[size_t(tk.node)] = nd;
+        stack.push_back({pn[size_t(tk.ref)].c[1], l + 1, tk.depth + 1});
+        stack.push_back({pn[size_t(tk.ref)].c[0], l, tk.depth + 1});
+    }
+    return filled == nt;
 }
 
 // Moller-Trumbore in precision R. Accepts tnear < t <= tfar.
